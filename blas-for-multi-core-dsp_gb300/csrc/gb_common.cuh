@@ -1,0 +1,99 @@
+// gb_common.cuh -- shared helpers of the GB300 BLAS library (host + device).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbblas.h"
+
+namespace gb {
+
+// ------------------------------------------------------------- status
+// Records the status of the calling host thread (thread-local) and returns it.
+gb_status set_status(gb_status st, const char *fmt, ...);
+gb_status ok();
+gb_status cuda_status(cudaError_t e, const char *where);
+
+#define GB_CHECK_ARG(cond, ...)                                                \
+    do {                                                                       \
+        if (!(cond)) return ::gb::set_status(GB_ERR_INVALID_ARG, __VA_ARGS__); \
+    } while (0)
+
+#define GB_CUDA_TRY(expr)                                                      \
+    do {                                                                       \
+        cudaError_t _e = (expr);                                               \
+        if (_e != cudaSuccess) return ::gb::cuda_status(_e, #expr);            \
+    } while (0)
+
+// Launch-error check after a kernel launch (asynchronous errors surface on
+// the next synchronising call, as usual for CUDA).
+#define GB_LAUNCH_CHECK(what)                                                  \
+    do {                                                                       \
+        ::gb::count_launch();                                                  \
+        cudaError_t _e = cudaGetLastError();                                   \
+        if (_e != cudaSuccess) return ::gb::cuda_status(_e, what);             \
+    } while (0)
+
+// Kernel launches issued by the library (all host threads).
+void count_launch();
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+// Opt-in shared memory per block (bytes) of the current device.
+int smem_optin();
+
+// Device-wide scratch owned by the library, grown on demand (per device,
+// guarded by a mutex).  Returns nullptr and sets GB_ERR_OOM on failure.
+// The buffer stays valid until the next call that needs more; callers use it
+// stream-ordered on one stream at a time.
+void *workspace(size_t bytes, void *stream);
+
+// Per-device error word (4 bytes of device memory, zero = no error) that
+// kernels with bounded waits set on timeout; gb_sync() reports and clears it.
+int *error_word();
+
+inline bool is_trans(char t) { return t == 'T' || t == 't'; }
+inline bool is_mode(char t) { return t == 'N' || t == 'n' || t == 'T' || t == 't'; }
+
+// Counter-based generator (identical to the oracle's gbo_* functions).
+__host__ __device__ inline uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace gb
+
+// ------------------------------------------------------------- launchers
+// Internal kernel entry points (one per .cu file), called by the dispatchers.
+namespace gb {
+
+struct GemmArgs {
+    bool ta, tb;
+    int64_t M, N, K;
+    const void *A; int64_t lda;
+    const void *B; int64_t ldb;
+    void *C; int64_t ldc;
+    double alpha, beta;
+    int semantics;   // gb_semantics
+    int k_block, k_slab, alpha_on_b;
+    cudaStream_t stream;
+};
+
+gb_status launch_gemm_ordered_f64(const GemmArgs &g);
+gb_status launch_gemm_ordered_f32(const GemmArgs &g);
+gb_status launch_sgemm_simt(const GemmArgs &g);
+gb_status launch_dgemm_dmma(const GemmArgs &g);
+gb_status launch_sgemm_bf16x3(const GemmArgs &g);
+gb_status launch_dgemm_ozaki(const GemmArgs &g, int slices);
+gb_status launch_skinny_f32(const GemmArgs &g);
+gb_status launch_skinny_f64(const GemmArgs &g);
+// C = beta*C (beta==0: C = 0) or C = C + beta (scalar) epilogue-only path (K == 0)
+gb_status launch_gemm_k0_f32(const GemmArgs &g);
+gb_status launch_gemm_k0_f64(const GemmArgs &g);
+
+}  // namespace gb

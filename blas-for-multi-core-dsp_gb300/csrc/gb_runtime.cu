@@ -1,0 +1,253 @@
+// gb_runtime.cu -- status codes, device queries, library workspace, memory
+// helpers and the seeded input generator.
+//
+// Replaces the parts of the MT-3000 host runtime the reference's host demos
+// use (hthread_dev_open / hthread_malloc / hthread_free,
+// sgemm_release_V1.3.2/host_code/sgemm_demo.c:50-61, :338-351) with plain
+// CUDA runtime calls.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <atomic>
+#include <mutex>
+
+#include "gb_common.cuh"
+
+namespace gb {
+
+static thread_local int t_status = GB_OK;
+static thread_local char t_msg[512] = "";
+
+gb_status set_status(gb_status st, const char *fmt, ...) {
+    t_status = st;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_msg, sizeof(t_msg), fmt, ap);
+    va_end(ap);
+    return st;
+}
+
+gb_status ok() { return GB_OK; }
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+gb_status cuda_status(cudaError_t e, const char *where) {
+    return set_status(GB_ERR_CUDA, "%s: %s (%s)", where, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+static const int kMaxDev = 64;
+
+int sm_count() {
+    static int cache[kMaxDev] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDev) return 148;
+    if (cache[dev] == 0) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = n > 0 ? n : 148;
+    }
+    return cache[dev];
+}
+
+int smem_optin() {
+    static int cache[kMaxDev] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDev) return 227 * 1024;
+    if (cache[dev] == 0) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cache[dev] = n > 0 ? n : 227 * 1024;
+    }
+    return cache[dev];
+}
+
+static std::mutex g_ws_mu;
+static void *g_ws_ptr[kMaxDev] = {nullptr};
+static size_t g_ws_size[kMaxDev] = {0};
+
+void *workspace(size_t bytes, void *stream) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDev) {
+        set_status(GB_ERR_INVALID_ARG, "workspace: device ordinal %d out of range", dev);
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    if (g_ws_size[dev] >= bytes && g_ws_ptr[dev]) return g_ws_ptr[dev];
+    if (g_ws_ptr[dev]) {
+        // the old buffer may still be in use by work queued on any stream
+        cudaDeviceSynchronize();
+        cudaFree(g_ws_ptr[dev]);
+        g_ws_ptr[dev] = nullptr;
+        g_ws_size[dev] = 0;
+    }
+    size_t want = bytes < (size_t(64) << 20) ? (size_t(64) << 20) : bytes;
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_status(GB_ERR_OOM, "workspace: cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+        return nullptr;
+    }
+    (void)stream;
+    g_ws_ptr[dev] = p;
+    g_ws_size[dev] = want;
+    return p;
+}
+
+static int *g_err_word[kMaxDev] = {nullptr};
+
+int *error_word() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDev) return nullptr;
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    if (!g_err_word[dev]) {
+        int *p = nullptr;
+        if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        cudaMemset(p, 0, sizeof(int));
+        g_err_word[dev] = p;
+    }
+    return g_err_word[dev];
+}
+
+// -------------------------------------------------------------- generator
+template <typename T>
+__global__ void fill_kernel(T *X, int64_t rows, int64_t cols, int64_t ld, uint64_t seed, int kind) {
+    const uint64_t s = mix64(seed);
+    const uint64_t s2 = mix64(seed ^ 0x5851F42D4C957F2DULL);
+    const int64_t total = rows * cols;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t idx = (uint64_t)i;
+        uint64_t b = mix64(s + (idx + 1) * 0x9E3779B97F4A7C15ULL);
+        double u = (double)(b >> 11) * 0x1.0p-53;
+        double v;
+        if (kind == 1) {
+            v = u;
+        } else {
+            v = 2.0 * u - 1.0;
+            if (kind == 2) {
+                uint64_t be = mix64(s2 + (idx + 1) * 0x9E3779B97F4A7C15ULL);
+                int e = (int)(be % 41ULL) - 20;
+                v = ldexp(v, e);
+            }
+        }
+        int64_t r = i / cols, c = i - r * cols;
+        X[r * ld + c] = (T)v;
+    }
+}
+
+template <typename T>
+static gb_status fill(T *X, int64_t rows, int64_t cols, int64_t ld, uint64_t seed, int kind, void *stream) {
+    GB_CHECK_ARG(rows >= 0 && cols >= 0, "fill: negative size");
+    GB_CHECK_ARG(ld >= cols, "fill: ld (%lld) < cols (%lld)", (long long)ld, (long long)cols);
+    GB_CHECK_ARG(kind >= 0 && kind <= 2, "fill: kind %d not in 0..2", kind);
+    if (rows == 0 || cols == 0) return ok();
+    GB_CHECK_ARG(X != nullptr, "fill: null pointer");
+    int64_t total = rows * cols;
+    int blocks = (int)(total / 256 + 1 < (int64_t)sm_count() * 16 ? total / 256 + 1 : (int64_t)sm_count() * 16);
+    fill_kernel<T><<<blocks, 256, 0, as_stream(stream)>>>(X, rows, cols, ld, seed, kind);
+    GB_LAUNCH_CHECK("fill_kernel");
+    return ok();
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+const char *gb_status_string(int status) {
+    switch (status) {
+        case GB_OK: return "GB_OK";
+        case GB_ERR_INVALID_ARG: return "GB_ERR_INVALID_ARG";
+        case GB_ERR_UNSUPPORTED: return "GB_ERR_UNSUPPORTED";
+        case GB_ERR_OOM: return "GB_ERR_OOM";
+        case GB_ERR_DEVICE_TIMEOUT: return "GB_ERR_DEVICE_TIMEOUT";
+        case GB_ERR_CUDA: return "GB_ERR_CUDA";
+        case GB_ERR_NO_DEVICE: return "GB_ERR_NO_DEVICE";
+        default: return "GB_ERR_UNKNOWN";
+    }
+}
+
+int gb_get_last_status(void) { return t_status; }
+const char *gb_last_error(void) { return t_msg; }
+void gb_clear_last_status(void) {
+    t_status = GB_OK;
+    t_msg[0] = 0;
+}
+
+int gb_version(void) { return 100; }
+
+uint64_t gb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int gb_device_arch(void) {
+    int dev = 0, maj = 0, min = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaDeviceGetAttribute(&maj, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&min, cudaDevAttrComputeCapabilityMinor, dev);
+    return maj * 10 + min;
+}
+
+gb_status gb_sync(void *stream) {
+    GB_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < kMaxDev && g_err_word[dev]) {
+        int code = 0;
+        GB_CUDA_TRY(cudaMemcpy(&code, g_err_word[dev], sizeof(int), cudaMemcpyDeviceToHost));
+        if (code != 0) {
+            cudaMemset(g_err_word[dev], 0, sizeof(int));
+            return set_status(GB_ERR_DEVICE_TIMEOUT, "a device-side wait gave up (code %d)", code);
+        }
+    }
+    return ok();
+}
+
+gb_status gb_malloc(void **ptr, size_t bytes) {
+    GB_CHECK_ARG(ptr != nullptr, "gb_malloc: null out-pointer");
+    *ptr = nullptr;
+    if (bytes == 0) return ok();
+    cudaError_t e = cudaMalloc(ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_status(GB_ERR_OOM, "gb_malloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return ok();
+}
+
+gb_status gb_free(void *ptr) {
+    if (ptr) GB_CUDA_TRY(cudaFree(ptr));
+    return ok();
+}
+
+gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int kind, void *stream) {
+    GB_CHECK_ARG(kind >= 0 && kind <= 2, "gb_memcpy: kind %d not in 0..2", kind);
+    if (bytes == 0) return ok();
+    GB_CHECK_ARG(dst && src, "gb_memcpy: null pointer");
+    cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost
+                                                                      : cudaMemcpyDeviceToDevice;
+    GB_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, k, as_stream(stream)));
+    return ok();
+}
+
+gb_status gb_fill_f64(double *X, int64_t rows, int64_t cols, int64_t ld, uint64_t seed, int kind, void *stream) {
+    return fill<double>(X, rows, cols, ld, seed, kind, stream);
+}
+
+gb_status gb_fill_f32(float *X, int64_t rows, int64_t cols, int64_t ld, uint64_t seed, int kind, void *stream) {
+    return fill<float>(X, rows, cols, ld, seed, kind, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+// gemm_api.cu -- gb_sgemm / gb_dgemm: argument checks, semantics and the
+// per-shape choice of kernel.
+//
+// Covers the reference entry points sgemm_{NN,NT,TN,TT}_qxx
+// (sgemm_release_V1.3.2/include/sgemm_kernel.h:11-22), dgemm_{NN,NT,TN,TT}
+// (dgemm_release_V1.1/include/dgemm_kernel.h:39-60) and the irregular
+// irr_{shortA,thinB}_{s,d}gemm_* (irr_*_kernel.h:11-22) behind one BLAS-style
+// call; the transpose mode picks operand layouts, not separate drivers.
+#include <string.h>
+
+#include "gb_common.cuh"
+
+namespace gb {
+namespace {
+
+// C = beta*C (BLAS) / C = beta (scalar) / C = C + beta when K == 0.
+template <typename T>
+__global__ void k0_kernel(T *C, int64_t M, int64_t N, int64_t ldc, T beta, int semantics) {
+    const int64_t total = M * N;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t m = e / N, n = e - m * N;
+        T *cp = C + m * ldc + n;
+        if (semantics == GB_SEM_BLAS)
+            *cp = (beta == T(0)) ? T(0) : beta * *cp;
+        else if (semantics == GB_SEM_SCALAR_BETA)
+            *cp = T(0) + beta;
+        else
+            *cp = *cp + (T(0) + beta);
+    }
+}
+
+template <typename T>
+gb_status k0(const GemmArgs &g) {
+    if (g.M == 0 || g.N == 0) return ok();
+    int64_t total = g.M * g.N;
+    int blocks = (int)(ceil_div(total, 256) < 8 * sm_count() ? ceil_div(total, 256) : 8 * sm_count());
+    k0_kernel<T><<<blocks, 256, 0, g.stream>>>((T *)g.C, g.M, g.N, g.ldc, (T)g.beta, g.semantics);
+    GB_LAUNCH_CHECK("k0_kernel");
+    return ok();
+}
+
+int pick(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
+    (void)ta; (void)tb;
+    const int64_t small = M < N ? M : N;
+    const int64_t large = M < N ? N : M;
+    if (small <= 64 && large >= 4 * small && large >= 1024) return GB_ALGO_SKINNY;
+    if (bits == 64) return GB_ALGO_ORDERED;   // FP64-pipe bound either way; bit-exact
+    (void)K;
+    return GB_ALGO_SIMT;
+}
+
+template <typename T>
+gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alpha, const T *A, int64_t lda,
+               const T *B, int64_t ldb, T beta, T *C, int64_t ldc, const gb_gemm_opts *opts) {
+    gb_gemm_opts o;
+    if (opts) o = *opts; else gb_gemm_opts_init(&o);
+    const char *fn = sizeof(T) == 8 ? "gb_dgemm" : "gb_sgemm";
+    GB_CHECK_ARG(is_mode(transA) && is_mode(transB), "%s: transA/transB must be 'N' or 'T'", fn);
+    GB_CHECK_ARG(M >= 0 && N >= 0 && K >= 0, "%s: negative dimension", fn);
+    const bool ta = is_trans(transA), tb = is_trans(transB);
+    const int64_t arows = ta ? K : M, acols = ta ? M : K;
+    const int64_t brows = tb ? N : K, bcols = tb ? K : N;
+    GB_CHECK_ARG(lda >= (acols > 1 ? acols : 1), "%s: lda (%lld) < %lld", fn, (long long)lda, (long long)acols);
+    GB_CHECK_ARG(ldb >= (bcols > 1 ? bcols : 1), "%s: ldb (%lld) < %lld", fn, (long long)ldb, (long long)bcols);
+    GB_CHECK_ARG(ldc >= (N > 1 ? N : 1), "%s: ldc (%lld) < N (%lld)", fn, (long long)ldc, (long long)N);
+    GB_CHECK_ARG(o.semantics >= 0 && o.semantics <= 2, "%s: unknown semantics %d", fn, o.semantics);
+    GB_CHECK_ARG(o.algo >= 0 && o.algo <= 6, "%s: unknown algo %d", fn, o.algo);
+    GB_CHECK_ARG(o.k_block >= 0 && o.k_slab >= 0, "%s: negative k_block/k_slab", fn);
+    if (M == 0 || N == 0) return ok();
+    GB_CHECK_ARG(C != nullptr, "%s: C is null", fn);
+    if (K > 0) GB_CHECK_ARG(A != nullptr && B != nullptr, "%s: A or B is null", fn);
+    (void)arows; (void)brows;
+
+    GemmArgs g;
+    g.ta = ta; g.tb = tb; g.M = M; g.N = N; g.K = K;
+    g.A = A; g.lda = lda; g.B = B; g.ldb = ldb; g.C = C; g.ldc = ldc;
+    g.alpha = (double)alpha; g.beta = (double)beta;
+    g.semantics = o.semantics;
+    g.k_block = o.k_block; g.k_slab = o.k_slab; g.alpha_on_b = o.alpha_on_b;
+    g.stream = as_stream(o.stream);
+
+    int algo = o.algo;
+    if (algo == GB_ALGO_AUTO) algo = pick(sizeof(T) * 8, ta, tb, M, N, K);
+    if (algo == GB_ALGO_ORDERED)
+        return sizeof(T) == 8 ? launch_gemm_ordered_f64(g) : launch_gemm_ordered_f32(g);
+    if (K == 0) return k0<T>(g);
+    switch (algo) {
+        case GB_ALGO_SIMT:
+            return sizeof(T) == 8 ? launch_gemm_ordered_f64(g) : launch_sgemm_simt(g);
+        case GB_ALGO_DMMA:
+            if (sizeof(T) != 8) return set_status(GB_ERR_UNSUPPORTED, "gb_sgemm: DMMA is an FP64 algorithm");
+            return launch_dgemm_dmma(g);
+        case GB_ALGO_BF16X3:
+            if (sizeof(T) != 4) return set_status(GB_ERR_UNSUPPORTED, "gb_dgemm: BF16X3 is an FP32 algorithm");
+            return launch_sgemm_bf16x3(g);
+        case GB_ALGO_OZAKI: {
+            if (sizeof(T) != 8) return set_status(GB_ERR_UNSUPPORTED, "gb_sgemm: OZAKI is an FP64 algorithm");
+            int s = o.ozaki_slices;
+            GB_CHECK_ARG(s == 0 || (s >= 2 && s <= 8), "gb_dgemm: ozaki_slices %d not in 2..8", s);
+            return launch_dgemm_ozaki(g, s);
+        }
+        case GB_ALGO_SKINNY:
+            return sizeof(T) == 8 ? launch_skinny_f64(g) : launch_skinny_f32(g);
+        default:
+            return set_status(GB_ERR_UNSUPPORTED, "%s: algo %d", fn, algo);
+    }
+}
+
+}  // namespace
+}  // namespace gb
+
+extern "C" {
+
+void gb_gemm_opts_init(gb_gemm_opts *opts) {
+    if (!opts) return;
+    memset(opts, 0, sizeof(*opts));
+    opts->algo = GB_ALGO_AUTO;
+    opts->semantics = GB_SEM_BLAS;
+}
+
+int gb_gemm_pick_algo(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K) {
+    return gb::pick(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K);
+}
+
+gb_status gb_sgemm(char transA, char transB, int64_t M, int64_t N, int64_t K, float alpha, const float *A,
+                   int64_t lda, const float *B, int64_t ldb, float beta, float *C, int64_t ldc,
+                   const gb_gemm_opts *opts) {
+    return gb::gemm<float>(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, opts);
+}
+
+gb_status gb_dgemm(char transA, char transB, int64_t M, int64_t N, int64_t K, double alpha, const double *A,
+                   int64_t lda, const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
+                   const gb_gemm_opts *opts) {
+    return gb::gemm<double>(transA, transB, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, opts);
+}
+
+}  // extern "C"

@@ -1,0 +1,227 @@
+"""gbblas -- Python binding of libgbblas.so, the GB300 (sm_103a) BLAS hot path.
+
+A thin ctypes layer over the C ABI in include/gbblas.h and
+include/gbblas_ref.h.  Device buffers are passed as torch CUDA tensors or as
+raw device addresses (int).  There is no CPU fallback: if libgbblas.so is
+missing or no sm_103 device is present the calls raise.
+
+    import gbblas
+    gbblas.sgemm('N', 'T', M, N, K, 1.5, A, lda, B, ldb, -0.5, C, ldc,
+                 algo=gbblas.ALGO_BF16X3)
+"""
+import ctypes
+import os
+import re
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.dirname(_HERE)
+_REPO = os.path.dirname(_PKG)
+LIB_PATH = os.path.join(_HERE, "libgbblas.so")
+INCLUDE_DIR = os.path.join(_REPO, "include")
+
+# gb_status
+OK, ERR_INVALID_ARG, ERR_UNSUPPORTED, ERR_OOM, ERR_DEVICE_TIMEOUT, ERR_CUDA, ERR_NO_DEVICE = range(7)
+# gb_algo
+ALGO_AUTO, ALGO_ORDERED, ALGO_SIMT, ALGO_DMMA, ALGO_BF16X3, ALGO_OZAKI, ALGO_SKINNY = range(7)
+ALGO_NAMES = {0: "auto", 1: "ordered", 2: "simt", 3: "dmma", 4: "bf16x3", 5: "ozaki", 6: "skinny"}
+# gb_semantics
+SEM_BLAS, SEM_SCALAR_BETA, SEM_ACCUM_SCALAR_BETA = range(3)
+# gb_stencil_order
+STENCIL_HOST, STENCIL_SCALAR, STENCIL_VECTOR = range(3)
+
+
+class GBError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_status_name(status), msg))
+        self.status = status
+
+
+def _status_name(st):
+    return {0: "GB_OK", 1: "GB_ERR_INVALID_ARG", 2: "GB_ERR_UNSUPPORTED", 3: "GB_ERR_OOM",
+            4: "GB_ERR_DEVICE_TIMEOUT", 5: "GB_ERR_CUDA", 6: "GB_ERR_NO_DEVICE"}.get(st, "GB_ERR_%d" % st)
+
+
+class GemmOpts(ctypes.Structure):
+    _fields_ = [("stream", ctypes.c_void_p), ("algo", ctypes.c_int32), ("semantics", ctypes.c_int32),
+                ("k_block", ctypes.c_int32), ("k_slab", ctypes.c_int32), ("alpha_on_b", ctypes.c_int32),
+                ("ozaki_slices", ctypes.c_int32), ("target_err", ctypes.c_double),
+                ("reserved", ctypes.c_int32 * 4)]
+
+
+_i64, _vp, _int, _dbl, _flt = ctypes.c_int64, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_float
+_ul = ctypes.c_ulong
+_SIGS = {
+    "gb_status_string": ([_int], ctypes.c_char_p),
+    "gb_get_last_status": ([], _int),
+    "gb_last_error": ([], ctypes.c_char_p),
+    "gb_clear_last_status": ([], None),
+    "gb_version": ([], _int),
+    "gb_launch_count": ([], ctypes.c_uint64),
+    "gb_device_arch": ([], _int),
+    "gb_sync": ([_vp], _int),
+    "gb_malloc": ([ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t], _int),
+    "gb_free": ([_vp], _int),
+    "gb_memcpy": ([_vp, _vp, ctypes.c_size_t, _int, _vp], _int),
+    "gb_fill_f64": ([_vp, _i64, _i64, _i64, ctypes.c_uint64, _int, _vp], _int),
+    "gb_fill_f32": ([_vp, _i64, _i64, _i64, ctypes.c_uint64, _int, _vp], _int),
+    "gb_gemm_opts_init": ([ctypes.POINTER(GemmOpts)], None),
+    "gb_sgemm": ([ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, _flt, _vp, _i64, _vp, _i64, _flt, _vp, _i64,
+                  ctypes.POINTER(GemmOpts)], _int),
+    "gb_dgemm": ([ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, _dbl, _vp, _i64, _vp, _i64, _dbl, _vp, _i64,
+                  ctypes.POINTER(GemmOpts)], _int),
+    "gb_gemm_pick_algo": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64], _int),
+    "gb_transpose_f32": ([_i64, _i64, _vp, _i64, _vp, _i64, _vp], _int),
+    "gb_transpose_f64": ([_i64, _i64, _vp, _i64, _vp, _i64, _vp], _int),
+    "gb_stencil2d_f64": ([_i64, _i64, _vp, _vp, _int, _int, _vp], _int),
+    "gb_stencil2d_f32": ([_i64, _i64, _vp, _vp, _int, _int, _vp], _int),
+    "gb_exec": ([ctypes.c_char_p, _int, _int, ctypes.POINTER(_ul)], _int),
+    "gb_ref_set_stream": ([_vp], None),
+    "gb_ref_set_algo": ([_int], None),
+}
+
+_LIB = None
+
+
+def lib():
+    """Load libgbblas.so (raises if it was not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise GBError(ERR_NO_DEVICE, "libgbblas.so not built: run __graft_entry__.build() or "
+                                         "python blas-for-multi-core-dsp_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGS.items():
+            f = getattr(L, name, None)
+            if f is None:
+                continue
+            f.argtypes = args
+            f.restype = res
+        _LIB = L
+    return _LIB
+
+
+def declared_symbols():
+    """Every function name declared in include/*.h."""
+    names = set()
+    for fn in sorted(os.listdir(INCLUDE_DIR)):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(INCLUDE_DIR, fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\([^;{}]*\)\s*;", src):
+            name = m.group(1)
+            if name not in ("if", "while", "for", "return", "sizeof"):
+                names.add(name)
+    return sorted(names)
+
+
+def _check(st, what=""):
+    if st != OK:
+        raise GBError(st, (lib().gb_last_error() or b"").decode() or what)
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError("expected a torch tensor or an int device address, got %r" % type(x))
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream
+
+
+def launch_count():
+    return lib().gb_launch_count()
+
+
+def arch():
+    return lib().gb_device_arch()
+
+
+def sync(stream=None):
+    _check(lib().gb_sync(_stream(stream)))
+
+
+def opts(algo=ALGO_AUTO, semantics=SEM_BLAS, stream=None, k_block=0, k_slab=0, alpha_on_b=0,
+         ozaki_slices=0, target_err=0.0):
+    o = GemmOpts()
+    lib().gb_gemm_opts_init(ctypes.byref(o))
+    o.stream = _stream(stream)
+    o.algo = algo
+    o.semantics = semantics
+    o.k_block = k_block
+    o.k_slab = k_slab
+    o.alpha_on_b = alpha_on_b
+    o.ozaki_slices = ozaki_slices
+    o.target_err = target_err
+    return o
+
+
+def sgemm(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, **kw):
+    o = opts(**kw)
+    _check(lib().gb_sgemm(ta.encode(), tb.encode(), M, N, K, alpha, _ptr(A), lda, _ptr(B), ldb, beta, _ptr(C),
+                          ldc, ctypes.byref(o)), "gb_sgemm")
+
+
+def dgemm(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, **kw):
+    o = opts(**kw)
+    _check(lib().gb_dgemm(ta.encode(), tb.encode(), M, N, K, alpha, _ptr(A), lda, _ptr(B), ldb, beta, _ptr(C),
+                          ldc, ctypes.byref(o)), "gb_dgemm")
+
+
+def gemm(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, dtype_bits, **kw):
+    f = dgemm if dtype_bits == 64 else sgemm
+    f(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, **kw)
+
+
+def pick_algo(bits, ta, tb, M, N, K):
+    return lib().gb_gemm_pick_algo(bits, ta.encode(), tb.encode(), M, N, K)
+
+
+def transpose(M, N, A, lda, B, ldb, bits, stream=None):
+    f = lib().gb_transpose_f64 if bits == 64 else lib().gb_transpose_f32
+    _check(f(M, N, _ptr(A), lda, _ptr(B), ldb, _stream(stream)), "transpose")
+
+
+def stencil2d(M, N, A, B, iters, order=STENCIL_HOST, bits=64, stream=None):
+    f = lib().gb_stencil2d_f64 if bits == 64 else lib().gb_stencil2d_f32
+    _check(f(M, N, _ptr(A), _ptr(B), iters, order, _stream(stream)), "stencil2d")
+
+
+def fill(X, rows, cols, ld, seed, kind=0, bits=64, stream=None):
+    f = lib().gb_fill_f64 if bits == 64 else lib().gb_fill_f32
+    _check(f(_ptr(X), rows, cols, ld, seed & 0xFFFFFFFFFFFFFFFF, kind, _stream(stream)), "fill")
+
+
+def exec_by_name(name, scalars, pointers):
+    """The reference's launch-by-name call: scalars first, then pointers."""
+    vals = [int(s) for s in scalars] + [_ptr(p) for p in pointers]
+    arr = (_ul * len(vals))(*vals)
+    _check(lib().gb_exec(name.encode(), len(scalars), len(pointers), arr), "gb_exec " + name)
+
+
+def ref_call(name, *args):
+    """Call a reference-named entry point of gbblas_ref.h with plain ints /
+    floats / tensors (pointers by data_ptr).  Returns the recorded status."""
+    f = getattr(lib(), name)
+    cargs = []
+    for a in args:
+        if isinstance(a, float):
+            cargs.append(ctypes.c_float(a))
+        elif isinstance(a, int):
+            cargs.append(ctypes.c_ulong(a))
+        else:
+            cargs.append(ctypes.c_void_p(_ptr(a)))
+    lib().gb_clear_last_status()
+    f.restype = None
+    f(*cargs)
+    return lib().gb_get_last_status()

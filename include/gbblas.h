@@ -1,0 +1,166 @@
+/*
+ * gbblas.h -- C ABI of the GB300 (sm_103a) BLAS hot path.
+ *
+ * A drop-in for the GEMM / transpose / Jacobi path of
+ * VVinstonSmith/BLAS-for-multi-core-DSP.  Conventions follow the reference:
+ * row-major storage, OFFSET(row, col, ld) = row*ld + col; an operand used
+ * transposed is stored transposed (op(A) = A^T means A is a K x M buffer,
+ * lda >= M).  All pointers are device pointers (cudaMalloc, cudaMallocManaged
+ * or any device-visible allocation) unless a function says otherwise.  The
+ * library never frees caller memory.
+ *
+ * Calls are stream-ordered and asynchronous on the stream given (NULL: the
+ * legacy default stream); gb_sync() waits for a stream.  Every entry point
+ * returns a gb_status; the reference-named wrappers (gbblas_ref.h) return
+ * void, as the reference does, and record their status for
+ * gb_get_last_status().  Status and error text are per host thread.
+ *
+ * Plain pointers and integers only: no CUDA or torch types in signatures.
+ */
+#ifndef GBBLAS_H
+#define GBBLAS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status */
+typedef enum gb_status {
+    GB_OK = 0,
+    GB_ERR_INVALID_ARG = 1,    /* bad size, leading dimension, pointer, mode */
+    GB_ERR_UNSUPPORTED = 2,    /* valid request this build cannot run        */
+    GB_ERR_OOM = 3,            /* device allocation failed / over budget      */
+    GB_ERR_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up          */
+    GB_ERR_CUDA = 5,           /* CUDA runtime error (text in gb_last_error)  */
+    GB_ERR_NO_DEVICE = 6       /* no usable sm_103 device                     */
+} gb_status;
+
+const char *gb_status_string(int status);
+/* Status and message of the last failing call on this host thread. */
+int         gb_get_last_status(void);
+const char *gb_last_error(void);
+void        gb_clear_last_status(void);
+
+/* Library version and the device it runs on (major*10+minor, e.g. 103). */
+int gb_version(void);
+int gb_device_arch(void);
+
+/* Kernel launches the library has issued so far (all threads). */
+uint64_t gb_launch_count(void);
+
+/* Stream-ordered completion; NULL = legacy default stream. */
+gb_status gb_sync(void *stream);
+
+/* Device memory helpers (cudaMalloc / cudaFree / cudaMemcpy wrappers) so a
+ * C caller needs no CUDA headers.  kind: 0 host->device, 1 device->host,
+ * 2 device->device (asynchronous on `stream`). */
+gb_status gb_malloc(void **ptr, size_t bytes);
+gb_status gb_free(void *ptr);
+gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int kind, void *stream);
+
+/* ------------------------------------------------------------ inputs */
+/* Seeded counter-based generator (bit-identical to the oracle's): element
+ * (r,c) of a rows x cols matrix (leading dimension ld) gets f(seed, r*cols+c).
+ * kind 0: U[-1,1], 1: U[0,1], 2: ldexp(U[-1,1], e) with e ~ U{-20..20}. */
+gb_status gb_fill_f64(double *X, int64_t rows, int64_t cols, int64_t ld, uint64_t seed, int kind, void *stream);
+gb_status gb_fill_f32(float *X, int64_t rows, int64_t cols, int64_t ld, uint64_t seed, int kind, void *stream);
+
+/* ------------------------------------------------------------- GEMM */
+typedef enum gb_algo {
+    GB_ALGO_AUTO = 0,     /* pick per shape and dtype                          */
+    GB_ALGO_ORDERED = 1,  /* the reference's summation order, bit-exact         */
+    GB_ALGO_SIMT = 2,     /* plain FP32 FFMA / FP64 DFMA register tiles         */
+    GB_ALGO_DMMA = 3,     /* FP64 tensor pipe (mma.sync m8n8k4 f64)             */
+    GB_ALGO_BF16X3 = 4,   /* SGEMM as hi*hi+hi*lo+lo*hi BF16 on tcgen05, FP32 acc */
+    GB_ALGO_OZAKI = 5,    /* DGEMM from exact integer slices on tensor cores    */
+    GB_ALGO_SKINNY = 6    /* tiny M (shortA) / tiny N (thinB) streaming kernels */
+} gb_algo;
+
+typedef enum gb_semantics {
+    /* C = alpha*op(A)op(B) + beta*C (BLAS; beta == 0: C is not read).  With
+     * alpha == beta == 1 and GB_ALGO_ORDERED this is the reference DGEMM /
+     * irregular V0.0 update C += op(A)op(B) in its order. */
+    GB_SEM_BLAS = 0,
+    /* C = alpha*op(A)op(B) + beta, beta a scalar added to every element, C not
+     * read (sgemm_release_V1.3.2, irr_thinB_sgemm_release_V1.2). */
+    GB_SEM_SCALAR_BETA = 1,
+    /* C = C + alpha*op(A)op(B) + beta (sgemm_release_V1.3.1). */
+    GB_SEM_ACCUM_SCALAR_BETA = 2
+} gb_semantics;
+
+typedef struct gb_gemm_opts {
+    void   *stream;        /* cudaStream_t; NULL = legacy default stream       */
+    int32_t algo;          /* gb_algo                                          */
+    int32_t semantics;     /* gb_semantics                                     */
+    int32_t k_block;       /* ORDERED: outer K block (reference K_G), 0 -> 512  */
+    int32_t k_slab;        /* ORDERED: inner K slab (K_A, three-level sum of
+                              irr_thinB_sgemm V1.2), 0 -> two-level sum        */
+    int32_t alpha_on_b;    /* ORDERED: alpha pre-scales op(B) (thinB V1.2)
+                              instead of op(A) (sgemm V1.3.x)                  */
+    int32_t ozaki_slices;  /* OZAKI: slices per operand (2..8), 0 -> from
+                              target_err                                      */
+    double  target_err;    /* OZAKI: normwise error target, 0 -> 2^-52         */
+    int32_t reserved[4];
+} gb_gemm_opts;
+
+/* Fill *opts with defaults (AUTO, BLAS, NULL stream). */
+void gb_gemm_opts_init(gb_gemm_opts *opts);
+
+/* transA/transB: 'N' or 'T' (case-insensitive).  Shapes: op(A) is M x K,
+ * op(B) is K x N, C is M x N.  lda >= (transA=='N' ? K : M),
+ * ldb >= (transB=='N' ? N : K), ldc >= N.  M, N or K == 0 is valid
+ * (K == 0 still applies beta).  opts may be NULL. */
+gb_status gb_sgemm(char transA, char transB, int64_t M, int64_t N, int64_t K,
+                   float alpha, const float *A, int64_t lda, const float *B, int64_t ldb,
+                   float beta, float *C, int64_t ldc, const gb_gemm_opts *opts);
+gb_status gb_dgemm(char transA, char transB, int64_t M, int64_t N, int64_t K,
+                   double alpha, const double *A, int64_t lda, const double *B, int64_t ldb,
+                   double beta, double *C, int64_t ldc, const gb_gemm_opts *opts);
+
+/* Algorithm that GB_ALGO_AUTO picks for a shape (for logging/tests). */
+int gb_gemm_pick_algo(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K);
+
+/* ------------------------------------------------------ transpose */
+/* B (N x M, ldb >= M) = A^T, A is M x N (lda >= N).  Bit-exact copy.
+ * Replaces transpose/device_code/kernel.c:2002 transpose_float_32x32_dbuf
+ * and :1167 transpose_16x16_dbuf, and dgemm_kernel.c:974 transpose_A2B. */
+gb_status gb_transpose_f32(int64_t M, int64_t N, const float *A, int64_t lda, float *B, int64_t ldb, void *stream);
+gb_status gb_transpose_f64(int64_t M, int64_t N, const double *A, int64_t lda, double *B, int64_t ldb, void *stream);
+
+/* -------------------------------------------------------- stencil */
+typedef enum gb_stencil_order {
+    GB_STENCIL_HOST = 0,   /* ((((top+left)+right)+down)+middle)*0.2 (matrix_stencil.c:45)  */
+    GB_STENCIL_SCALAR = 1, /* 0.2*((((top+middle)+down)+left)+right) (kernel_stencil.c:70)  */
+    GB_STENCIL_VECTOR = 2  /* row-parity add tree of micro_kernel_cross_reduce_V3          */
+} gb_stencil_order;
+
+/* `iters` 5-point Jacobi sweeps on (M+2) x (N+2) padded grids A and B
+ * (row stride N+2), ping-ponging: sweep 1 reads A writes B, sweep 2 reads B
+ * writes A, ...  Halo cells are never written (Dirichlet boundary: set it in
+ * both buffers).  The result is in B when iters is odd, in A when even;
+ * the interior of the other buffer is scratch (sweeps are fused several per
+ * launch, so it holds some earlier sweep, not necessarily iters-1).
+ * iters == 1 is the reference stencil_vector(M, N, A, B)
+ * (stencil_2d_V1.2/device_code/kernel_stencil.c:1042).  Bit-exact for the
+ * chosen order. */
+gb_status gb_stencil2d_f64(int64_t M, int64_t N, double *A, double *B, int iters, int order, void *stream);
+gb_status gb_stencil2d_f32(int64_t M, int64_t N, float *A, float *B, int iters, int order, void *stream);
+
+/* --------------------------------------------------- launch by name */
+/* The reference host drives the device by kernel name with packed
+ * arguments: hthread_group_exec(tg, "launch_sgemm_NN", n_scalar, n_ptr, args)
+ * (sgemm_release_V1.3.2/host_code/sgemm_demo.c:144), scalars first then
+ * pointers.  gb_exec runs the named reference kernel with the same packing
+ * (names and argument lists of the reference launchers and device entries:
+ * launch_dgemm_XX, launch_sgemm_XX, launch_irr_{shortA,thinB}_{s,d}gemm_XX,
+ * transpose_float_32x32_dbuf, transpose_16x16_dbuf, stencil_vector, *_null)
+ * and waits for it, as hthread_group_exec + hthread_group_wait do. */
+gb_status gb_exec(const char *name, int n_scalar, int n_ptr, const unsigned long *args);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,106 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol declared
+in include/*.h, and rejects bad arguments on the host before any device
+work (status codes + messages)."""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+import gbblas
+
+
+@pytest.fixture(scope="module")
+def L():
+    if not os.path.exists(gbblas.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    return gbblas.lib()
+
+
+def test_exports_every_declared_symbol(L):
+    names = gbblas.declared_symbols()
+    assert "gb_sgemm" in names and "dgemm_NN" in names and "stencil_vector" in names
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", gbblas.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if l.strip()}
+    assert set(names) <= exported, sorted(set(names) - exported)
+
+
+def test_status_strings(L):
+    assert L.gb_status_string(0) == b"GB_OK"
+    assert L.gb_status_string(1) == b"GB_ERR_INVALID_ARG"
+    assert L.gb_version() >= 100
+
+
+def _sgemm(L, ta="N", tb="N", M=4, N=4, K=4, lda=4, ldb=4, ldc=4, A=8, B=8, C=8, **kw):
+    o = gbblas.opts(**kw)
+    return L.gb_sgemm(ta.encode(), tb.encode(), M, N, K, 1.0, A, lda, B, ldb, 0.0, C, ldc, ctypes.byref(o))
+
+
+@pytest.mark.parametrize("kw,frag", [
+    (dict(ta="X"), "transA"),
+    (dict(M=-1), "negative"),
+    (dict(lda=3), "lda"),
+    (dict(ta="T", M=8, lda=4), "lda"),
+    (dict(ldb=3), "ldb"),
+    (dict(tb="T", K=8, lda=8, ldb=4), "ldb"),
+    (dict(ldc=3), "ldc"),
+    (dict(C=None), "C is null"),
+    (dict(A=None), "A or B is null"),
+    (dict(semantics=7), "semantics"),
+    (dict(algo=42), "algo"),
+])
+def test_gemm_rejects_bad_arguments(L, kw, frag):
+    st = _sgemm(L, **kw)
+    assert st == gbblas.ERR_INVALID_ARG
+    assert frag in L.gb_last_error().decode()
+
+
+def test_gemm_empty_is_ok_without_device(L):
+    assert _sgemm(L, M=0) == gbblas.OK
+    assert _sgemm(L, N=0, A=None, B=None, C=None) == gbblas.OK
+
+
+def test_dgemm_rejects_bad_arguments(L):
+    o = gbblas.opts()
+    st = L.gb_dgemm(b"N", b"N", 4, 4, 4, 1.0, 8, 2, 8, 4, 0.0, 8, 4, ctypes.byref(o))
+    assert st == gbblas.ERR_INVALID_ARG and b"lda" in L.gb_last_error()
+    o = gbblas.opts(algo=gbblas.ALGO_OZAKI, ozaki_slices=11)
+    st = L.gb_dgemm(b"N", b"N", 4, 4, 4, 1.0, 8, 4, 8, 4, 0.0, 8, 4, ctypes.byref(o))
+    assert st == gbblas.ERR_INVALID_ARG and b"ozaki_slices" in L.gb_last_error()
+
+
+def test_transpose_and_stencil_reject_bad_arguments(L):
+    assert L.gb_transpose_f32(4, 5, 8, 4, 16, 4, None) == gbblas.ERR_INVALID_ARG   # lda < N
+    assert L.gb_transpose_f64(4, 5, 8, 5, 16, 3, None) == gbblas.ERR_INVALID_ARG   # ldb < M
+    assert L.gb_transpose_f32(4, 5, 8, 5, 8, 4, None) == gbblas.ERR_INVALID_ARG    # in place
+    assert L.gb_transpose_f32(0, 5, None, 5, None, 0, None) == gbblas.OK
+    assert L.gb_stencil2d_f64(4, 4, 8, 16, 1, 5, None) == gbblas.ERR_INVALID_ARG   # order
+    assert L.gb_stencil2d_f64(4, 4, 8, 8, 1, 0, None) == gbblas.ERR_INVALID_ARG    # A == B
+    assert L.gb_stencil2d_f64(4, 4, 8, 16, -1, 0, None) == gbblas.ERR_INVALID_ARG
+    assert L.gb_stencil2d_f32(4, 4, 8, 16, 0, 0, None) == gbblas.OK                # no sweeps
+    assert L.gb_fill_f32(8, 2, 2, 2, 1, 3, None) == gbblas.ERR_INVALID_ARG         # kind
+
+
+def test_exec_rejects_unknown_names_and_bad_packing(L):
+    arr = (ctypes.c_ulong * 10)(*range(10))
+    assert L.gb_exec(b"launch_nothing_NN", 7, 3, arr) == gbblas.ERR_INVALID_ARG
+    assert L.gb_exec(b"launch_dgemm_NN", 6, 3, arr) == gbblas.ERR_INVALID_ARG      # needs 7 scalars
+    assert L.gb_exec(b"launch_dgemm_TN", 7, 3, arr) == gbblas.ERR_INVALID_ARG      # TN needs 8
+    assert L.gb_exec(b"launch_sgemm_NX", 4, 3, arr) == gbblas.ERR_INVALID_ARG
+    assert L.gb_exec(b"launch_dgemm_null", 7, 3, arr) == gbblas.OK                 # no-op kernels
+    assert L.gb_exec(b"stencil_vector", 1, 2, arr) == gbblas.ERR_INVALID_ARG
+
+
+def test_null_kernels_are_noops(L):
+    assert gbblas.ref_call("sgemm_null", 4, 4, 4, 0, 0, 0, 0, 1.0, 1.0) == gbblas.OK
+    assert gbblas.ref_call("stencil_null", 4, 4, 0, 0) == gbblas.OK
+
+
+def test_auto_algorithm_choice(L):
+    assert gbblas.pick_algo(32, "N", "N", 262144, 8, 4096) == gbblas.ALGO_SKINNY
+    assert gbblas.pick_algo(64, "T", "T", 16, 262144, 4096) == gbblas.ALGO_SKINNY
+    assert gbblas.pick_algo(64, "N", "N", 512, 512, 512) == gbblas.ALGO_ORDERED
+    assert gbblas.pick_algo(32, "N", "N", 4096, 4096, 4096) != gbblas.ALGO_SKINNY
