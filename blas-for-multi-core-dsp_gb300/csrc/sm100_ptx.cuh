@@ -157,6 +157,18 @@ __device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t smem_addr) {
     return d;
 }
 
+// Same, 64-byte swizzle: rows of 64 B (32 BF16), 8-row groups 512 B apart,
+// layout type 4 = SWIZZLE_64B.
+__device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t smem_addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((smem_addr & 0x3FFFF) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(512 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)4 << 61;
+    return d;
+}
+
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
 // N >> 3 at bits 17-22, M >> 4 at bits 24-28.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {

@@ -3,8 +3,13 @@
 * Small-integer inputs: the hi/lo split is exact and every partial sum is an
   integer below 2^24, so the result must equal the exact product bit for
   bit -- this pins the TMA / UMMA descriptor layouts and the TMEM epilogue.
-* U[-1,1] inputs: normwise error against the Dot2 oracle <= 2*K*u32.
+* U[-1,1] inputs: normwise error against the Dot2 oracle <= 2*K*u32 plus
+  the split's own representation error: hi + lo keeps ~16 of FP32's 24
+  bits, so each product carries up to ~3 * 2^-17 relative error however
+  small K is (below K ~ 12 that exceeds 2*K*u32 alone).
 """
+
+SPLIT_ERR = 3 * 2.0 ** -17
 import numpy as np
 import pytest
 
@@ -28,7 +33,8 @@ def _ints(rows, cols, seed, ld=None):
 
 
 @pytest.mark.parametrize("mode", MODES)
-@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (256, 512, 192), (130, 300, 70), (7, 9, 5)])
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (256, 512, 192), (130, 300, 70), (7, 9, 5), (1030, 2050, 96),
+                                   (2048, 4096, 64)])
 def test_bf16x3_exact_on_integers(torch, mode, M, N, K):
     import gbblas
     ta, tb = mode
@@ -64,7 +70,9 @@ def test_bf16x3_normwise(torch, mode, M, N, K, pad):
     cols = np.arange(0, N, max(1, N // 97))
     err, _ = oracle.normwise_error(got, ta, tb, M, N, K, 1.5, A, ac + pad, B, bc + pad, -0.5, C0, N + pad,
                                    rows, cols)
-    assert err <= 2 * K * 2.0 ** -24, err
+    assert err <= 2 * K * 2.0 ** -24 + SPLIT_ERR, err
+    if K >= 64:
+        assert err <= 2 * K * 2.0 ** -24, err
     # columns beyond N (the ld padding) are untouched
     if pad:
         assert np.array_equal(got[:, N:], C0[:, N:])
