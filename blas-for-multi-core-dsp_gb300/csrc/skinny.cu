@@ -206,3 +206,120 @@ gb_status launch_skinny_f32(const GemmArgs &g) { return dispatch<float>(g); }
 gb_status launch_skinny_f64(const GemmArgs &g) { return dispatch<double>(g); }
 
 }  // namespace gb
+
+// ---------------------------------------------------------------------------
+// gb_sgemm_skinny_noalloc: the FP32 skinny GEMM for callers that cannot
+// allocate device memory on the call path.  It is the same two kernels with
+// the same split-K plan as the GB_ALGO_SKINNY path above, but the split-K
+// partial sums live in a fixed array of device memory reserved when the
+// library is loaded, so the call itself never calls cudaMalloc / cudaFree or
+// any allocating routine.
+#include <mutex>
+
+namespace gb {
+namespace {
+
+// Size of the fixed split-K scratch.  Every GPU that loads the library keeps
+// this array until the process exits.
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;   // 16 MiB
+
+static __device__ __align__(256) unsigned char g_skinny_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxNoAllocDev = 64;
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_addr[kMaxNoAllocDev] = {nullptr};
+
+// Device address of the scratch array on the current device.  In host code
+// the array's name is only a host-side stand-in, so the address is looked
+// up once per device (with that device current) and cached.
+gb_status noalloc_scratch(void **out) {
+    int dev = -1;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxNoAllocDev)
+        return set_status(GB_ERR_UNSUPPORTED, "gb_sgemm_skinny_noalloc: device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_skinny_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) return cuda_status(e, "cudaGetSymbolAddress(skinny no-alloc scratch)");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return ok();
+}
+
+// Mirrors run<float, NB, R>() above with the static scratch in place of the
+// library workspace.  Every partial the reduce kernel reads is written by the
+// first kernel of the same call, so nothing has to be cleared between calls.
+template <int NB, int R>
+gb_status run_noalloc(SkParams p, cudaStream_t st) {
+    constexpr int BR = NT * R;
+    const int64_t rtiles = ceil_div(p.rows, BR);
+    if (rtiles > 0x7fffffff) return set_status(GB_ERR_UNSUPPORTED, "gb_sgemm_skinny_noalloc: too many rows");
+    const int64_t target = 2 * (int64_t)sm_count();
+    int splits = 1;
+    while (rtiles * splits < target && p.K / (splits * 2) >= 256 && splits < 64) splits *= 2;
+    constexpr int BK = SkTile<float, R>::BK;
+    p.kchunk = ceil_div(ceil_div(p.K, splits), BK) * BK;
+    p.splits = (int)ceil_div(p.K, p.kchunk);
+    if (p.splits < 1) p.splits = 1;
+    if (p.splits > 1) {
+        const size_t bytes = (size_t)p.splits * p.rows * NB * sizeof(float);
+        if (bytes > kNoAllocScratchBytes)
+            return set_status(GB_ERR_INVALID_ARG,
+                              "gb_sgemm_skinny_noalloc: %d-way split-K over %lld rows needs %zu bytes of scratch, "
+                              "more than the fixed %zu bytes",
+                              p.splits, (long long)p.rows, bytes, kNoAllocScratchBytes);
+        void *s = nullptr;
+        gb_status stt = noalloc_scratch(&s);
+        if (stt != GB_OK) return stt;
+        p.part = s;
+    }
+    dim3 grid((unsigned)rtiles, (unsigned)p.splits);
+    skinny_kernel<float, NB, R><<<grid, NT, 0, st>>>(p);
+    GB_LAUNCH_CHECK("skinny_kernel (no-alloc)");
+    if (p.splits > 1) {
+        int blocks = (int)(ceil_div(p.rows * p.n, 256) < 4 * sm_count() ? ceil_div(p.rows * p.n, 256) : 4 * sm_count());
+        skinny_reduce_kernel<float, NB><<<blocks, 256, 0, st>>>(p);
+        GB_LAUNCH_CHECK("skinny_reduce_kernel (no-alloc)");
+    }
+    return ok();
+}
+
+}  // namespace
+}  // namespace gb
+
+extern "C" gb_status gb_sgemm_skinny_noalloc(char transA, char transB, int64_t M, int64_t N, int64_t K, float alpha,
+                                             const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
+                                             float *C, int64_t ldc, int semantics, void *stream) {
+    using namespace gb;
+    const char *fn = "gb_sgemm_skinny_noalloc";
+    GB_CHECK_ARG(is_mode(transA) && is_mode(transB), "%s: transA/transB must be 'N' or 'T'", fn);
+    GB_CHECK_ARG(M >= 0 && N >= 0 && K >= 0, "%s: negative dimension", fn);
+    GB_CHECK_ARG(semantics >= 0 && semantics <= 2, "%s: unknown semantics %d", fn, semantics);
+    const bool ta = is_trans(transA), tb = is_trans(transB);
+    const int64_t acols = ta ? M : K, bcols = tb ? K : N;
+    GB_CHECK_ARG(lda >= (acols > 1 ? acols : 1), "%s: lda (%lld) < %lld", fn, (long long)lda, (long long)acols);
+    GB_CHECK_ARG(ldb >= (bcols > 1 ? bcols : 1), "%s: ldb (%lld) < %lld", fn, (long long)ldb, (long long)bcols);
+    GB_CHECK_ARG(ldc >= (N > 1 ? N : 1), "%s: ldc (%lld) < N (%lld)", fn, (long long)ldc, (long long)N);
+    if (M == 0 || N == 0) return ok();
+    GB_CHECK_ARG(K > 0, "%s: K must be positive (K == 0 has no product to compute; use gb_sgemm)", fn);
+    GB_CHECK_ARG(A && B && C, "%s: null pointer", fn);
+    SkParams p{};
+    if (N <= M) {
+        p.rows = M; p.X = A; p.ldx = lda; p.tx = ta;
+        p.W = B; p.ldw = ldb; p.tw = tb; p.n = (int)(N < 65 ? N : 65);
+        p.cs_r = ldc; p.cs_c = 1;
+    } else {
+        p.rows = N; p.X = B; p.ldx = ldb; p.tx = !tb;
+        p.W = A; p.ldw = lda; p.tw = !ta; p.n = (int)(M < 65 ? M : 65);
+        p.cs_r = 1; p.cs_c = ldc;
+    }
+    GB_CHECK_ARG(p.n <= 64, "%s: min(M, N) must be <= 64 (got M=%lld, N=%lld)", fn, (long long)M, (long long)N);
+    p.K = K; p.C = C; p.alpha = alpha; p.beta = beta; p.semantics = semantics;
+    cudaStream_t st = as_stream(stream);
+    if (p.n <= 8) return run_noalloc<8, 4>(p, st);
+    if (p.n <= 16) return run_noalloc<16, 4>(p, st);
+    if (p.n <= 32) return run_noalloc<32, 2>(p, st);
+    return run_noalloc<64, 1>(p, st);
+}

@@ -120,6 +120,27 @@ gb_status gb_dgemm(char transA, char transB, int64_t M, int64_t N, int64_t K,
                    double alpha, const double *A, int64_t lda, const double *B, int64_t ldb,
                    double beta, double *C, int64_t ldc, const gb_gemm_opts *opts);
 
+/* Skinny FP32 GEMM that allocates no device memory.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc on the call
+ * path -- a serving loop that admits work against a fixed HBM budget, a host
+ * framework whose device memory belongs to its own pool allocator, or code
+ * that must not trigger the device-wide synchronisation cudaFree implies.
+ * It computes exactly what gb_sgemm with GB_ALGO_SKINNY computes (same
+ * kernels, same split-K plan; thinB when N <= M, else shortA), with
+ * min(M, N) <= 64 and K >= 1, but keeps the split-K partial sums in a fixed
+ * 16 MiB array of device memory that every GPU loading the library reserves
+ * until the process exits.  A call whose split-K plan needs more than 16 MiB
+ * (splits x max(M, N) x padded min(M, N) x 4 bytes) is rejected with
+ * GB_ERR_INVALID_ARG before anything runs.  The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the one array: calls that overlap on the GPU (different streams, or
+ * different host threads) race on it and must be serialised by the caller.
+ * `semantics` is a gb_semantics value; `stream` as in gb_gemm_opts. */
+gb_status gb_sgemm_skinny_noalloc(char transA, char transB, int64_t M, int64_t N, int64_t K,
+                                  float alpha, const float *A, int64_t lda, const float *B, int64_t ldb,
+                                  float beta, float *C, int64_t ldc, int semantics, void *stream);
+
 /* Algorithm that GB_ALGO_AUTO picks for a shape (for logging/tests). */
 int gb_gemm_pick_algo(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K);
 
