@@ -1,31 +1,40 @@
-"""Benchmark of the GB300 BLAS hot path on the SGEMM headline workload.
+"""Benchmarks of the GB300 BLAS hot path.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--algo best|bf16x3|simt]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload sgemm|dgemm|thinb|shorta|transpose|jacobi] [options]
 
-Workload (one "step"): SGEMM C = alpha*op(A)op(B) + beta*C, FP32, row-major,
-M = N = K = 4096, leading dimensions padded to 4112, alpha = 1.5,
-beta = -0.5, in all four transpose modes (NN, NT, TN, TT), entries uniform in
-[-1,1] from seed 1 (the project's counter-based generator, on the device).
-Each step runs the four GEMMs; the operands of a step (8 x 67 MB + C) exceed
-the 129 MB L2, so no explicit flush is needed between iterations.
+With no flags it runs the headline workload (the default line):
 
-value   = whole-job TFLOP/s = n_gpus * 4 * 2*M*N*K / (max over ranks of the
-          timed region), inputs resident in HBM;
-e2e     = the same metric through the C ABI with host buffers: each GEMM's
-          A, B, C are copied host->device (pinned memory, gb_memcpy), computed,
-          and C is copied back, all inside the timed region;
-roofline: the GEMM kernel's achieved TFLOP/s (2*M*N*K per launch / the mean
-          CUDA-event duration of its launches in the timed region) against
-          the measured peak of its pipe (MEASURED_PEAKS.json);
-cpu_baseline: the reference's host SGEMM loop (the oracle's restatement of
-          sgemm_release_V1.3.2/host_code/sgemm_demo.c:214-242) on a bounded
-          sample of rows, with every host core.
-Multi-GPU: replicas (each rank runs the same workload; no collective on the
-data path), "scaling": "weak".
+sgemm   SGEMM C = alpha*op(A)op(B) + beta*C, FP32, row-major, M = N = K = 4096,
+        leading dimensions 4112, alpha 1.5, beta -0.5, all four transpose modes,
+        entries U[-1,1] from seed 1 (generated on the device by gb_fill_f32).
+        One step = the four GEMMs with the best algorithm (3xBF16 on tcgen05);
+        the plain FFMA kernel is timed beside it, and each algorithm's
+        normwise error against the Dot2 oracle is reported.
+
+Other workloads (one JSON line each, same contract):
+dgemm     M = N = K = 8192 FP64, NN and TT, alpha = beta = 1, entries u*2^e
+          (u ~ U[-1,1], e ~ U{-20..20}, seed 3): Ozaki slices vs native FP64,
+          TFLOP/s and normwise error on a seeded 1024 x 1024 subgrid.
+thinb     M = 262144, K = 4096, N in {8,16,32,64} (--n), FP32 or FP64 (--bits),
+          all four modes, U[-1,1] seed 2: HBM GB/s, bytes = s(MK + KN + 2MN).
+shorta    the mirror: M in {8..64}, K = 4096, N = 262144.
+transpose 30000 x 17000, FP32 or FP64: HBM GB/s, bytes = 2*M*N*s.
+jacobi    8192 x 8192 interior, boundary 1.0, interior U[0,1] seed 2, 200 sweeps,
+          FP32 or FP64: algorithmic GB/s = 2*M*N*s per sweep.
+
+value is the whole-job figure over all ranks (replicas: each rank runs the same
+workload, no collective on the data path; "scaling": "weak"), timed with CUDA
+events on the launching stream between a barrier + synchronize on both sides,
+max over ranks.  e2e repeats the metric through the C ABI with host (pinned)
+buffers, host<->device copies inside the timed region.  Inputs of every
+workload exceed the 129 MB L2.  cpu_baseline times the oracle's port of the
+reference host loop on a bounded sample with every host core.
 """
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -40,11 +49,7 @@ for _p in (REPO, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "TFLOP/s (emulated vs plain FP64/FP32) at matched error; serve p50/p99, req/s"
-M = N = K = 4096
-LD = 4112
-ALPHA, BETA = 1.5, -0.5
 MODES = ("NN", "NT", "TN", "TT")
-FLOPS_PER_GEMM = 2.0 * M * N * K
 
 
 def log(*a):
@@ -54,18 +59,15 @@ def log(*a):
 def measured_peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
-            p = json.load(f)
-        return p, "measured"
+            return json.load(f), "measured"
     except (OSError, ValueError):
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
 def profile_traffic(name):
-    """DRAM bytes per launch recorded from an ncu capture in profiles/<name>.txt
-    (a line 'traffic_bytes_per_launch: <int>'), else None."""
-    path = os.path.join(REPO, "profiles", name + ".txt")
+    """DRAM bytes per launch from profiles/<name>.txt ('traffic_bytes_per_launch: N'), else None."""
     try:
-        for line in open(path):
+        for line in open(os.path.join(REPO, "profiles", name + ".txt")):
             if line.startswith("traffic_bytes_per_launch:"):
                 return int(float(line.split(":", 1)[1].strip()))
     except OSError:
@@ -73,24 +75,25 @@ def profile_traffic(name):
     return None
 
 
+FP32_SIMT_PEAK = 152 * 128 * 2 * 2.07e9 / 1e12       # nominal FFMA TFLOP/s
+FP64_PEAK = 1.25                                      # nominal FP64 TFLOP/s (GB300)
+
+
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    """nvidia-smi samples of SM clock and throttle reasons during a timed region."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
-        self.proc = None
-        self.lines = []
+        self.index, self.proc, self.lines = index, None, []
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
 
@@ -126,284 +129,712 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-# ------------------------------------------------------------- CPU legs
-def cpu_reference_sample(max_seconds=12.0):
-    """The reference's host SGEMM loop (oracle restatement) on a bounded sample
-    of C rows, all four modes; returns (TFLOP/s, threads, description)."""
+# ================================================================== context
+class Ctx:
+    def __init__(self, args):
+        import torch
+        import gbblas
+        self.args = args
+        self.torch, self.gb = torch, gbblas
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(self.local)
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("nccl")
+            self.dist = dist
+        gbblas.lib()
+        arch = gbblas.arch()
+        if arch != 103:
+            raise SystemExit("bench.py: needs an sm_103 GPU (found sm_%d)" % arch)
+        self.dev = torch.device("cuda", self.local)
+        self.stream = torch.cuda.current_stream(self.dev)
+        self.peaks, self.peak_src = measured_peaks()
+
+    def event(self):
+        return self.torch.cuda.Event(enable_timing=True)
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+        self.torch.cuda.synchronize()
+
+    def max_over_ranks(self, ms):
+        if not self.dist:
+            return ms
+        t = self.torch.tensor([ms], device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(self, step, steps, per_launch=None):
+        """Run `steps` steps between barriers; returns (elapsed ms max over ranks,
+        mean ms of the launches recorded by per_launch, clocks, launch count)."""
+        sampler = ClockSampler(self.local)
+        self.barrier()
+        sampler.start()
+        time.sleep(0.25)
+        l0 = self.gb.launch_count()
+        t0, t1 = self.event(), self.event()
+        evs = []
+        t0.record(self.stream)
+        for _ in range(steps):
+            step(evs)
+        t1.record(self.stream)
+        self.torch.cuda.synchronize()
+        launches = self.gb.launch_count() - l0
+        clocks = sampler.stop()
+        ms = self.max_over_ranks(t0.elapsed_time(t1))
+        kms = statistics.mean(a.elapsed_time(b) for a, b in evs) if evs else None
+        return ms, kms, clocks, int(launches)
+
+    def finish(self, line):
+        if self.dist:
+            self.dist.barrier()
+            self.dist.destroy_process_group()
+        if self.rank == 0:
+            print(json.dumps(line), flush=True)
+
+
+def base_line(ctx, metric, value, unit, ms, steps, dtype, config, hib=True):
+    return {"metric": metric, "value": value, "unit": unit, "n_gpus": ctx.world, "steps": steps,
+            "warmup": ctx.args.warmup, "ms_per_step": ms / steps, "higher_is_better": hib, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config}
+
+
+def memcpy(ctx, dst, src, nbytes, kind):
+    st = ctx.gb.lib().gb_memcpy(ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src.data_ptr()), nbytes, kind,
+                                ctypes.c_void_p(ctx.stream.cuda_stream))
+    assert st == 0, ctx.gb.lib().gb_last_error()
+
+
+def e2e_measure(ctx, step_host, steps, flops_or_bytes, unit_div):
+    """Time step_host() (copies + compute through the C ABI) `steps` times."""
+    step_host()
+    ctx.torch.cuda.synchronize()
+    ctx.barrier()
+    t0, t1 = ctx.event(), ctx.event()
+    t0.record(ctx.stream)
+    for _ in range(steps):
+        h2d, d2h = step_host()
+    t1.record(ctx.stream)
+    ctx.torch.cuda.synchronize()
+    ms = ctx.max_over_ranks(t0.elapsed_time(t1))
+    return ctx.world * steps * flops_or_bytes / (ms * 1e-3) / unit_div, h2d, d2h
+
+
+# ================================================================== CPU legs
+def cpu_sgemm_sample(max_seconds=10.0):
     import numpy as np
     import oracle
-
+    M = N = K = 4096
+    LD = 4112
     nt = os.cpu_count() or 1
     oracle.set_threads(nt)
     A = oracle.fill(M, K, 11, dtype=np.float32, ld=LD)
     B = oracle.fill(K, N, 12, dtype=np.float32, ld=LD)
     rows = 8
     while True:
-        flops, secs = 0.0, 0.0
+        flops = secs = 0.0
         for mode in MODES:
-            ta, tb = mode
             Cs = np.zeros((rows, LD), dtype=np.float32)
             t0 = time.perf_counter()
-            # rows of C: op(A) restricted to `rows` rows (TN/TT read A^T storage: same bytes pattern)
-            oracle.sgemm_ref(ta, tb, rows, N, K, ALPHA, A, LD, B, LD, BETA, Cs, LD)
+            oracle.sgemm_ref(mode[0], mode[1], rows, N, K, 1.5, A, LD, B, LD, -0.5, Cs, LD)
             secs += time.perf_counter() - t0
             flops += 2.0 * rows * N * K
         if secs * 3 > max_seconds or rows >= 256:
             break
         rows *= 2
-    return flops / secs / 1e12, nt, "%d of %d rows of C per mode, 4 modes, K=%d (oracle port of the reference " \
-        "host loop, gcc -O2 -fopenmp, %d threads)" % (rows, M, K, nt)
+    return (flops / secs / 1e12, nt, "%d of %d rows of C per mode, 4 modes, K=%d: oracle port of the reference "
+            "host loop sgemm_demo.c:214-242, gcc -O2 -fopenmp, %d threads" % (rows, M, K, nt))
 
 
-def run_reference_arm(args, rank, world):
-    if rank != 0:
-        return
-    import numpy as np  # noqa: F401
-    nt = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        pass
-    vals = []
-    desc = ""
-    for _ in range(max(1, args.steps)):
-        v, nt, desc = cpu_reference_sample(max_seconds=6.0)
-        vals.append(v)
-    value = statistics.median(vals)
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_dict(world, "reference host loop (CPU)"),
-            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": nt, "kind": "port", "sample": desc},
-            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-
-
-def config_dict(world, algo):
-    return {"workload": "SGEMM 4096^3, ld 4112, alpha 1.5, beta -0.5, NN/NT/TN/TT, U[-1,1] seed 1",
-            "M": M, "N": N, "K": K, "ld": LD, "alpha": ALPHA, "beta": BETA, "modes": list(MODES),
-            "algo": algo, "parallelism": "replicas x%d" % world,
-            "l2": "inputs larger than L2 (8 operand buffers of 67 MB + C per step)"}
-
-
-# ------------------------------------------------------------- GPU leg
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--algo", default="best", choices=["best", "bf16x3", "simt"])
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
-
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-
-    if args.impl == "reference":
-        return run_reference_arm(args, rank, world)
-
+def cpu_dgemm_sample(max_seconds=10.0):
     import numpy as np
-    import torch
+    import oracle
+    n = 8192
+    nt = os.cpu_count() or 1
+    oracle.set_threads(nt)
+    A = oracle.fill(64, n, 31, kind=2)
+    B = oracle.fill(n, n, 32, kind=2)
+    rows = 4
+    while True:
+        C = np.zeros((rows, n))
+        t0 = time.perf_counter()
+        oracle.dgemm_ref("N", "N", rows, n, n, A, n, B, n, C, n)
+        secs = time.perf_counter() - t0
+        if secs * 3 > max_seconds or rows >= 64:
+            break
+        rows *= 2
+    return (2.0 * rows * n * n / secs / 1e12, nt, "%d of 8192 rows of C, NN, K=8192: oracle port of "
+            "dgemm_demo.c:233-252, %d threads (rate extrapolated to the full problem)" % (rows, nt))
 
-    import gbblas
 
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    gbblas.lib()
-    arch = gbblas.arch()
-    if arch != 103:
-        raise SystemExit("bench.py: needs an sm_103 GPU (found sm_%d)" % arch)
+def cpu_bw_sample(kind, bits, max_seconds=8.0):
+    """Reference host loops for the bandwidth workloads on a bounded sample; returns GB/s."""
+    import numpy as np
+    import oracle
+    nt = os.cpu_count() or 1
+    oracle.set_threads(nt)
+    dt = np.float64 if bits == 64 else np.float32
+    s = 8 if bits == 64 else 4
+    if kind == "transpose":
+        M, N = 30000, 4000
+        A = oracle.fill(M, N, 2, dtype=dt)
+        B = np.zeros((N, M), dtype=dt)
+        t0 = time.perf_counter()
+        oracle.transpose_into(M, N, A, N, B, M)
+        secs = time.perf_counter() - t0
+        return 2.0 * M * N * s / secs / 1e9, nt, "30000 x 4000 slice, transpose.c:113-119 loop, %d threads" % nt
+    if kind == "jacobi":
+        M = N = 8192
+        A = np.ones((M + 2, N + 2), dtype=dt)
+        A[1:-1, 1:-1] = oracle.fill(M, N, 2, kind=1, dtype=dt)
+        B = A.copy()
+        t0 = time.perf_counter()
+        oracle.stencil(M, N, A, B, 2, 0)
+        secs = time.perf_counter() - t0
+        return 2 * 2.0 * M * N * s / secs / 1e9, nt, "2 sweeps of 8192^2, matrix_stencil.c:35-48 loop, %d threads" % nt
+    # skinny: thinB rows sample
+    n, K = 8, 4096
+    rows = 2048
+    A = oracle.fill(rows, K, 2, dtype=dt)
+    B = oracle.fill(K, n, 3, dtype=dt)
+    C = np.zeros((rows, n), dtype=dt)
+    t0 = time.perf_counter()
+    if bits == 64:
+        oracle.dgemm_ref("N", "N", rows, n, K, A, K, B, n, C, n)
+    else:
+        oracle.sgemm_irr_ref("N", "N", rows, n, K, A, K, B, n, C, n)
+    secs = time.perf_counter() - t0
+    return (s * (rows * K + K * n + 2 * rows * n) / secs / 1e9, nt,
+            "%d rows of thinB N=8 K=4096, irr demo loop, %d threads" % (rows, nt))
 
-    dev = torch.device("cuda", local)
-    stream = torch.cuda.current_stream(dev)
+
+# ================================================================== workloads
+def run_sgemm(ctx):
+    torch, gb, args = ctx.torch, ctx.gb, ctx.args
+    import numpy as np
+    M = N = K = 4096
+    LD = 4112
+    ALPHA, BETA = 1.5, -0.5
+    flops = 2.0 * M * N * K
     bufs = {}
-    seeds = {"A_N": 11, "A_T": 12, "B_N": 13, "B_T": 14, "C": 15}
-    for name, seed in seeds.items():
-        t = torch.empty((M, LD), dtype=torch.float32, device=dev)
-        gbblas.fill(t, M, K, LD, seed, 0, 32, stream=stream)
+    for name, seed in {"A_N": 11, "A_T": 12, "B_N": 13, "B_T": 14, "C": 15}.items():
+        t = torch.empty((M, LD), dtype=torch.float32, device=ctx.dev)
+        gb.fill(t, M, K, LD, seed, 0, 32, stream=ctx.stream)
         bufs[name] = t
     C0 = bufs["C"].clone()
 
-    def operands(mode):
+    def ops(mode):
         return bufs["A_T" if mode[0] == "T" else "A_N"], bufs["B_T" if mode[1] == "T" else "B_N"]
 
-    def algo_id(name):
-        return {"bf16x3": gbblas.ALGO_BF16X3, "simt": gbblas.ALGO_SIMT}[name]
-
     def gemm(mode, algo, C=None):
-        A, B = operands(mode)
-        gbblas.sgemm(mode[0], mode[1], M, N, K, ALPHA, A, LD, B, LD, BETA, bufs["C"] if C is None else C, LD,
-                     algo=algo, stream=stream)
+        A, B = ops(mode)
+        gb.sgemm(mode[0], mode[1], M, N, K, ALPHA, A, LD, B, LD, BETA, bufs["C"] if C is None else C, LD,
+                 algo=algo, stream=ctx.stream)
 
-    # choose the headline algorithm
-    algo_name = args.algo
-    if algo_name == "best":
-        algo_name = "bf16x3"
+    algo_name = args.algo if args.algo != "best" else "bf16x3"
+    if algo_name == "bf16x3":
         try:
-            gemm("NN", gbblas.ALGO_BF16X3)
+            gemm("NN", gb.ALGO_BF16X3)
             torch.cuda.synchronize()
-        except gbblas.GBError as e:
-            if e.status != gbblas.ERR_UNSUPPORTED:
+        except gb.GBError as e:
+            if e.status != gb.ERR_UNSUPPORTED:
                 raise
             algo_name = "simt"
-    algo = algo_id(algo_name)
+    algo = {"bf16x3": gb.ALGO_BF16X3, "simt": gb.ALGO_SIMT}[algo_name]
 
-    # ---- accuracy (checker): normwise error on a seeded 128x128 subgrid
     errors = {}
     try:
         import oracle
         rng = np.random.default_rng(1)
         rows = np.sort(rng.choice(M, 128, replace=False))
         cols = np.sort(rng.choice(N, 128, replace=False))
-        hostbuf = {k: v.cpu().numpy() for k, v in bufs.items() if k != "C"}
+        hb = {k: v.cpu().numpy() for k, v in bufs.items() if k != "C"}
         c0 = C0.cpu().numpy()
-        for an in (["simt", "bf16x3"] if algo_name == "bf16x3" else ["simt"]):
+        for an, aid in (("simt", gb.ALGO_SIMT), ("bf16x3", gb.ALGO_BF16X3)):
+            if an == "bf16x3" and algo_name != "bf16x3":
+                continue
             worst = 0.0
             for mode in MODES:
                 Cw = C0.clone()
-                gemm(mode, algo_id(an), Cw)
-                got = Cw.cpu().numpy()
-                A = hostbuf["A_T" if mode[0] == "T" else "A_N"]
-                B = hostbuf["B_T" if mode[1] == "T" else "B_N"]
-                e, _ = oracle.normwise_error(got, mode[0], mode[1], M, N, K, ALPHA, A, LD, B, LD, BETA, c0, LD,
-                                             rows, cols)
+                gemm(mode, aid, Cw)
+                A = hb["A_T" if mode[0] == "T" else "A_N"]
+                B = hb["B_T" if mode[1] == "T" else "B_N"]
+                e, _ = oracle.normwise_error(Cw.cpu().numpy(), mode[0], mode[1], M, N, K, ALPHA, A, LD, B, LD, BETA,
+                                             c0, LD, rows, cols)
                 worst = max(worst, e)
             errors[an] = worst
         errors["bound_2Ku"] = 2 * K * 2.0 ** -24
-    except Exception as e:  # the error report must not hide the timing
+        errors["subgrid"] = "seeded 128 x 128 rows/cols, Dot2 oracle, worst of 4 modes"
+    except Exception as e:
         errors["error"] = repr(e)
 
-    # ---- warmup
     for _ in range(args.warmup):
         for mode in MODES:
             gemm(mode, algo)
     torch.cuda.synchronize()
 
-    # ---- timed region (device-resident inputs)
-    nev = args.steps * len(MODES)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nev)]
-    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    sampler = ClockSampler(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    sampler.start()
-    time.sleep(0.3)
-    launches0 = gbblas.launch_count()
-    t_start.record(stream)
-    i = 0
-    for _ in range(args.steps):
+    def step(evs):
         for mode in MODES:
-            ev[i][0].record(stream)
+            a, b = ctx.event(), ctx.event()
+            a.record(ctx.stream)
             gemm(mode, algo)
-            ev[i][1].record(stream)
-            i += 1
-    t_end.record(stream)
-    torch.cuda.synchronize()
-    launches = gbblas.launch_count() - launches0
-    clocks = sampler.stop()
-    elapsed_ms = t_start.elapsed_time(t_end)
-    if dist:
-        t = torch.tensor([elapsed_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    per_launch_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
-    value = world * args.steps * len(MODES) * FLOPS_PER_GEMM / (elapsed_ms * 1e-3) / 1e12
+            b.record(ctx.stream)
+            evs.append((a, b))
 
-    # ---- plain SIMT comparison (one step, same workload), when the headline is bf16x3
+    ms, kms, clocks, launches = ctx.timed(step, args.steps)
+    value = ctx.world * args.steps * len(MODES) * flops / (ms * 1e-3) / 1e12
+
     compare = {}
     if algo_name != "simt":
-        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         for mode in MODES:
-            gemm(mode, gbblas.ALGO_SIMT)
-        s0.record(stream)
+            gemm(mode, gb.ALGO_SIMT)
+        s0, s1 = ctx.event(), ctx.event()
+        s0.record(ctx.stream)
         for _ in range(2):
             for mode in MODES:
-                gemm(mode, gbblas.ALGO_SIMT)
-        s1.record(stream)
+                gemm(mode, gb.ALGO_SIMT)
+        s1.record(ctx.stream)
         torch.cuda.synchronize()
-        compare["simt_tflops"] = 2 * len(MODES) * FLOPS_PER_GEMM / (s0.elapsed_time(s1) * 1e-3) / 1e12
+        compare["simt_tflops"] = 2 * len(MODES) * flops / (s0.elapsed_time(s1) * 1e-3) / 1e12
+        compare["speedup_vs_simt"] = value / ctx.world / compare["simt_tflops"]
 
-    # ---- e2e through the C ABI with host buffers
     pin = {k: v.cpu().pin_memory() for k, v in bufs.items()}
     hostC = torch.empty((M, LD), dtype=torch.float32).pin_memory()
     nbytes = M * LD * 4
-    L = gbblas.lib()
 
-    def e2e_step():
+    def step_host():
         h2d = d2h = 0
         for mode in MODES:
             an, bn = ("A_T" if mode[0] == "T" else "A_N"), ("B_T" if mode[1] == "T" else "B_N")
-            for src, dst in ((pin[an], bufs[an]), (pin[bn], bufs[bn]), (pin["C"], bufs["C"])):
-                st = L.gb_memcpy(ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src.data_ptr()), nbytes, 0,
-                                 ctypes.c_void_p(stream.cuda_stream))
-                assert st == 0
+            for name in (an, bn, "C"):
+                memcpy(ctx, bufs[name], pin[name], nbytes, 0)
                 h2d += nbytes
             gemm(mode, algo)
-            st = L.gb_memcpy(ctypes.c_void_p(hostC.data_ptr()), ctypes.c_void_p(bufs["C"].data_ptr()), nbytes, 1,
-                             ctypes.c_void_p(stream.cuda_stream))
-            assert st == 0
+            memcpy(ctx, hostC, bufs["C"], nbytes, 1)
             d2h += nbytes
         return h2d, d2h
 
-    e2e_step()
-    torch.cuda.synchronize()
-    e_steps = max(1, min(args.steps, 5))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
-    e0.record(stream)
-    for _ in range(e_steps):
-        h2d, d2h = e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e_ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e_ms = float(t.item())
-    e2e_value = world * e_steps * len(MODES) * FLOPS_PER_GEMM / (e_ms * 1e-3) / 1e12
+    e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 5)), len(MODES) * flops, 1e12)
 
-    # ---- roofline of the GEMM kernel
-    peaks, peak_src = measured_peaks()
-    kernel_tflops = FLOPS_PER_GEMM / (per_launch_ms * 1e-3) / 1e12
+    kernel_tflops = flops / (kms * 1e-3) / 1e12
     if algo_name == "bf16x3":
-        # three BF16 products per FP32 product on the tensor pipe
-        roof = {"bound": "tensor", "achieved": kernel_tflops, "peak": peaks["bf16_tflops"] / 3.0,
-                "unit": "TFLOP/s", "peak_note": "bf16 dense %s peak / 3 (3 products per FP32 FMA)" % peak_src}
+        roof = {"bound": "tensor", "achieved": kernel_tflops, "peak": ctx.peaks["bf16_tflops"] / 3.0,
+                "unit": "TFLOP/s", "peak_note": "BF16 dense %s burst peak / 3 (three BF16 products per FP32 "
+                "product); achieved = 2MNK / mean duration of one gb_sgemm call (split + MMA kernels)" % ctx.peak_src}
         kname = "sgemm_bf16x3_4096"
     else:
-        fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
-        roof = {"bound": "fp32-simt", "achieved": kernel_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+        roof = {"bound": "fp32-simt", "achieved": kernel_tflops, "peak": FP32_SIMT_PEAK, "unit": "TFLOP/s",
                 "peak_note": "nominal FFMA peak 152 SMs x 128 lanes x 2 x 2.07 GHz (no measured FP32 peak)"}
         kname = "sgemm_simt_4096"
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["traffic"] = profile_traffic(kname)
-    roof["kernel_ms"] = per_launch_ms
+    roof["kernel_ms"] = kms
 
-    line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_dict(world, algo_name), "roofline": roof,
-            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": int(launches), "clocks": clocks, "errors_normwise": errors, "compare": compare}
+    config = {"workload": "SGEMM 4096^3, ld 4112, alpha 1.5, beta -0.5, NN/NT/TN/TT, U[-1,1] seed 1",
+              "M": M, "N": N, "K": K, "ld": LD, "alpha": ALPHA, "beta": BETA, "modes": list(MODES),
+              "algo": algo_name, "parallelism": "replicas x%d" % ctx.world,
+              "l2": "inputs larger than L2 (8 operand buffers of 67 MB + C per step)"}
+    line = base_line(ctx, METRIC, value, "TFLOP/s", ms, args.steps, "f32", config)
+    line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+                                           "d2h_bytes_per_step": d2h},
+                 "gpu_launches": launches, "clocks": clocks, "errors_normwise": errors, "compare": compare})
+    if ctx.rank == 0 and not args.no_cpu_baseline:
+        v, nt, desc = cpu_sgemm_sample()
+        line["cpu_baseline"] = {"value": v, "unit": "TFLOP/s", "cores": nt, "kind": "port", "sample": desc}
+    ctx.finish(line)
 
-    if rank == 0 and not args.no_cpu_baseline:
-        try:
-            v, nt, desc = cpu_reference_sample()
-            line["cpu_baseline"] = {"value": v, "unit": "TFLOP/s", "cores": nt, "kind": "port", "sample": desc}
-        except Exception as e:
-            line["cpu_baseline"] = {"value": None, "unit": "TFLOP/s", "cores": 0, "kind": "port",
-                                    "sample": "failed: %r" % e}
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+
+def run_dgemm(ctx):
+    torch, gb, args = ctx.torch, ctx.gb, ctx.args
+    import numpy as np
+    n = args.size or 8192
+    flops = 2.0 * n ** 3
+    bufs = {}
+    for name, seed in {"A": 31, "AT": 33, "B": 32, "BT": 34, "C": 35}.items():
+        t = torch.empty((n, n), dtype=torch.float64, device=ctx.dev)
+        gb.fill(t, n, n, n, seed, 2, 64, stream=ctx.stream)
+        bufs[name] = t
+    C0 = bufs["C"].clone()
+    modes = ("NN", "TT")
+
+    def gemm(mode, algo, C, s=0):
+        A = bufs["AT" if mode[0] == "T" else "A"]
+        B = bufs["BT" if mode[1] == "T" else "B"]
+        gb.dgemm(mode[0], mode[1], n, n, n, 1.0, A, n, B, n, 1.0, C, n, algo=algo, ozaki_slices=s, stream=ctx.stream)
+
+    slices = args.slices
+    study = {}
+    try:
+        import oracle
+        rng = np.random.default_rng(3)
+        sub = args.subgrid
+        rows = np.sort(rng.choice(n, sub, replace=False))
+        cols = np.sort(rng.choice(n, sub, replace=False))
+        hb = {k: v.cpu().numpy() for k, v in bufs.items() if k != "C"}
+        c0 = C0.cpu().numpy()
+        refs = {}
+        for mode in modes:
+            A = hb["AT" if mode[0] == "T" else "A"]
+            B = hb["BT" if mode[1] == "T" else "B"]
+            refs[mode] = (A, B, oracle.gemm_dot2(mode[0], mode[1], n, n, n, 1.0, A, n, B, n, 1.0, c0, n, rows, cols))
+        rn2 = {m: oracle.op_norms(m[0], m[1], n, n, n, refs[m][0], n, refs[m][1], n, rows, cols) for m in modes}
+
+        def err_of(mode, C):
+            A, B, ref = refs[mode]
+            got = C.cpu().numpy()[np.ix_(rows, cols)]
+            r2, c2 = rn2[mode]
+            den = math.sqrt(r2.sum() * c2.sum()) + np.linalg.norm(c0[np.ix_(rows, cols)])
+            maxrel = float(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)))
+            return float(np.linalg.norm(got - ref) / den), maxrel
+
+        for s in (4, 5, 6, 7, 8):
+            res = {}
+            for mode in modes:
+                Cw = C0.clone()
+                gemm(mode, gb.ALGO_OZAKI, Cw, s)
+                a, b = ctx.event(), ctx.event()
+                Cw2 = C0.clone()
+                a.record(ctx.stream)
+                gemm(mode, gb.ALGO_OZAKI, Cw2, s)
+                b.record(ctx.stream)
+                torch.cuda.synchronize()
+                e, mr = err_of(mode, Cw2)
+                res[mode] = {"tflops": flops / (a.elapsed_time(b) * 1e-3) / 1e12, "normwise": e, "max_rel": mr}
+            study["ozaki_s%d" % s] = res
+        res = {}
+        for mode in modes:
+            Cw = C0.clone()
+            a, b = ctx.event(), ctx.event()
+            a.record(ctx.stream)
+            gemm(mode, gb.ALGO_ORDERED, Cw)
+            b.record(ctx.stream)
+            torch.cuda.synchronize()
+            e, mr = err_of(mode, Cw)
+            res[mode] = {"tflops": flops / (a.elapsed_time(b) * 1e-3) / 1e12, "normwise": e, "max_rel": mr}
+        study["native_fp64"] = res
+        study["subgrid"] = "seeded %d x %d rows/cols, Dot2 oracle" % (sub, sub)
+        if slices == 0:   # fewest slices whose error is no worse than native in both modes
+            for s in (4, 5, 6, 7, 8):
+                if all(study["ozaki_s%d" % s][m]["normwise"] <= study["native_fp64"][m]["normwise"] for m in modes):
+                    slices = s
+                    break
+            else:
+                slices = 8
+    except Exception as e:
+        study["error"] = repr(e)
+        slices = slices or 8
+
+    for _ in range(args.warmup):
+        for mode in modes:
+            gemm(mode, gb.ALGO_OZAKI, bufs["C"], slices)
+    torch.cuda.synchronize()
+
+    def step(evs):
+        for mode in modes:
+            a, b = ctx.event(), ctx.event()
+            a.record(ctx.stream)
+            gemm(mode, gb.ALGO_OZAKI, bufs["C"], slices)
+            b.record(ctx.stream)
+            evs.append((a, b))
+
+    ms, kms, clocks, launches = ctx.timed(step, args.steps)
+    value = ctx.world * args.steps * len(modes) * flops / (ms * 1e-3) / 1e12
+    npairs = slices * (slices + 1) // 2
+    roof = {"bound": "tensor", "achieved": flops * npairs / (kms * 1e-3) / 1e12, "peak": ctx.peaks["bf16_tflops"],
+            "unit": "TFLOP/s", "peak_note": "BF16 slice-product flops (%d pairs x 2MNK) / mean gb_dgemm duration "
+            "(exponents + slicing + MMA) against the %s BF16 burst peak" % (npairs, ctx.peak_src)}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = profile_traffic("dgemm_ozaki_8192")
+    roof["kernel_ms"] = kms
+    nbytes = n * n * 8
+    pin = {k: v.cpu().pin_memory() for k, v in bufs.items()}
+    hostC = torch.empty((n, n), dtype=torch.float64).pin_memory()
+
+    def step_host():
+        h2d = d2h = 0
+        for mode in modes:
+            for name in (("AT" if mode[0] == "T" else "A"), ("BT" if mode[1] == "T" else "B"), "C"):
+                memcpy(ctx, bufs[name], pin[name], nbytes, 0)
+                h2d += nbytes
+            gemm(mode, gb.ALGO_OZAKI, bufs["C"], slices)
+            memcpy(ctx, hostC, bufs["C"], nbytes, 1)
+            d2h += nbytes
+        return h2d, d2h
+
+    e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 3)), len(modes) * flops, 1e12)
+    config = {"workload": "DGEMM 8192^3 NN+TT, alpha=beta=1, entries u*2^e (e in [-20,20]) seed 3",
+              "M": n, "N": n, "K": n, "modes": list(modes), "algo": "ozaki", "slices": slices,
+              "parallelism": "replicas x%d" % ctx.world, "l2": "inputs larger than L2 (5 x 512 MB)"}
+    line = base_line(ctx, METRIC, value, "TFLOP/s", ms, args.steps, "f64", config)
+    line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+                                           "d2h_bytes_per_step": d2h},
+                 "gpu_launches": launches, "clocks": clocks, "precision_study": study})
+    if ctx.rank == 0 and not args.no_cpu_baseline:
+        v, nt, desc = cpu_dgemm_sample()
+        line["cpu_baseline"] = {"value": v, "unit": "TFLOP/s", "cores": nt, "kind": "port", "sample": desc}
+    ctx.finish(line)
+
+
+def bw_roof(ctx, gbs, kms_bytes_per_launch, kname, extra=None):
+    roof = {"bound": "hbm", "achieved": gbs, "peak": ctx.peaks["hbm_gbs"], "unit": "GB/s",
+            "peak_note": "%s copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" % ctx.peak_src}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = profile_traffic(kname)
+    if extra:
+        roof.update(extra)
+    return roof
+
+
+def run_skinny(ctx):
+    torch, gb, args = ctx.torch, ctx.gb, ctx.args
+    bits = args.bits
+    dt = torch.float64 if bits == 64 else torch.float32
+    s = bits // 8
+    small, big, K = args.n, 262144, 4096
+    thin = args.workload == "thinb"
+    M, N = (big, small) if thin else (small, big)
+    nbytes_alg = s * (M * K + K * N + 2 * M * N)
+    flops = 2.0 * M * N * K
+    ops = {}
+    for mode in MODES:
+        ar, ac = (K, M) if mode[0] == "T" else (M, K)
+        br, bc = (N, K) if mode[1] == "T" else (K, N)
+        A = torch.empty((ar, ac), dtype=dt, device=ctx.dev)
+        B = torch.empty((br, bc), dtype=dt, device=ctx.dev)
+        gb.fill(A, ar, ac, ac, 21 + (mode[0] == "T"), 0, bits, stream=ctx.stream)
+        gb.fill(B, br, bc, bc, 23 + (mode[1] == "T"), 0, bits, stream=ctx.stream)
+        ops[mode] = (A, ac, B, bc)
+    C = torch.empty((M, N), dtype=dt, device=ctx.dev)
+    gb.fill(C, M, N, N, 25, 0, bits, stream=ctx.stream)
+
+    def gemm(mode):
+        A, lda, B, ldb = ops[mode]
+        gb.gemm(mode[0], mode[1], M, N, K, 1.0, A, lda, B, ldb, 1.0, C, N, bits, algo=gb.ALGO_SKINNY,
+                stream=ctx.stream)
+
+    for _ in range(args.warmup):
+        for mode in MODES:
+            gemm(mode)
+    torch.cuda.synchronize()
+
+    def step(evs):
+        for mode in MODES:
+            a, b = ctx.event(), ctx.event()
+            a.record(ctx.stream)
+            gemm(mode)
+            b.record(ctx.stream)
+            evs.append((a, b))
+
+    ms, kms, clocks, launches = ctx.timed(step, args.steps)
+    value = ctx.world * args.steps * len(MODES) * nbytes_alg / (ms * 1e-3) / 1e9
+    tflops = flops / (kms * 1e-3) / 1e12
+    cpeak = FP64_PEAK if bits == 64 else FP32_SIMT_PEAK
+    roof = bw_roof(ctx, nbytes_alg / (kms * 1e-3) / 1e9, None, "%s_%s_n%d" % (args.workload, "f%d" % bits, small),
+                   {"compute_tflops": tflops, "compute_peak_tflops": cpeak,
+                    "compute_frac": tflops / cpeak, "kernel_ms": kms,
+                    "peak_note_compute": "nominal %s peak" % ("FP64" if bits == 64 else "FP32 FFMA")})
+    hostbufs = {m: (ops[m][0].cpu().pin_memory(), ops[m][2].cpu().pin_memory()) for m in MODES}
+    hostC = C.cpu().pin_memory()
+
+    def step_host():
+        h2d = d2h = 0
+        for mode in MODES:
+            A, _, B, _ = ops[mode]
+            hA, hB = hostbufs[mode]
+            for d, h in ((A, hA), (B, hB), (C, hostC)):
+                memcpy(ctx, d, h, d.numel() * s, 0)
+                h2d += d.numel() * s
+            gemm(mode)
+            memcpy(ctx, hostC, C, C.numel() * s, 1)
+            d2h += C.numel() * s
+        return h2d, d2h
+
+    e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 3)), len(MODES) * nbytes_alg, 1e9)
+    config = {"workload": "%s FP%d M=%d N=%d K=%d, NN/NT/TN/TT, U[-1,1] seed 2" % (args.workload, bits, M, N, K),
+              "M": M, "N": N, "K": K, "modes": list(MODES), "algo": "skinny",
+              "bytes_per_gemm": nbytes_alg, "parallelism": "replicas x%d" % ctx.world,
+              "l2": "inputs larger than L2 (large operand %d MB)" % (s * big * K // 10 ** 6)}
+    line = base_line(ctx, "HBM GB/s (%s)" % args.workload, value, "GB/s", ms, args.steps, "f%d" % bits, config)
+    line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+                                           "d2h_bytes_per_step": d2h},
+                 "gpu_launches": launches, "clocks": clocks})
+    if ctx.rank == 0 and not args.no_cpu_baseline:
+        v, nt, desc = cpu_bw_sample("skinny", bits)
+        line["cpu_baseline"] = {"value": v, "unit": "GB/s", "cores": nt, "kind": "port", "sample": desc}
+    ctx.finish(line)
+
+
+def run_transpose(ctx):
+    torch, gb, args = ctx.torch, ctx.gb, ctx.args
+    bits = args.bits
+    dt = torch.float64 if bits == 64 else torch.float32
+    s = bits // 8
+    M, N = 30000, 17000
+    A = torch.empty((M, N), dtype=dt, device=ctx.dev)
+    gb.fill(A, M, N, N, 2, 0, bits, stream=ctx.stream)
+    B = torch.empty((N, M), dtype=dt, device=ctx.dev)
+    nbytes = 2.0 * M * N * s
+
+    def op():
+        gb.transpose(M, N, A, N, B, M, bits, stream=ctx.stream)
+
+    for _ in range(args.warmup):
+        op()
+    torch.cuda.synchronize()
+
+    def step(evs):
+        a, b = ctx.event(), ctx.event()
+        a.record(ctx.stream)
+        op()
+        b.record(ctx.stream)
+        evs.append((a, b))
+
+    ms, kms, clocks, launches = ctx.timed(step, args.steps)
+    value = ctx.world * args.steps * nbytes / (ms * 1e-3) / 1e9
+    roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "transpose_f%d_30000x17000" % bits, {"kernel_ms": kms})
+    hA = A.cpu().pin_memory()
+    hB = torch.empty_like(B, device="cpu").pin_memory()
+
+    def step_host():
+        memcpy(ctx, A, hA, A.numel() * s, 0)
+        op()
+        memcpy(ctx, hB, B, B.numel() * s, 1)
+        return A.numel() * s, B.numel() * s
+
+    e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 3)), nbytes, 1e9)
+    config = {"workload": "transpose 30000 x 17000 FP%d, bit-exact" % bits, "M": M, "N": N,
+              "parallelism": "replicas x%d" % ctx.world, "l2": "inputs larger than L2"}
+    line = base_line(ctx, "HBM GB/s (transpose)", value, "GB/s", ms, args.steps, "f%d" % bits, config)
+    line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+                                           "d2h_bytes_per_step": d2h},
+                 "gpu_launches": launches, "clocks": clocks})
+    if ctx.rank == 0 and not args.no_cpu_baseline:
+        v, nt, desc = cpu_bw_sample("transpose", bits)
+        line["cpu_baseline"] = {"value": v, "unit": "GB/s", "cores": nt, "kind": "port", "sample": desc}
+    ctx.finish(line)
+
+
+def run_jacobi(ctx):
+    torch, gb, args = ctx.torch, ctx.gb, ctx.args
+    bits = args.bits
+    dt = torch.float64 if bits == 64 else torch.float32
+    s = bits // 8
+    M = N = 8192
+    iters = args.iters
+    A = torch.ones((M + 2, N + 2), dtype=dt, device=ctx.dev)
+    inner = torch.empty((M, N), dtype=dt, device=ctx.dev)
+    gb.fill(inner, M, N, N, 2, 1, bits, stream=ctx.stream)
+    A[1:-1, 1:-1] = inner
+    del inner
+    A0 = A.clone()
+    B = A.clone()
+    nbytes = 2.0 * M * N * s * iters
+
+    def op():
+        gb.stencil2d(M, N, A, B, iters, gb.STENCIL_HOST, bits, stream=ctx.stream)
+
+    for _ in range(max(1, args.warmup)):
+        op()
+    torch.cuda.synchronize()
+
+    def step(evs):
+        a, b = ctx.event(), ctx.event()
+        a.record(ctx.stream)
+        op()
+        b.record(ctx.stream)
+        evs.append((a, b))
+
+    ms, kms, clocks, launches = ctx.timed(step, args.steps)
+    value = ctx.world * args.steps * nbytes / (ms * 1e-3) / 1e9
+    gflops = 5.0 * M * N * iters / (kms * 1e-3) / 1e12
+    extra = {"kernel_ms": kms, "points_per_s": M * N * iters / (kms * 1e-3),
+             "fp_tflops": gflops, "note": "achieved = algorithmic bytes (2*M*N*s per sweep) / time; temporal "
+             "blocking lets it exceed the HBM peak (DRAM bytes in profiles/)"}
+    if bits == 64:
+        extra.update({"compute_bound": "fp64", "compute_peak_tflops": FP64_PEAK, "compute_frac": gflops / FP64_PEAK})
+    roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "jacobi_f%d_8192" % bits, extra)
+    hA = A0.cpu().pin_memory()
+    hR = torch.empty_like(A, device="cpu").pin_memory()
+
+    def step_host():
+        memcpy(ctx, A, hA, A.numel() * s, 0)
+        memcpy(ctx, B, hA, A.numel() * s, 0)
+        op()
+        memcpy(ctx, hR, B if iters % 2 else A, A.numel() * s, 1)
+        return 2 * A.numel() * s, A.numel() * s
+
+    e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 3)), nbytes, 1e9)
+    config = {"workload": "Jacobi 8192^2 FP%d, %d sweeps, boundary 1.0, interior U[0,1] seed 2" % (bits, iters),
+              "M": M, "N": N, "iters": iters, "order": "host", "parallelism": "replicas x%d" % ctx.world,
+              "l2": "grid larger than L2"}
+    line = base_line(ctx, "HBM GB/s (jacobi)", value, "GB/s", ms, args.steps, "f%d" % bits, config)
+    line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+                                           "d2h_bytes_per_step": d2h},
+                 "gpu_launches": launches, "clocks": clocks})
+    if ctx.rank == 0 and not args.no_cpu_baseline:
+        v, nt, desc = cpu_bw_sample("jacobi", bits)
+        line["cpu_baseline"] = {"value": v, "unit": "GB/s", "cores": nt, "kind": "port", "sample": desc}
+    ctx.finish(line)
+
+
+# ================================================================== reference arm
+def run_reference_arm(args):
+    """The reference's own CPU implementation of the path (the oracle's port of
+    its host loop; the reference is not installable -- see the design doc), timed on
+    the host cores, rank 0 only."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    vals, desc, nt = [], "", 1
+    fn = {"sgemm": cpu_sgemm_sample, "dgemm": cpu_dgemm_sample}.get(args.workload)
+    for _ in range(max(1, args.steps)):
+        if fn:
+            v, nt, desc = fn(max_seconds=6.0)
+        else:
+            v, nt, desc = cpu_bw_sample("skinny" if args.workload in ("thinb", "shorta") else args.workload, args.bits)
+        vals.append(v)
+    value = statistics.median(vals)
+    unit = "TFLOP/s" if fn else "GB/s"
+    metric = METRIC if fn else "HBM GB/s (%s)" % args.workload
+    line = {"impl": "reference", "metric": metric, "value": value, "unit": unit, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.workload == "sgemm" else "f%d" % args.bits,
+            "data": "synthetic",
+            "config": {"workload": args.workload, "algo": "reference host loop (CPU)"},
+            "cpu_baseline": {"value": value, "unit": unit, "cores": nt, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.workload == "sgemm":
+        line["config"].update({"workload": "SGEMM 4096^3, ld 4112, alpha 1.5, beta -0.5, NN/NT/TN/TT, U[-1,1] seed 1",
+                               "M": 4096, "N": 4096, "K": 4096})
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="sgemm", choices=["sgemm", "dgemm", "thinb", "shorta", "transpose", "jacobi"])
+    ap.add_argument("--algo", default="best", choices=["best", "bf16x3", "simt"])
+    ap.add_argument("--bits", type=int, default=32, choices=[32, 64])
+    ap.add_argument("--n", type=int, default=8, help="small dimension of thinb/shorta")
+    ap.add_argument("--iters", type=int, default=200, help="jacobi sweeps")
+    ap.add_argument("--slices", type=int, default=0, help="dgemm: Ozaki slices (0: fewest matching native error)")
+    ap.add_argument("--size", type=int, default=0, help="dgemm: M=N=K (default 8192)")
+    ap.add_argument("--subgrid", type=int, default=1024, help="dgemm: error subgrid size")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    args.warmup = max(args.warmup, 3)
+    ctx = Ctx(args)
+    {"sgemm": run_sgemm, "dgemm": run_dgemm, "thinb": run_skinny, "shorta": run_skinny,
+     "transpose": run_transpose, "jacobi": run_jacobi}[args.workload](ctx)
 
 
 if __name__ == "__main__":

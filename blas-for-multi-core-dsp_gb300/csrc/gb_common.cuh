@@ -90,6 +90,8 @@ gb_status launch_sgemm_simt(const GemmArgs &g);
 gb_status launch_dgemm_dmma(const GemmArgs &g);
 gb_status launch_sgemm_bf16x3(const GemmArgs &g);
 gb_status launch_dgemm_ozaki(const GemmArgs &g, int slices);
+// Slice count (2..8) whose truncation error meets a normwise target for this K.
+int ozaki_pick_slices(double target_err, int64_t K);
 gb_status launch_skinny_f32(const GemmArgs &g);
 gb_status launch_skinny_f64(const GemmArgs &g);
 // C = beta*C (beta==0: C = 0) or C = C + beta (scalar) epilogue-only path (K == 0)

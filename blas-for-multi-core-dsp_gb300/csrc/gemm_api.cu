@@ -98,6 +98,8 @@ gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alph
             if (sizeof(T) != 8) return set_status(GB_ERR_UNSUPPORTED, "gb_sgemm: OZAKI is an FP64 algorithm");
             int s = o.ozaki_slices;
             GB_CHECK_ARG(s == 0 || (s >= 2 && s <= 8), "gb_dgemm: ozaki_slices %d not in 2..8", s);
+            GB_CHECK_ARG(o.target_err >= 0.0, "gb_dgemm: negative target_err");
+            if (s == 0) s = ozaki_pick_slices(o.target_err, K);
             return launch_dgemm_ozaki(g, s);
         }
         case GB_ALGO_SKINNY:

@@ -1,0 +1,471 @@
+// gemm_ozaki.cu -- DGEMM from exact integer slices on the tcgen05 tensor cores
+// (Ozaki scheme: Ozaki, Ogita, Oishi & Rump, "Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication and
+// its applications", Numer. Algorithms 59, 2012; integer-slice form as in
+// Ootomo, Ozaki & Yokota, "DGEMM on integer matrix multiplication unit",
+// IJHPCA 2024).  Precision form of the reference's DGEMM
+// (dgemm_release_V1.1/device_code/dgemm_kernel.c:1994-3170); it has no
+// counterpart in the reference.
+//
+// Each row i of op(A) is scaled by 2^-e_i (e_i: max_k |a_ik| < 2^e_i) and
+// written as s base-128 digits, a_ik = 2^e_i * sum_t v_ikt 2^-7t (+ a
+// remainder < 2^(e_i-7s)), v in [-127, 127]; columns of op(B) likewise with
+// exponents f_j and digits w.  Then
+//     C_ij ~= 2^(e_i+f_j) sum_{t+u <= s+1} 2^-7(t+u) (V_t W_u^T)_ij .
+// The digits are integers that BF16 holds exactly, so each slice product
+// runs on tcgen05.mma kind::f16 with an FP32 accumulator in TMEM, and every
+// partial sum of a 1024-long K chunk is an integer below 1024*127^2 < 2^24:
+// exact.  Chunk sums are added exactly in int32 registers (up to 127 chunks),
+// and FP64 appears only in the per-pair scaled sum kept in TMEM and in the
+// final 2^(e_i+f_j), alpha, beta epilogue.  (sm_103a has no kind::i8 MMA, so
+// the INT8 products are carried in BF16; products and sums stay exact.)
+//
+// Kernels: row/column exponents (integer max of |x| bit patterns), digit
+// extraction (integer shifts of the FP64 mantissa; the transpose modes are
+// absorbed here, slices are written K-major), and a persistent GEMM: one CTA
+// per SM over 128 x 128 C tiles, per tile a loop over slice pairs and K
+// chunks; warp 0 issues TMA (one digit tile of V_t and one of W_u per 64-wide
+// K block), warp 1 issues the MMAs into one of two FP32 accumulators
+// (alternating per chunk), warps 2-5 drain them into int32 registers and the
+// FP64 sum in TMEM, and write C.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include "gb_common.cuh"
+#include "sm100_ptx.cuh"
+
+namespace gb {
+
+bool make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                    uint32_t box_inner, uint32_t box_outer, int swizzle_bytes);
+
+int ozaki_pick_slices(double target_err, int64_t K) {
+    // truncation error of the triangular slice sum ~ 2^(-7s) * sqrt(K) * small
+    // constant relative to |A||B|; pick the smallest s meeting the target
+    if (target_err <= 0) target_err = 0x1.0p-52;
+    double logk = 0;
+    for (int64_t k = K; k > 1; k >>= 1) logk += 0.5;
+    for (int s = 2; s <= 8; s++)
+        if (-7.0 * s + logk + 2.0 <= __builtin_log2(target_err)) return s;
+    return 8;
+}
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 5, GROUP_M = 8;
+constexpr int KCHUNK_BLOCKS = 16;              // 1024-long exact FP32 chunk
+constexpr int MAX_CHUNKS_INT32 = 127;          // chunk sums per int32 accumulator
+constexpr int MAXS = 8, MAXPAIRS = MAXS * (MAXS + 1) / 2;
+constexpr int TILE_BYTES = BM * BK * 2;        // 16 KB (BM == BN)
+constexpr int STAGE_BYTES = 2 * TILE_BYTES;
+constexpr int EPI_BYTES = 4 * 32 * 33 * 8;     // per-warp 32 x 32 FP64 staging
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_BYTES + 1024 + 256;
+constexpr int NT = 192;
+constexpr uint32_t TMEM_COLS = 512;            // [0,256): two FP32 accumulators, [256,512): FP64 sum
+
+// ------------------------------------------------------------- exponents
+// e = smallest integer with max |x| < 2^e (0 for an all-zero line), from
+// the maximum of the |x| bit patterns (monotone for non-negative doubles).
+__device__ __forceinline__ int exp_of_maxbits(unsigned long long mb) {
+    if (mb == 0) return 0;
+    int E = (int)((mb >> 52) & 0x7FF);
+    if (E == 0) {   // subnormal: value = m * 2^-1074, m < 2^52
+        int lz = __clzll((long long)mb);      // m has 64 - lz significant bits
+        return (64 - lz) - 1074;
+    }
+    return E - 1022;   // value in [2^(E-1023), 2^(E-1022))
+}
+
+// one warp per line of `len` contiguous elements
+__global__ void maxexp_contig_kernel(const double *__restrict__ X, int64_t ld, int64_t lines, int64_t len,
+                                     int *__restrict__ e) {
+    const int64_t line = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+    if (line >= lines) return;
+    unsigned long long mb = 0;
+    const unsigned long long *p = reinterpret_cast<const unsigned long long *>(X + line * ld);
+    for (int64_t k = lane; k < len; k += 32) {
+        unsigned long long b = __ldg(p + k) & 0x7FFFFFFFFFFFFFFFull;
+        mb = b > mb ? b : mb;
+    }
+    for (int o = 16; o; o >>= 1) {
+        unsigned long long v = __shfl_xor_sync(0xffffffffu, mb, o);
+        mb = v > mb ? v : mb;
+    }
+    if (lane == 0) e[line] = exp_of_maxbits(mb);
+}
+
+// one thread per column j of a len x cols storage (rows strided by ld)
+__global__ void maxexp_strided_kernel(const double *__restrict__ X, int64_t ld, int64_t cols, int64_t len,
+                                      int *__restrict__ e) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cols) return;
+    unsigned long long mb = 0;
+    const unsigned long long *p = reinterpret_cast<const unsigned long long *>(X);
+    for (int64_t k = 0; k < len; k++) {
+        unsigned long long b = __ldg(p + k * ld + j) & 0x7FFFFFFFFFFFFFFFull;
+        mb = b > mb ? b : mb;
+    }
+    e[j] = exp_of_maxbits(mb);
+}
+
+// ---------------------------------------------------------------- digits
+// s base-128 digits of x * 2^-e (|x| < 2^e), truncated, sign of x, as BF16.
+__device__ __forceinline__ void digits(double x, int e, int s, unsigned short *out, int64_t stride) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned short sign = (unsigned short)((b >> 48) & 0x8000);
+    const int E = (int)((b >> 52) & 0x7FF);
+    unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    int ex;
+    if (E == 0) {
+        ex = -1074;
+    } else {
+        m |= 1ull << 52;
+        ex = E - 1075;
+    }
+    const int shift = ex + 7 * s - e;   // F = m * 2^shift < 2^(7s)
+    unsigned long long F;
+    if (m == 0 || shift <= -64) F = 0;
+    else if (shift >= 0) F = m << shift;
+    else F = m >> (-shift);
+    for (int t = 1; t <= s; t++) {
+        unsigned v = (unsigned)((F >> (7 * (s - t))) & 0x7F);
+        unsigned short h = v ? (unsigned short)(__bfloat16_as_ushort(__float2bfloat16_rn((float)v)) | sign) : 0;
+        out[(int64_t)(t - 1) * stride] = h;
+    }
+}
+
+// out: s slices of rows_p x kp (K-major).  Source element (r, k):
+// trans ? X[k*ldx + r] : X[r*ldx + k]; padding rows / columns are zero.
+__global__ void __launch_bounds__(256) slice_kernel(const double *__restrict__ X, int64_t ldx, int trans, int64_t rows,
+                                                    int64_t K, int64_t rows_p, int64_t kp, const int *__restrict__ e,
+                                                    int s, unsigned short *__restrict__ out) {
+    __shared__ double tile[32][33];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+    const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
+#pragma unroll
+    for (int i = 0; i < 32; i += 8) {
+        double v = 0.0;
+        if (trans) {
+            int64_t k = k0 + ty + i, r = r0 + tx;
+            if (k < K && r < rows) v = X[k * ldx + r];
+            tile[ty + i][tx] = v;
+        } else {
+            int64_t r = r0 + ty + i, k = k0 + tx;
+            if (k < K && r < rows) v = X[r * ldx + k];
+            tile[tx][ty + i] = v;
+        }
+    }
+    __syncthreads();
+    const int64_t stride = rows_p * kp;
+#pragma unroll
+    for (int i = 0; i < 32; i += 8) {
+        int64_t r = r0 + ty + i, k = k0 + tx;
+        if (r < rows_p && k < kp) digits(tile[tx][ty + i], r < rows ? e[r] : 0, s, out + r * kp + k, stride);
+    }
+}
+
+// ------------------------------------------------------------------ gemm
+struct OzParams {
+    double *C;
+    int64_t M, N, ldc;
+    double alpha, beta;
+    int semantics;
+    int num_kb;                    // K blocks of 64
+    int tiles_m, tiles_n;
+    int64_t mp, np;                // padded rows of one V / W slice
+    int npairs;
+    signed char pt[MAXPAIRS], pu[MAXPAIRS];   // 1-based digit indices per pair
+    const int *erow, *fcol;
+    int *err;
+};
+
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int &tm, int &tn) {
+    const int per_group = GROUP_M * tiles_n;
+    const int g = t / per_group;
+    const int first_m = g * GROUP_M;
+    const int gm = min(GROUP_M, tiles_m - first_m);
+    const int r = t - g * per_group;
+    tm = first_m + r % gm;
+    tn = r / gm;
+}
+
+__global__ void __launch_bounds__(NT, 1)
+    ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmV, const __grid_constant__ CUtensorMap tmW, OzParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    double *epi = reinterpret_cast<double *>(smem + STAGES * STAGE_BYTES);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES + EPI_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *acc_full = empty + STAGES;
+    uint64_t *acc_empty = acc_full + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int num_tiles = p.tiles_m * p.tiles_n;
+    const int nchunks = (p.num_kb + KCHUNK_BLOCKS - 1) / KCHUNK_BLOCKS;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            ptx::mbar_init(&full[s], 1);
+            ptx::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            ptx::mbar_init(&acc_full[b], 1);
+            ptx::mbar_init(&acc_empty[b], 4);
+        }
+        ptx::fence_mbar_init();
+        ptx::tma_prefetch_desc(&tmV);
+        ptx::tma_prefetch_desc(&tmW);
+    }
+    if (warp == 1) ptx::tmem_alloc(tmem_slot, TMEM_COLS);
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {   // TMA producer: per tile, per pair, every K block
+            int kbg = 0;
+            bool go = true;
+            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+                int tm, tn;
+                tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+                for (int q = 0; q < p.npairs && go; q++) {
+                    const int vrow = (int)((p.pt[q] - 1) * p.mp + (int64_t)tm * BM);
+                    const int wrow = (int)((p.pu[q] - 1) * p.np + (int64_t)tn * BN);
+                    for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
+                        const int s = kbg % STAGES;
+                        if (kbg >= STAGES && !ptx::mbar_wait(&empty[s], ((kbg / STAGES) & 1) ^ 1, p.err, 11)) {
+                            go = false;
+                            break;
+                        }
+                        uint8_t *st = smem + s * STAGE_BYTES;
+                        ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+                        ptx::tma_load_2d(st, &tmV, &full[s], kb * BK, vrow);
+                        ptx::tma_load_2d(st + TILE_BYTES, &tmW, &full[s], kb * BK, wrow);
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer: one accumulator per K chunk of a pair
+            constexpr uint32_t idesc = ptx::idesc_bf16_f32(BM, BN);
+            int kbg = 0, gi = 0;
+            bool go = true;
+            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+                for (int q = 0; q < p.npairs && go; q++) {
+                    for (int c = 0; c < nchunks && go; c++, gi++) {
+                        const int b = gi & 1;
+                        if (gi >= 2 && !ptx::mbar_wait(&acc_empty[b], ((gi >> 1) & 1) ^ 1, p.err, 12)) {
+                            go = false;
+                            break;
+                        }
+                        ptx::tc_fence_after();
+                        const uint32_t acc = tmem + (uint32_t)(b * BN);
+                        const int kb_end = min(p.num_kb, (c + 1) * KCHUNK_BLOCKS);
+                        for (int kb = c * KCHUNK_BLOCKS; kb < kb_end; kb++, kbg++) {
+                            const int s = kbg % STAGES;
+                            if (!ptx::mbar_wait(&full[s], (kbg / STAGES) & 1, p.err, 13)) {
+                                go = false;
+                                break;
+                            }
+                            ptx::tc_fence_after();
+                            const uint32_t st = ptx::smem_u32(smem + s * STAGE_BYTES);
+                            const uint64_t vd = ptx::sdesc_kmajor_sw128(st);
+                            const uint64_t wd = ptx::sdesc_kmajor_sw128(st + TILE_BYTES);
+#pragma unroll
+                            for (int k = 0; k < BK / 16; k++) {
+                                const uint64_t dk = (uint64_t)((k * 32) >> 4);
+                                ptx::umma_f16(acc, vd + dk, wd + dk, idesc, (kb != c * KCHUNK_BLOCKS) || (k != 0));
+                            }
+                            ptx::umma_commit(&empty[s]);
+                        }
+                        if (go) ptx::umma_commit(&acc_full[b]);
+                    }
+                }
+            }
+        }
+    } else {               // epilogue warps 2..5: TMEM lane quarter q = warp % 4
+        const int q = warp % 4;
+        double *stage = epi + q * 32 * 33;
+        const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+        const uint32_t tot = tmem + 256u + lane_base;   // FP64 sum: element j at columns 2j, 2j+1
+        int gi = 0;
+        bool go = true;
+        for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+            int tm, tn;
+            tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+            bool first_flush = true;
+            for (int qq = 0; qq < p.npairs && go; qq++) {
+                int iacc[BN];
+#pragma unroll
+                for (int j = 0; j < BN; j++) iacc[j] = 0;
+                const double scale = __longlong_as_double((long long)(1023 - 7 * (p.pt[qq] + p.pu[qq])) << 52);
+                for (int c = 0; c < nchunks; c++, gi++) {
+                    const int b = gi & 1;
+                    if (!ptx::mbar_wait(&acc_full[b], (gi >> 1) & 1, p.err, 14)) { go = false; break; }
+                    ptx::tc_fence_after();
+#pragma unroll
+                    for (int cb = 0; cb < BN / 32; cb++) {
+                        uint32_t r[32];
+                        ptx::tmem_ld_32x32b_x32(tmem + (uint32_t)(b * BN) + lane_base + (uint32_t)(cb * 32), r);
+                        ptx::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 32; j++) iacc[cb * 32 + j] += __float2int_rn(__uint_as_float(r[j]));
+                    }
+                    ptx::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
+                    const bool flush = (c == nchunks - 1) || ((c + 1) % MAX_CHUNKS_INT32 == 0);
+                    if (flush) {   // FP64 sum += 2^-7(t+u) * iacc (exact scaling, one rounding)
+#pragma unroll
+                        for (int cb = 0; cb < (2 * BN) / 32; cb++) {
+                            uint32_t r[32];
+                            if (!first_flush) {
+                                ptx::tmem_ld_32x32b_x32(tot + (uint32_t)(cb * 32), r);
+                                ptx::tmem_ld_wait();
+                            }
+#pragma unroll
+                            for (int j = 0; j < 16; j++) {
+                                double v = first_flush ? 0.0 : __hiloint2double((int)r[2 * j + 1], (int)r[2 * j]);
+                                v = fma((double)iacc[cb * 16 + j], scale, v);
+                                r[2 * j] = (uint32_t)__double2loint(v);
+                                r[2 * j + 1] = (uint32_t)__double2hiint(v);
+                                iacc[cb * 16 + j] = 0;
+                            }
+                            ptx::tmem_st_32x32b_x32(tot + (uint32_t)(cb * 32), r);
+                        }
+                        ptx::tmem_st_wait();
+                        first_flush = false;
+                    }
+                }
+            }
+            if (!go) break;
+            // C = alpha * 2^(e_i + f_j) * sum (+ beta ...), staged for row-contiguous stores
+            const int64_t row0 = (int64_t)tm * BM + q * 32;
+            const int64_t n0 = (int64_t)tn * BN;
+            const int64_t myrow = row0 + lane;
+            const int erow = myrow < p.M ? p.erow[myrow] : 0;
+            for (int cb = 0; cb < BN / 32; cb++) {
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    uint32_t r[32];
+                    ptx::tmem_ld_32x32b_x32(tot + (uint32_t)(cb * 64 + h * 32), r);
+                    ptx::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 16; j++)
+                        stage[lane * 33 + h * 16 + j] = scalbn(__hiloint2double((int)r[2 * j + 1], (int)r[2 * j]), erow);
+                }
+                __syncwarp();
+                const int64_t col = n0 + cb * 32 + lane;
+                if (col < p.N) {
+                    const int fc = p.fcol[col];
+                    const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
+                    for (int rr = 0; rr < rows; rr++) {
+                        double *cp = p.C + (row0 + rr) * p.ldc + col;
+                        double v = p.alpha * scalbn(stage[rr * 33 + lane], fc);
+                        if (p.semantics == GB_SEM_BLAS) {
+                            if (p.beta != 0.0) v = fma(p.beta, *cp, v);
+                        } else if (p.semantics == GB_SEM_SCALAR_BETA) {
+                            v = v + p.beta;
+                        } else {
+                            v = *cp + (v + p.beta);
+                        }
+                        *cp = v;
+                    }
+                }
+                __syncwarp();
+            }
+            ptx::tc_fence_before();
+        }
+    }
+
+    ptx::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+}  // namespace
+
+gb_status launch_dgemm_ozaki(const GemmArgs &g, int slices) {
+    if (g.M == 0 || g.N == 0) return ok();
+    const int s = slices > 0 ? slices : ozaki_pick_slices(0.0, g.K);
+    if (s < 2 || s > MAXS) return set_status(GB_ERR_INVALID_ARG, "ozaki: slices %d not in 2..%d", s, MAXS);
+    const int64_t kp = ceil_div(g.K, BK) * BK;
+    const int64_t mp = ceil_div(g.M, BM) * BM, np = ceil_div(g.N, BN) * BN;
+    if (s * mp > 0x7fffffff || s * np > 0x7fffffff || kp > 0x7fffffff)
+        return set_status(GB_ERR_UNSUPPORTED, "ozaki: problem too large for 32-bit TMA coordinates");
+    const size_t ebytes = (size_t)(mp + np) * sizeof(int);
+    const size_t vbytes = (size_t)s * mp * kp * 2, wbytes = (size_t)s * np * kp * 2;
+    uint8_t *ws = (uint8_t *)workspace(vbytes + wbytes + ebytes + 4096, g.stream);
+    if (!ws) return (gb_status)gb_get_last_status();
+    unsigned short *V = (unsigned short *)ws;
+    unsigned short *W = (unsigned short *)(ws + vbytes);
+    int *erow = (int *)(ws + vbytes + wbytes);
+    int *fcol = erow + mp;
+    int *err = error_word();
+    if (!err) return set_status(GB_ERR_OOM, "ozaki: no device error word");
+
+    // exponents: rows of op(A), columns of op(B)
+    const double *A = (const double *)g.A, *B = (const double *)g.B;
+    if (!g.ta) {
+        maxexp_contig_kernel<<<(unsigned)ceil_div(g.M, 8), 256, 0, g.stream>>>(A, g.lda, g.M, g.K, erow);
+    } else {
+        maxexp_strided_kernel<<<(unsigned)ceil_div(g.M, 256), 256, 0, g.stream>>>(A, g.lda, g.M, g.K, erow);
+    }
+    GB_LAUNCH_CHECK("ozaki exponents A");
+    if (g.tb) {
+        maxexp_contig_kernel<<<(unsigned)ceil_div(g.N, 8), 256, 0, g.stream>>>(B, g.ldb, g.N, g.K, fcol);
+    } else {
+        maxexp_strided_kernel<<<(unsigned)ceil_div(g.N, 256), 256, 0, g.stream>>>(B, g.ldb, g.N, g.K, fcol);
+    }
+    GB_LAUNCH_CHECK("ozaki exponents B");
+
+    // digits: V_t = digits of op(A) rows (M x K), W_u = digits of op(B)^T rows (N x K)
+    dim3 gA((unsigned)ceil_div(kp, 32), (unsigned)ceil_div(mp, 32));
+    dim3 gB((unsigned)ceil_div(kp, 32), (unsigned)ceil_div(np, 32));
+    if (gA.y > 65535u || gB.y > 65535u) return set_status(GB_ERR_UNSUPPORTED, "ozaki: M or N too large");
+    slice_kernel<<<gA, 256, 0, g.stream>>>(A, g.lda, g.ta ? 1 : 0, g.M, g.K, mp, kp, erow, s, V);
+    GB_LAUNCH_CHECK("ozaki slices A");
+    slice_kernel<<<gB, 256, 0, g.stream>>>(B, g.ldb, g.tb ? 0 : 1, g.N, g.K, np, kp, fcol, s, W);
+    GB_LAUNCH_CHECK("ozaki slices B");
+
+    CUtensorMap tV, tW;
+    if (!make_tmap_bf16(&tV, V, kp, (uint64_t)s * mp, kp * 2, BK, BM, 128) ||
+        !make_tmap_bf16(&tW, W, kp, (uint64_t)s * np, kp * 2, BK, BN, 128))
+        return set_status(GB_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
+
+    OzParams p{};
+    p.C = (double *)g.C; p.M = g.M; p.N = g.N; p.ldc = g.ldc;
+    p.alpha = g.alpha; p.beta = g.beta; p.semantics = g.semantics;
+    p.num_kb = (int)(kp / BK);
+    p.tiles_m = (int)(mp / BM); p.tiles_n = (int)(np / BN);
+    p.mp = mp; p.np = np;
+    p.erow = erow; p.fcol = fcol; p.err = err;
+    // slice pairs t + u <= s + 1, least significant diagonals first (the FP64
+    // sum then adds terms in increasing magnitude)
+    int n = 0;
+    for (int d = s + 1; d >= 2; d--)
+        for (int t = 1; t <= s; t++) {
+            int u = d - t;
+            if (u >= 1 && u <= s) { p.pt[n] = (signed char)t; p.pu[n] = (signed char)u; n++; }
+        }
+    p.npairs = n;
+
+    static bool attr_set = false;
+    if (!attr_set) {
+        GB_CUDA_TRY(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        attr_set = true;
+    }
+    const int tiles = p.tiles_m * p.tiles_n;
+    const int grid = tiles < sm_count() ? tiles : sm_count();
+    ozaki_gemm_kernel<<<grid, NT, SMEM_BYTES, g.stream>>>(tV, tW, p);
+    GB_LAUNCH_CHECK("ozaki_gemm_kernel");
+    return ok();
+}
+
+}  // namespace gb
