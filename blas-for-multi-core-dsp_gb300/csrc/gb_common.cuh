@@ -44,10 +44,10 @@ int sm_count();
 // Opt-in shared memory per block (bytes) of the current device.
 int smem_optin();
 
-// Device-wide scratch owned by the library, grown on demand (per device,
-// guarded by a mutex).  Returns nullptr and sets GB_ERR_OOM on failure.
-// The buffer stays valid until the next call that needs more; callers use it
-// stream-ordered on one stream at a time.
+// Scratch owned by the library, one grow-only buffer per (device, stream),
+// guarded by a mutex.  Returns nullptr and sets GB_ERR_OOM on failure.  The
+// buffer stays valid until the next call on the same stream needs more;
+// work on that stream uses it in stream order.
 void *workspace(size_t bytes, void *stream);
 
 // Per-device error word (4 bytes of device memory, zero = no error) that

@@ -11,6 +11,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <vector>
 
 #include "gb_common.cuh"
 
@@ -66,24 +67,30 @@ int smem_optin() {
 }
 
 static std::mutex g_ws_mu;
-static void *g_ws_ptr[kMaxDev] = {nullptr};
-static size_t g_ws_size[kMaxDev] = {0};
+// one grow-only buffer per (device, stream): work queued on different
+// streams never shares scratch
+struct WsEntry {
+    int dev;
+    void *stream;
+    void *ptr;
+    size_t size;
+};
+static std::vector<WsEntry> g_ws;
 
 void *workspace(size_t bytes, void *stream) {
     int dev = 0;
     cudaGetDevice(&dev);
-    if (dev < 0 || dev >= kMaxDev) {
-        set_status(GB_ERR_INVALID_ARG, "workspace: device ordinal %d out of range", dev);
-        return nullptr;
-    }
     std::lock_guard<std::mutex> lk(g_ws_mu);
-    if (g_ws_size[dev] >= bytes && g_ws_ptr[dev]) return g_ws_ptr[dev];
-    if (g_ws_ptr[dev]) {
-        // the old buffer may still be in use by work queued on any stream
-        cudaDeviceSynchronize();
-        cudaFree(g_ws_ptr[dev]);
-        g_ws_ptr[dev] = nullptr;
-        g_ws_size[dev] = 0;
+    WsEntry *w = nullptr;
+    for (auto &e : g_ws)
+        if (e.dev == dev && e.stream == stream) w = &e;
+    if (w && w->size >= bytes) return w->ptr;
+    if (w && w->ptr) {
+        // the old buffer may still be read by work queued on its stream
+        cudaStreamSynchronize(as_stream(stream));
+        cudaFree(w->ptr);
+        w->ptr = nullptr;
+        w->size = 0;
     }
     size_t want = bytes < (size_t(64) << 20) ? (size_t(64) << 20) : bytes;
     void *p = nullptr;
@@ -93,9 +100,12 @@ void *workspace(size_t bytes, void *stream) {
         set_status(GB_ERR_OOM, "workspace: cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
         return nullptr;
     }
-    (void)stream;
-    g_ws_ptr[dev] = p;
-    g_ws_size[dev] = want;
+    if (!w) {
+        g_ws.push_back(WsEntry{dev, stream, nullptr, 0});
+        w = &g_ws.back();
+    }
+    w->ptr = p;
+    w->size = want;
     return p;
 }
 
@@ -227,6 +237,18 @@ gb_status gb_malloc(void **ptr, size_t bytes) {
     return ok();
 }
 
+gb_status gb_malloc_managed(void **ptr, size_t bytes) {
+    GB_CHECK_ARG(ptr != nullptr, "gb_malloc_managed: null out-pointer");
+    *ptr = nullptr;
+    if (bytes == 0) return ok();
+    cudaError_t e = cudaMallocManaged(ptr, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_status(GB_ERR_OOM, "gb_malloc_managed(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return ok();
+}
+
 gb_status gb_free(void *ptr) {
     if (ptr) GB_CUDA_TRY(cudaFree(ptr));
     return ok();
@@ -239,6 +261,12 @@ gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int kind, void *st
     cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : kind == 1 ? cudaMemcpyDeviceToHost
                                                                       : cudaMemcpyDeviceToDevice;
     GB_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, k, as_stream(stream)));
+    return ok();
+}
+
+gb_status gb_workspace_reserve(size_t bytes, void *stream) {
+    if (bytes == 0) return ok();
+    if (!workspace(bytes, stream)) return (gb_status)gb_get_last_status();
     return ok();
 }
 

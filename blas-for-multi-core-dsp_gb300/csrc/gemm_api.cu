@@ -40,13 +40,25 @@ gb_status k0(const GemmArgs &g) {
     return ok();
 }
 
+// GB_ALGO_AUTO: skinny shapes stream through the skinny kernels; large FP32
+// products go to 3xBF16 on tcgen05 once K is long enough for its
+// representation error to sit inside 2*K*u32; large FP64 products go to the
+// Ozaki slices (slice count chosen for FP64-level error), small ones stay on
+// the bit-exact ordered DFMA kernel (GB300's FP64 pipe is ~1.2 TFLOP/s).
+// (FP64 skinny products go to Ozaki too: native FP64 is ~1.2 TFLOP/s, and
+// the slices of a very long K are processed in chunks of bounded workspace.)
 int pick(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
     (void)ta; (void)tb;
     const int64_t small = M < N ? M : N;
     const int64_t large = M < N ? N : M;
+    const double work = (double)M * (double)N * (double)K;
+    if (bits == 64) {
+        if (work > 134217728.0) return GB_ALGO_OZAKI;   // 2^27 = 512^3
+        if (small <= 64 && large >= 4 * small && large >= 1024) return GB_ALGO_SKINNY;
+        return GB_ALGO_ORDERED;
+    }
     if (small <= 64 && large >= 4 * small && large >= 1024) return GB_ALGO_SKINNY;
-    if (bits == 64) return GB_ALGO_ORDERED;   // FP64-pipe bound either way; bit-exact
-    (void)K;
+    if (K >= 64 && work > 134217728.0) return GB_ALGO_BF16X3;
     return GB_ALGO_SIMT;
 }
 
@@ -97,7 +109,7 @@ gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alph
         case GB_ALGO_OZAKI: {
             if (sizeof(T) != 8) return set_status(GB_ERR_UNSUPPORTED, "gb_sgemm: OZAKI is an FP64 algorithm");
             int s = o.ozaki_slices;
-            GB_CHECK_ARG(s == 0 || (s >= 2 && s <= 8), "gb_dgemm: ozaki_slices %d not in 2..8", s);
+            GB_CHECK_ARG(s == 0 || (s >= 2 && s <= 9), "gb_dgemm: ozaki_slices %d not in 2..9", s);
             GB_CHECK_ARG(o.target_err >= 0.0, "gb_dgemm: negative target_err");
             if (s == 0) s = ozaki_pick_slices(o.target_err, K);
             return launch_dgemm_ozaki(g, s);

@@ -45,9 +45,9 @@ int ozaki_pick_slices(double target_err, int64_t K) {
     if (target_err <= 0) target_err = 0x1.0p-52;
     double logk = 0;
     for (int64_t k = K; k > 1; k >>= 1) logk += 0.5;
-    for (int s = 2; s <= 8; s++)
+    for (int s = 2; s <= 9; s++)
         if (-7.0 * s + logk + 2.0 <= __builtin_log2(target_err)) return s;
-    return 8;
+    return 9;
 }
 
 namespace {
@@ -55,7 +55,7 @@ namespace {
 constexpr int BM = 128, BN = 128, BK = 64, STAGES = 5, GROUP_M = 8;
 constexpr int KCHUNK_BLOCKS = 16;              // 1024-long exact FP32 chunk
 constexpr int MAX_CHUNKS_INT32 = 127;          // chunk sums per int32 accumulator
-constexpr int MAXS = 8, MAXPAIRS = MAXS * (MAXS + 1) / 2;
+constexpr int MAXS = 9, MAXPAIRS = MAXS * (MAXS + 1) / 2;
 constexpr int TILE_BYTES = BM * BK * 2;        // 16 KB (BM == BN)
 constexpr int STAGE_BYTES = 2 * TILE_BYTES;
 constexpr int EPI_BYTES = 4 * 32 * 33 * 8;     // per-warp 32 x 32 FP64 staging
@@ -123,7 +123,7 @@ __device__ __forceinline__ void digits(double x, int e, int s, unsigned short *o
         m |= 1ull << 52;
         ex = E - 1075;
     }
-    const int shift = ex + 7 * s - e;   // F = m * 2^shift < 2^(7s)
+    const int shift = ex + 7 * s - e;   // F = m * 2^shift < 2^(7s) <= 2^63
     unsigned long long F;
     if (m == 0 || shift <= -64) F = 0;
     else if (shift >= 0) F = m << shift;
@@ -391,10 +391,39 @@ __global__ void __launch_bounds__(NT, 1)
 
 }  // namespace
 
+static gb_status ozaki_one(const GemmArgs &g, int s);
+
+// Slices of both operands take s * (Mp + Np) * Kp * 2 bytes of workspace.
+// Past kWorkspaceCap the K range is cut into chunks, each sliced and
+// multiplied on its own and accumulated into C (beta applied by the first
+// chunk, later chunks add with beta = 1); each chunk gets its own row and
+// column exponents.
+constexpr double kWorkspaceCap = 4.0 * (1ull << 30);
+
 gb_status launch_dgemm_ozaki(const GemmArgs &g, int slices) {
     if (g.M == 0 || g.N == 0) return ok();
     const int s = slices > 0 ? slices : ozaki_pick_slices(0.0, g.K);
     if (s < 2 || s > MAXS) return set_status(GB_ERR_INVALID_ARG, "ozaki: slices %d not in 2..%d", s, MAXS);
+    const double per_k = (double)s * (double)(ceil_div(g.M, BM) * BM + ceil_div(g.N, BN) * BN) * 2.0;
+    int64_t kc = (int64_t)(kWorkspaceCap / per_k) / (KCHUNK_BLOCKS * BK) * (KCHUNK_BLOCKS * BK);
+    if (kc < KCHUNK_BLOCKS * BK) kc = KCHUNK_BLOCKS * BK;
+    if (g.K <= kc) return ozaki_one(g, s);
+    for (int64_t k0 = 0; k0 < g.K; k0 += kc) {
+        GemmArgs c = g;
+        c.K = (g.K - k0) < kc ? (g.K - k0) : kc;
+        c.A = (const double *)g.A + (g.ta ? k0 * g.lda : k0);
+        c.B = (const double *)g.B + (g.tb ? k0 : k0 * g.ldb);
+        if (k0 > 0) {   // later chunks: C += alpha * A_k B_k
+            c.semantics = GB_SEM_BLAS;
+            c.beta = 1.0;
+        }
+        gb_status st = ozaki_one(c, s);
+        if (st != GB_OK) return st;
+    }
+    return ok();
+}
+
+static gb_status ozaki_one(const GemmArgs &g, int s) {
     const int64_t kp = ceil_div(g.K, BK) * BK;
     const int64_t mp = ceil_div(g.M, BM) * BM, np = ceil_div(g.N, BN) * BN;
     if (s * mp > 0x7fffffff || s * np > 0x7fffffff || kp > 0x7fffffff)

@@ -1,0 +1,569 @@
+// serve.cu -- request loop: HBM-budget admission, continuous batching into
+// grouped launches, CUDA-graph replay, per-request latency (p50 / p99).
+//
+// The reference host runs one kernel at a time (hthread_group_exec +
+// hthread_group_wait, sgemm_release_V1.3.2/host_code/sgemm_demo.c:144-145);
+// this is the GB300 serving layer built on the same hot-path kernels.  It has
+// no reference counterpart.
+//
+// Requests (GEMM, transpose, Jacobi) carry device pointers to operands the
+// caller keeps resident.  A request is charged the bytes of its operands
+// while it is in flight; it is admitted when the in-flight total plus its
+// charge fits the budget (FIFO; a request larger than the whole budget is
+// rejected).  A dispatcher thread takes every admitted request as soon as it
+// is admitted: GEMMs below the grouping threshold go together into one launch
+// of the grouped persistent kernel (replayed from a CUDA graph per slot),
+// the rest go one launch each with the algorithm the autotune table (or the
+// AUTO heuristic) picks, round-robin over the stream pool.  A host callback
+// on the stream stamps completion, releases the charge and wakes the
+// dispatcher, so new requests are admitted while earlier ones run.
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <tuple>
+#include <vector>
+
+#include "gb_common.cuh"
+#include "gb_internal.h"
+
+namespace gb {
+
+static double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// ------------------------------------------------------------ autotune table
+namespace {
+struct TuneKey {
+    int bits, ta, tb, lm, ln, lk;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(bits, ta, tb, lm, ln, lk) < std::tie(o.bits, o.ta, o.tb, o.lm, o.ln, o.lk);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;
+
+int lg(int64_t x) {   // bucket: round(log2(x)) (0 for x <= 1)
+    if (x <= 1) return 0;
+    return (int)lround(log2((double)x));
+}
+
+TuneKey key_of(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
+    return TuneKey{bits, ta ? 1 : 0, tb ? 1 : 0, lg(M), lg(N), lg(K)};
+}
+}  // namespace
+
+int tuned_algo(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key_of(bits, ta, tb, M, N, K));
+    return it == g_tune.end() ? -1 : it->second;
+}
+
+// ------------------------------------------------------------------- server
+namespace {
+
+struct Pending {
+    gb_request r;
+    uint64_t bytes;
+    double t_submit;
+};
+
+struct Batch;   // completion context of one launch
+
+}  // namespace
+
+struct Server {
+    gb_server_config cfg;
+    std::mutex mu;
+    std::condition_variable cv_dispatch, cv_done;
+    std::deque<Pending> waiting;
+    uint64_t inflight_bytes = 0;
+    int64_t inflight = 0, submitted = 0, completed = 0, rejected = 0, failed = 0;
+    int64_t launches = 0, grouped_launches = 0, grouped_requests = 0;
+    double t_first = 0, t_last = 0;
+    std::vector<double> latencies;
+    std::vector<uint64_t> done_tags;
+    std::vector<double> done_lat;
+    std::vector<cudaStream_t> streams;
+    size_t rr = 0;
+    GroupRunner *grouped = nullptr;
+    std::thread dispatcher;
+    bool stop = false;
+    int device = 0;
+    int last_error = GB_OK;
+};
+
+namespace {
+
+struct Batch {
+    Server *s;
+    std::vector<std::pair<uint64_t, double>> reqs;   // tag, submit time
+    uint64_t bytes;
+};
+
+void CUDART_CB on_done(void *p) {
+    Batch *b = static_cast<Batch *>(p);
+    Server *s = b->s;
+    const double t = now_s();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto &q : b->reqs) {
+            const double lat = t - q.second;
+            s->latencies.push_back(lat);
+            s->done_tags.push_back(q.first);
+            s->done_lat.push_back(lat);
+        }
+        s->completed += (int64_t)b->reqs.size();
+        s->inflight -= (int64_t)b->reqs.size();
+        s->inflight_bytes -= b->bytes;
+        s->t_last = t;
+    }
+    s->cv_dispatch.notify_all();
+    s->cv_done.notify_all();
+    delete b;
+}
+
+uint64_t request_bytes(const gb_request &r) {
+    const uint64_t es = r.dtype_bits == 64 ? 8 : 4;
+    if (r.bytes) return r.bytes;
+    switch (r.op) {
+        case GB_OP_GEMM: {
+            const uint64_t a = (uint64_t)r.M * r.K, b = (uint64_t)r.K * r.N, c = (uint64_t)r.M * r.N;
+            return es * (a + b + c);
+        }
+        case GB_OP_TRANSPOSE: return es * 2 * (uint64_t)r.M * r.N;
+        default: return es * 2 * (uint64_t)(r.M + 2) * (r.N + 2);
+    }
+}
+
+gb_status validate(const gb_request &r) {
+    GB_CHECK_ARG(r.op >= GB_OP_GEMM && r.op <= GB_OP_STENCIL, "server: unknown op %d", r.op);
+    GB_CHECK_ARG(r.dtype_bits == 32 || r.dtype_bits == 64, "server: dtype_bits must be 32 or 64");
+    GB_CHECK_ARG(r.M >= 0 && r.N >= 0 && r.K >= 0, "server: negative dimension");
+    if (r.op == GB_OP_GEMM) {
+        gb_gemm_desc d;
+        memset(&d, 0, sizeof(d));
+        d.dtype_bits = r.dtype_bits; d.transA = r.transA; d.transB = r.transB; d.semantics = r.semantics;
+        d.M = r.M; d.N = r.N; d.K = r.K; d.A = r.A; d.lda = r.lda; d.B = r.B; d.ldb = r.ldb; d.C = r.C; d.ldc = r.ldc;
+        return check_desc(d, 0);
+    }
+    if (r.op == GB_OP_TRANSPOSE) {
+        GB_CHECK_ARG(r.lda >= r.N && r.ldb >= r.M, "server: transpose leading dimensions");
+        GB_CHECK_ARG((r.M == 0 || r.N == 0) || (r.A && r.B && r.A != r.B), "server: transpose pointers");
+    } else {
+        GB_CHECK_ARG(r.iters >= 0 && r.order >= 0 && r.order <= 2, "server: stencil iters/order");
+        GB_CHECK_ARG((r.M == 0 || r.N == 0) || (r.A && r.C && (const void *)r.A != r.C), "server: stencil pointers");
+    }
+    return ok();
+}
+
+bool groupable(const Server *s, const gb_request &r) {
+    if (!s->cfg.use_grouped || r.op != GB_OP_GEMM || r.algo != GB_ALGO_AUTO) return false;
+    const double work = (double)r.M * r.N * r.K;
+    const int64_t small = r.M < r.N ? r.M : r.N;
+    if (small <= 64) return false;   // the skinny kernel streams those better
+    return work <= s->cfg.group_max_work;
+}
+
+gb_status launch_one(Server *s, const gb_request &r, cudaStream_t st) {
+    if (r.op == GB_OP_GEMM) {
+        gb_gemm_opts o;
+        gb_gemm_opts_init(&o);
+        o.stream = st;
+        o.semantics = r.semantics;
+        o.algo = r.algo;
+        if (o.algo == GB_ALGO_AUTO) {
+            int t = tuned_algo(r.dtype_bits, is_trans(r.transA), is_trans(r.transB), r.M, r.N, r.K);
+            if (t >= 0) o.algo = t;
+        }
+        if (r.dtype_bits == 64)
+            return gb_dgemm(r.transA, r.transB, r.M, r.N, r.K, r.alpha, (const double *)r.A, r.lda,
+                            (const double *)r.B, r.ldb, r.beta, (double *)r.C, r.ldc, &o);
+        return gb_sgemm(r.transA, r.transB, r.M, r.N, r.K, (float)r.alpha, (const float *)r.A, r.lda,
+                        (const float *)r.B, r.ldb, (float)r.beta, (float *)r.C, r.ldc, &o);
+    }
+    if (r.op == GB_OP_TRANSPOSE) {
+        if (r.dtype_bits == 64)
+            return gb_transpose_f64(r.M, r.N, (const double *)r.A, r.lda, (double *)r.B, r.ldb, st);
+        return gb_transpose_f32(r.M, r.N, (const float *)r.A, r.lda, (float *)r.B, r.ldb, st);
+    }
+    (void)s;
+    if (r.dtype_bits == 64)
+        return gb_stencil2d_f64(r.M, r.N, (double *)r.A, (double *)r.C, r.iters, r.order, st);
+    return gb_stencil2d_f32(r.M, r.N, (float *)r.A, (float *)r.C, r.iters, r.order, st);
+}
+
+void dispatcher_main(Server *s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        s->cv_dispatch.wait(lk, [s] {
+            return s->stop || (!s->waiting.empty() &&
+                               s->inflight_bytes + s->waiting.front().bytes <= s->cfg.hbm_budget_bytes &&
+                               s->inflight < s->cfg.max_inflight);
+        });
+        if (s->stop && s->waiting.empty()) break;
+        if (s->stop && s->inflight_bytes + s->waiting.front().bytes > s->cfg.hbm_budget_bytes) {
+            s->cv_dispatch.wait(lk);
+            continue;
+        }
+        // admit FIFO while the budget allows
+        std::vector<Pending> admitted;
+        while (!s->waiting.empty() && s->inflight_bytes + s->waiting.front().bytes <= s->cfg.hbm_budget_bytes &&
+               s->inflight < s->cfg.max_inflight) {
+            admitted.push_back(s->waiting.front());
+            s->inflight_bytes += s->waiting.front().bytes;
+            s->inflight++;
+            s->waiting.pop_front();
+        }
+        lk.unlock();
+
+        std::vector<gb_gemm_desc> group;
+        std::vector<Pending> group_reqs;
+        for (auto &p : admitted) {
+            if (groupable(s, p.r) && (int)group.size() < s->cfg.max_batch) {
+                gb_gemm_desc d;
+                memset(&d, 0, sizeof(d));
+                d.dtype_bits = p.r.dtype_bits; d.transA = p.r.transA; d.transB = p.r.transB;
+                d.semantics = p.r.semantics; d.M = p.r.M; d.N = p.r.N; d.K = p.r.K;
+                d.alpha = p.r.alpha; d.beta = p.r.beta;
+                d.A = p.r.A; d.lda = p.r.lda; d.B = p.r.B; d.ldb = p.r.ldb; d.C = p.r.C; d.ldc = p.r.ldc;
+                group.push_back(d);
+                group_reqs.push_back(p);
+                continue;
+            }
+            cudaStream_t st = s->streams[s->rr++ % s->streams.size()];
+            Batch *b = new Batch{s, {{p.r.tag, p.t_submit}}, p.bytes};
+            gb_status rc = s->cfg.dry_run ? GB_OK : launch_one(s, p.r, st);
+            if (rc != GB_OK) {
+                std::lock_guard<std::mutex> g(s->mu);
+                s->failed++;
+                s->last_error = rc;
+            }
+            if (s->cfg.dry_run) on_done(b);
+            else cudaLaunchHostFunc(st, on_done, b);
+            std::lock_guard<std::mutex> g(s->mu);
+            s->launches++;
+        }
+        if (!group.empty()) {
+            cudaStream_t st = s->streams[s->rr++ % s->streams.size()];
+            Batch *b = new Batch{s, {}, 0};
+            for (auto &p : group_reqs) {
+                b->reqs.push_back({p.r.tag, p.t_submit});
+                b->bytes += p.bytes;
+            }
+            gb_status rc = s->cfg.dry_run ? GB_OK
+                                          : group_runner_run(s->grouped, group.data(), (int)group.size(), st,
+                                                             s->cfg.use_graphs);
+            if (rc != GB_OK) {
+                std::lock_guard<std::mutex> g(s->mu);
+                s->failed += (int64_t)group.size();
+                s->last_error = rc;
+            }
+            if (s->cfg.dry_run) on_done(b);
+            else cudaLaunchHostFunc(st, on_done, b);
+            std::lock_guard<std::mutex> g(s->mu);
+            s->launches++;
+            s->grouped_launches++;
+            s->grouped_requests += (int64_t)group.size();
+        }
+        lk.lock();
+    }
+}
+
+double percentile(std::vector<double> v, double q) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    double pos = q * (v.size() - 1);
+    size_t i = (size_t)pos;
+    double f = pos - i;
+    return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+}
+
+}  // namespace
+}  // namespace gb
+
+using gb::Server;
+
+extern "C" {
+
+void gb_server_config_init(gb_server_config *c) {
+    if (!c) return;
+    memset(c, 0, sizeof(*c));
+    c->hbm_budget_bytes = 48ull << 30;
+    c->streams = 4;
+    c->max_batch = 256;
+    c->max_inflight = 1 << 20;
+    c->use_graphs = 1;
+    c->use_grouped = 1;
+    c->group_max_work = 512.0 * 512.0 * 512.0;
+}
+
+gb_status gb_server_create(const gb_server_config *cfg, gb_server **out) {
+    GB_CHECK_ARG(out != nullptr, "gb_server_create: null out-pointer");
+    *out = nullptr;
+    gb_server_config c;
+    if (cfg) c = *cfg; else gb_server_config_init(&c);
+    GB_CHECK_ARG(c.hbm_budget_bytes > 0, "gb_server_create: zero HBM budget");
+    GB_CHECK_ARG(c.streams >= 1 && c.streams <= 64, "gb_server_create: streams must be 1..64");
+    GB_CHECK_ARG(c.max_batch >= 1 && c.max_batch <= 4096, "gb_server_create: max_batch must be 1..4096");
+    GB_CHECK_ARG(c.max_inflight >= 1, "gb_server_create: max_inflight must be positive");
+    Server *s = new Server();
+    s->cfg = c;
+    if (!c.dry_run) {
+        cudaGetDevice(&s->device);
+        for (int i = 0; i < c.streams; i++) {
+            cudaStream_t st;
+            cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+            if (e != cudaSuccess) {
+                for (auto x : s->streams) cudaStreamDestroy(x);
+                delete s;
+                return gb::cuda_status(e, "gb_server_create: stream");
+            }
+            s->streams.push_back(st);
+            if (c.workspace_bytes) {
+                gb_status r = gb_workspace_reserve(c.workspace_bytes, st);
+                if (r != GB_OK) {
+                    for (auto x : s->streams) cudaStreamDestroy(x);
+                    delete s;
+                    return r;
+                }
+            }
+        }
+        s->grouped = gb::group_runner_create(2 * c.streams, c.max_batch);
+    } else {
+        s->streams.push_back(nullptr);
+    }
+    s->dispatcher = std::thread(gb::dispatcher_main, s);
+    *out = reinterpret_cast<gb_server *>(s);
+    return gb::ok();
+}
+
+gb_status gb_server_submit(gb_server *sv, const gb_request *req) {
+    GB_CHECK_ARG(sv && req, "gb_server_submit: null argument");
+    Server *s = reinterpret_cast<Server *>(sv);
+    gb_status v = gb::validate(*req);
+    if (v != GB_OK) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->rejected++;
+        return v;
+    }
+    const uint64_t bytes = gb::request_bytes(*req);
+    if (bytes > s->cfg.hbm_budget_bytes) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->rejected++;
+        return gb::set_status(GB_ERR_OOM, "gb_server_submit: request needs %llu bytes, budget is %llu",
+                              (unsigned long long)bytes, (unsigned long long)s->cfg.hbm_budget_bytes);
+    }
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        const double t = gb::now_s();
+        if (s->submitted == 0) s->t_first = t;
+        s->waiting.push_back(gb::Pending{*req, bytes, t});
+        s->submitted++;
+    }
+    s->cv_dispatch.notify_one();
+    return gb::ok();
+}
+
+int gb_server_poll(gb_server *sv, uint64_t *tags, double *latency_s, int max) {
+    if (!sv || max <= 0) return 0;
+    Server *s = reinterpret_cast<Server *>(sv);
+    std::lock_guard<std::mutex> lk(s->mu);
+    int n = (int)std::min<size_t>((size_t)max, s->done_tags.size());
+    for (int i = 0; i < n; i++) {
+        if (tags) tags[i] = s->done_tags[i];
+        if (latency_s) latency_s[i] = s->done_lat[i];
+    }
+    s->done_tags.erase(s->done_tags.begin(), s->done_tags.begin() + n);
+    s->done_lat.erase(s->done_lat.begin(), s->done_lat.begin() + n);
+    return n;
+}
+
+gb_status gb_server_drain(gb_server *sv, double timeout_s) {
+    GB_CHECK_ARG(sv != nullptr, "gb_server_drain: null server");
+    Server *s = reinterpret_cast<Server *>(sv);
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto pred = [s] { return s->completed >= s->submitted && s->waiting.empty() && s->inflight == 0; };
+    if (timeout_s > 0) {
+        if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred))
+            return gb::set_status(GB_ERR_DEVICE_TIMEOUT, "gb_server_drain: %lld requests still pending after %.1f s",
+                                  (long long)(s->submitted - s->completed), timeout_s);
+    } else {
+        s->cv_done.wait(lk, pred);
+    }
+    if (s->last_error != GB_OK)
+        return gb::set_status((gb_status)s->last_error, "gb_server_drain: %lld request(s) failed to launch",
+                              (long long)s->failed);
+    return gb::ok();
+}
+
+gb_status gb_server_get_stats(gb_server *sv, gb_server_stats *out) {
+    GB_CHECK_ARG(sv && out, "gb_server_get_stats: null argument");
+    Server *s = reinterpret_cast<Server *>(sv);
+    std::lock_guard<std::mutex> lk(s->mu);
+    memset(out, 0, sizeof(*out));
+    out->submitted = s->submitted;
+    out->completed = s->completed;
+    out->rejected = s->rejected;
+    out->failed = s->failed;
+    out->waiting = (int64_t)s->waiting.size();
+    out->inflight = s->inflight;
+    out->inflight_bytes = s->inflight_bytes;
+    out->launches = s->launches;
+    out->grouped_launches = s->grouped_launches;
+    out->grouped_requests = s->grouped_requests;
+    out->p50_s = gb::percentile(s->latencies, 0.50);
+    out->p99_s = gb::percentile(s->latencies, 0.99);
+    out->mean_s = 0;
+    for (double x : s->latencies) out->mean_s += x;
+    if (!s->latencies.empty()) out->mean_s /= (double)s->latencies.size();
+    const double span = s->t_last - s->t_first;
+    out->req_per_s = span > 0 ? (double)s->completed / span : 0.0;
+    return gb::ok();
+}
+
+void gb_server_destroy(gb_server *sv) {
+    if (!sv) return;
+    Server *s = reinterpret_cast<Server *>(sv);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_dispatch.notify_all();
+    if (s->dispatcher.joinable()) s->dispatcher.join();
+    if (!s->cfg.dry_run) {
+        for (auto st : s->streams) cudaStreamSynchronize(st);
+        gb::group_runner_destroy(s->grouped);
+        for (auto st : s->streams) cudaStreamDestroy(st);
+    }
+    delete s;
+}
+
+// ---------------------------------------------------------------- autotune
+gb_status gb_autotune_set(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K, int algo) {
+    GB_CHECK_ARG(dtype_bits == 32 || dtype_bits == 64, "gb_autotune_set: dtype_bits");
+    GB_CHECK_ARG(gb::is_mode(transA) && gb::is_mode(transB), "gb_autotune_set: mode");
+    GB_CHECK_ARG(algo >= GB_ALGO_AUTO && algo <= GB_ALGO_SKINNY, "gb_autotune_set: algo");
+    std::lock_guard<std::mutex> lk(gb::g_tune_mu);
+    gb::g_tune[gb::key_of(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K)] = algo;
+    return gb::ok();
+}
+
+int gb_autotune_get(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K) {
+    return gb::tuned_algo(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K);
+}
+
+gb_status gb_autotune_gemm(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K, int *best,
+                           double *best_ms) {
+    GB_CHECK_ARG(dtype_bits == 32 || dtype_bits == 64, "gb_autotune_gemm: dtype_bits");
+    GB_CHECK_ARG(gb::is_mode(transA) && gb::is_mode(transB), "gb_autotune_gemm: mode");
+    GB_CHECK_ARG(M > 0 && N > 0 && K > 0, "gb_autotune_gemm: dimensions must be positive");
+    const bool ta = gb::is_trans(transA), tb = gb::is_trans(transB);
+    const int64_t es = dtype_bits / 8;
+    const int64_t lda = ta ? M : K, ldb = tb ? K : N;
+    void *A = nullptr, *B = nullptr, *C = nullptr;
+    gb_status st;
+    if ((st = gb_malloc(&A, (size_t)(M * K * es))) != GB_OK) return st;
+    if ((st = gb_malloc(&B, (size_t)(K * N * es))) != GB_OK) { gb_free(A); return st; }
+    if ((st = gb_malloc(&C, (size_t)(M * N * es))) != GB_OK) { gb_free(A); gb_free(B); return st; }
+    if (dtype_bits == 64) {
+        gb_fill_f64((double *)A, ta ? K : M, lda, lda, 1, 0, nullptr);
+        gb_fill_f64((double *)B, tb ? N : K, ldb, ldb, 2, 0, nullptr);
+    } else {
+        gb_fill_f32((float *)A, ta ? K : M, lda, lda, 1, 0, nullptr);
+        gb_fill_f32((float *)B, tb ? N : K, ldb, ldb, 2, 0, nullptr);
+    }
+    std::vector<int> cands;
+    const int64_t small = M < N ? M : N;
+    if (dtype_bits == 32) {
+        cands = {GB_ALGO_SIMT};
+        if (K >= 64) cands.push_back(GB_ALGO_BF16X3);   // meets 2*K*u only from K ~ 12; keep a margin
+    } else {
+        cands = {GB_ALGO_ORDERED, GB_ALGO_OZAKI};
+    }
+    if (small <= 64) cands.push_back(GB_ALGO_SKINNY);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int arg = cands[0];
+    float bestt = 1e30f;
+    for (int a : cands) {
+        gb_gemm_opts o;
+        gb_gemm_opts_init(&o);
+        o.algo = a;
+        float tsum = 0;
+        bool okrun = true;
+        for (int rep = 0; rep < 3 && okrun; rep++) {
+            cudaEventRecord(e0, nullptr);
+            gb_status r = dtype_bits == 64
+                              ? gb_dgemm(transA, transB, M, N, K, 1.0, (const double *)A, lda, (const double *)B, ldb,
+                                         0.0, (double *)C, N, &o)
+                              : gb_sgemm(transA, transB, M, N, K, 1.0f, (const float *)A, lda, (const float *)B, ldb,
+                                         0.0f, (float *)C, N, &o);
+            cudaEventRecord(e1, nullptr);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (r != GB_OK) okrun = false;
+            else if (rep > 0) tsum += ms;   // first run warms up
+        }
+        if (okrun && tsum / 2 < bestt) {
+            bestt = tsum / 2;
+            arg = a;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    gb_free(A);
+    gb_free(B);
+    gb_free(C);
+    gb_status sync = gb_sync(nullptr);
+    if (sync != GB_OK) return sync;
+    gb_autotune_set(dtype_bits, transA, transB, M, N, K, arg);
+    if (best) *best = arg;
+    if (best_ms) *best_ms = bestt;
+    return gb::ok();
+}
+
+gb_status gb_autotune_save(const char *path) {
+    GB_CHECK_ARG(path != nullptr, "gb_autotune_save: null path");
+    FILE *f = fopen(path, "w");
+    if (!f) return gb::set_status(GB_ERR_INVALID_ARG, "gb_autotune_save: cannot open %s", path);
+    std::lock_guard<std::mutex> lk(gb::g_tune_mu);
+    fprintf(f, "# bits ta tb log2M log2N log2K algo\n");
+    for (auto &kv : gb::g_tune)
+        fprintf(f, "%d %d %d %d %d %d %d\n", kv.first.bits, kv.first.ta, kv.first.tb, kv.first.lm, kv.first.ln,
+                kv.first.lk, kv.second);
+    fclose(f);
+    return gb::ok();
+}
+
+gb_status gb_autotune_load(const char *path) {
+    GB_CHECK_ARG(path != nullptr, "gb_autotune_load: null path");
+    FILE *f = fopen(path, "r");
+    if (!f) return gb::set_status(GB_ERR_INVALID_ARG, "gb_autotune_load: cannot open %s", path);
+    char line[256];
+    std::lock_guard<std::mutex> lk(gb::g_tune_mu);
+    while (fgets(line, sizeof(line), f)) {
+        if (line[0] == '#') continue;
+        gb::TuneKey k;
+        int a;
+        if (sscanf(line, "%d %d %d %d %d %d %d", &k.bits, &k.ta, &k.tb, &k.lm, &k.ln, &k.lk, &a) == 7 &&
+            a >= GB_ALGO_AUTO && a <= GB_ALGO_SKINNY)
+            gb::g_tune[k] = a;
+    }
+    fclose(f);
+    return gb::ok();
+}
+
+}  // extern "C"

@@ -42,8 +42,16 @@ __device__ __forceinline__ T update(T top, T left, T right, T down, T mid, int64
     return O::mul(O::add(right, O::add(O::add(left, down), O::add(top, mid))), O::fifth());
 }
 
-constexpr int NT = 512;
+constexpr int NT = 256;   // 32 columns x 8 row bands
 
+// One CTA: a TH x TW output tile, loaded with a halo of `tsweeps` cells,
+// `tsweeps` sweeps in shared memory, the final tile written back.  In each
+// sweep warp w walks row band w of the still-valid region and lane l the
+// columns l, l+32, ...; a thread keeps (top, middle, down) of its column in
+// registers while it moves down the band, so a point costs three shared
+// loads (down, left, right) and one store.  Cells on the grid boundary keep
+// their value; cells outside the grid are computed but never read by an
+// interior cell and never written back.
 template <typename T, int ORDER>
 __global__ void __launch_bounds__(NT) stencil_tb_kernel(const T *__restrict__ src, T *__restrict__ dst, int64_t M,
                                                         int64_t N, int tsweeps, int TH, int TW) {
@@ -54,36 +62,53 @@ __global__ void __launch_bounds__(NT) stencil_tb_kernel(const T *__restrict__ sr
     const int64_t ld = N + 2;
     const int64_t R0 = 1 + (int64_t)blockIdx.y * TH - tsweeps;   // padded coords of local (0,0)
     const int64_t C0 = 1 + (int64_t)blockIdx.x * TW - tsweeps;
+    const int lane = threadIdx.x % 32, band = threadIdx.x / 32;
 
-    for (int idx = threadIdx.x; idx < H * W; idx += NT) {
-        int lr = idx / W, lc = idx - lr * W;
-        int64_t r = R0 + lr, c = C0 + lc;
-        if (r >= 0 && r <= M + 1 && c >= 0 && c <= N + 1) cur[idx] = src[r * ld + c];
+    for (int lr = band; lr < H; lr += NT / 32) {
+        const int64_t r = R0 + lr;
+        if (r < 0 || r > M + 1) continue;
+        const T *srow = src + r * ld;
+        for (int lc = lane; lc < W; lc += 32) {
+            const int64_t c = C0 + lc;
+            if (c >= 0 && c <= N + 1) cur[lr * W + lc] = srow[c];
+        }
     }
     __syncthreads();
 
     for (int s = 1; s <= tsweeps; s++) {
-        const int h = H - 2 * s, w = W - 2 * s;
-        for (int idx = threadIdx.x; idx < h * w; idx += NT) {
-            int lr = s + idx / w, lc = s + idx % w;
-            int64_t r = R0 + lr, c = C0 + lc;
-            if (r < 0 || r > M + 1 || c < 0 || c > N + 1) continue;
-            const int o = lr * W + lc;
-            T v;
-            if (r == 0 || r == M + 1 || c == 0 || c == N + 1)
-                v = cur[o];   // fixed boundary
-            else
-                v = update<T, ORDER>(cur[o - W], cur[o - 1], cur[o + 1], cur[o + W], cur[o], r - 1);
-            nxt[o] = v;
+        const int h = H - 2 * s;
+        const int per = (h + NT / 32 - 1) / (NT / 32);
+        const int rbeg = s + band * per;
+        const int rend = min(rbeg + per, H - s);
+        for (int lc = s + lane; lc < W - s; lc += 32) {
+            if (rbeg >= rend) break;
+            const int64_t gc = C0 + lc;
+            const bool col_fixed = gc <= 0 || gc >= N + 1;
+            const T *cp = cur + rbeg * W + lc;
+            T *np = nxt + rbeg * W + lc;
+            T top = cp[-W], mid = cp[0];
+            int64_t gr = R0 + rbeg;
+            for (int lr = rbeg; lr < rend; lr++, cp += W, np += W, gr++) {
+                const T down = cp[W];
+                T v = update<T, ORDER>(top, cp[-1], cp[1], down, mid, gr - 1);
+                if (col_fixed || gr <= 0 || gr >= M + 1) v = mid;
+                *np = v;
+                top = mid;
+                mid = down;
+            }
         }
         __syncthreads();
         T *tmp = cur; cur = nxt; nxt = tmp;
     }
 
-    for (int idx = threadIdx.x; idx < TH * TW; idx += NT) {
-        int lr = tsweeps + idx / TW, lc = tsweeps + idx % TW;
-        int64_t r = R0 + lr, c = C0 + lc;
-        if (r >= 1 && r <= M && c >= 1 && c <= N) dst[r * ld + c] = cur[lr * W + lc];
+    for (int lr = tsweeps + band; lr < tsweeps + TH; lr += NT / 32) {
+        const int64_t r = R0 + lr;
+        if (r < 1 || r > M) continue;
+        T *drow = dst + r * ld;
+        for (int lc = tsweeps + lane; lc < tsweeps + TW; lc += 32) {
+            const int64_t c = C0 + lc;
+            if (c >= 1 && c <= N) drow[c] = cur[lr * W + lc];
+        }
     }
 }
 
@@ -97,7 +122,7 @@ gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *
     // tile and temporal depth: FP32 is HBM-bound (block 8 sweeps); FP64 is
     // bound by the FP64 pipe, where recomputing halos only costs, so t = 1.
     const int tmax = sizeof(T) == 4 ? 8 : 1;
-    const int TH = 32, TW = sizeof(T) == 4 ? 128 : 64;
+    const int TH = sizeof(T) == 4 ? 64 : 32, TW = sizeof(T) == 4 ? 128 : 64;
     // launches L with L == iters (mod 2) so the result lands in B for odd
     // iters and in A for even iters, as with one sweep per launch
     int L = (int)ceil_div(iters, tmax);

@@ -48,6 +48,45 @@ class GemmOpts(ctypes.Structure):
                 ("reserved", ctypes.c_int32 * 4)]
 
 
+class GemmDesc(ctypes.Structure):
+    _fields_ = [("dtype_bits", ctypes.c_int32), ("transA", ctypes.c_char), ("transB", ctypes.c_char),
+                ("pad", ctypes.c_char * 2), ("semantics", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("M", ctypes.c_int64), ("N", ctypes.c_int64), ("K", ctypes.c_int64),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
+                ("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64),
+                ("C", ctypes.c_void_p), ("ldc", ctypes.c_int64)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_int32), ("dtype_bits", ctypes.c_int32), ("transA", ctypes.c_char),
+                ("transB", ctypes.c_char), ("pad", ctypes.c_char * 2), ("algo", ctypes.c_int32),
+                ("semantics", ctypes.c_int32), ("iters", ctypes.c_int32), ("order", ctypes.c_int32),
+                ("reserved", ctypes.c_int32),
+                ("M", ctypes.c_int64), ("N", ctypes.c_int64), ("K", ctypes.c_int64),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double),
+                ("A", ctypes.c_void_p), ("lda", ctypes.c_int64), ("B", ctypes.c_void_p), ("ldb", ctypes.c_int64),
+                ("C", ctypes.c_void_p), ("ldc", ctypes.c_int64), ("bytes", ctypes.c_uint64),
+                ("tag", ctypes.c_uint64)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("workspace_bytes", ctypes.c_uint64),
+                ("group_max_work", ctypes.c_double), ("streams", ctypes.c_int32), ("max_batch", ctypes.c_int32),
+                ("max_inflight", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("use_grouped", ctypes.c_int32),
+                ("dry_run", ctypes.c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("rejected", ctypes.c_int64),
+                ("failed", ctypes.c_int64), ("waiting", ctypes.c_int64), ("inflight", ctypes.c_int64),
+                ("inflight_bytes", ctypes.c_uint64), ("launches", ctypes.c_int64),
+                ("grouped_launches", ctypes.c_int64), ("grouped_requests", ctypes.c_int64),
+                ("p50_s", ctypes.c_double), ("p99_s", ctypes.c_double), ("mean_s", ctypes.c_double),
+                ("req_per_s", ctypes.c_double)]
+
+
+OP_GEMM, OP_TRANSPOSE, OP_STENCIL = range(3)
+
 _i64, _vp, _int, _dbl, _flt = ctypes.c_int64, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_float
 _ul = ctypes.c_ulong
 _SIGS = {
@@ -76,6 +115,21 @@ _SIGS = {
     "gb_stencil2d_f32": ([_i64, _i64, _vp, _vp, _int, _int, _vp], _int),
     "gb_exec": ([ctypes.c_char_p, _int, _int, ctypes.POINTER(_ul)], _int),
     "gb_ref_set_stream": ([_vp], None),
+    "gb_workspace_reserve": ([ctypes.c_size_t, _vp], _int),
+    "gb_gemm_batch": ([ctypes.POINTER(GemmDesc), _int, _vp], _int),
+    "gb_server_config_init": ([ctypes.POINTER(ServerConfig)], None),
+    "gb_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)], _int),
+    "gb_server_submit": ([_vp, ctypes.POINTER(Request)], _int),
+    "gb_server_poll": ([_vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_double), _int], _int),
+    "gb_server_drain": ([_vp, _dbl], _int),
+    "gb_server_get_stats": ([_vp, ctypes.POINTER(ServerStats)], _int),
+    "gb_server_destroy": ([_vp], None),
+    "gb_autotune_gemm": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, ctypes.POINTER(_int),
+                          ctypes.POINTER(_dbl)], _int),
+    "gb_autotune_set": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, _int], _int),
+    "gb_autotune_get": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64], _int),
+    "gb_autotune_save": ([ctypes.c_char_p], _int),
+    "gb_autotune_load": ([ctypes.c_char_p], _int),
     "gb_ref_set_algo": ([_int], None),
 }
 
@@ -104,7 +158,7 @@ def declared_symbols():
     """Every function name declared in include/*.h."""
     names = set()
     for fn in sorted(os.listdir(INCLUDE_DIR)):
-        if not fn.endswith(".h"):
+        if not fn.endswith(".h") or fn.startswith("gbblas_noexport"):
             continue
         src = open(os.path.join(INCLUDE_DIR, fn)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
@@ -225,3 +279,79 @@ def ref_call(name, *args):
     f.restype = None
     f(*cargs)
     return lib().gb_get_last_status()
+
+
+# ------------------------------------------------------------- grouped / serving
+def gemm_desc(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, bits, semantics=SEM_BLAS):
+    d = GemmDesc()
+    d.dtype_bits, d.transA, d.transB, d.semantics = bits, ta.encode(), tb.encode(), semantics
+    d.M, d.N, d.K, d.alpha, d.beta = M, N, K, alpha, beta
+    d.A, d.lda, d.B, d.ldb, d.C, d.ldc = _ptr(A), lda, _ptr(B), ldb, _ptr(C), ldc
+    return d
+
+
+def gemm_batch(descs, stream=None):
+    arr = (GemmDesc * len(descs))(*descs)
+    _check(lib().gb_gemm_batch(arr, len(descs), _stream(stream)), "gb_gemm_batch")
+
+
+def request(op, bits, M, N, K=0, A=None, lda=0, B=None, ldb=0, C=None, ldc=0, ta="N", tb="N", alpha=1.0,
+            beta=0.0, algo=ALGO_AUTO, semantics=SEM_BLAS, iters=0, order=STENCIL_HOST, tag=0, nbytes=0):
+    r = Request()
+    r.op, r.dtype_bits, r.transA, r.transB = op, bits, ta.encode(), tb.encode()
+    r.algo, r.semantics, r.iters, r.order = algo, semantics, iters, order
+    r.M, r.N, r.K, r.alpha, r.beta = M, N, K, alpha, beta
+    r.A, r.lda, r.B, r.ldb, r.C, r.ldc = _ptr(A), lda, _ptr(B), ldb, _ptr(C), ldc
+    r.bytes, r.tag = nbytes, tag
+    return r
+
+
+class Server:
+    """Thin wrapper over gb_server_* (include/gbblas.h)."""
+
+    def __init__(self, **cfg):
+        c = ServerConfig()
+        lib().gb_server_config_init(ctypes.byref(c))
+        for k, v in cfg.items():
+            setattr(c, k, v)
+        h = ctypes.c_void_p()
+        _check(lib().gb_server_create(ctypes.byref(c), ctypes.byref(h)), "gb_server_create")
+        self.h = h
+
+    def submit(self, req):
+        st = lib().gb_server_submit(self.h, ctypes.byref(req))
+        if st != OK:
+            raise GBError(st, (lib().gb_last_error() or b"").decode())
+
+    def poll(self, max_n=4096):
+        tags = (ctypes.c_uint64 * max_n)()
+        lat = (ctypes.c_double * max_n)()
+        n = lib().gb_server_poll(self.h, tags, lat, max_n)
+        return [(tags[i], lat[i]) for i in range(n)]
+
+    def drain(self, timeout_s=0.0):
+        _check(lib().gb_server_drain(self.h, timeout_s), "gb_server_drain")
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().gb_server_get_stats(self.h, ctypes.byref(st)), "gb_server_get_stats")
+        return {name: getattr(st, name) for name, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            lib().gb_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def autotune_gemm(bits, ta, tb, M, N, K):
+    best = ctypes.c_int()
+    ms = ctypes.c_double()
+    _check(lib().gb_autotune_gemm(bits, ta.encode(), tb.encode(), M, N, K, ctypes.byref(best), ctypes.byref(ms)),
+           "gb_autotune_gemm")
+    return best.value, ms.value

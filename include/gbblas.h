@@ -58,8 +58,16 @@ gb_status gb_sync(void *stream);
  * C caller needs no CUDA headers.  kind: 0 host->device, 1 device->host,
  * 2 device->device (asynchronous on `stream`). */
 gb_status gb_malloc(void **ptr, size_t bytes);
+/* Memory visible to host and device (cudaMallocManaged); free with gb_free. */
+gb_status gb_malloc_managed(void **ptr, size_t bytes);
 gb_status gb_free(void *ptr);
 gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int kind, void *stream);
+
+/* The library keeps one grow-only scratch buffer per (device, stream) for
+ * split-K partials and split / sliced GEMM operands.  Growing it
+ * synchronises that stream; reserve the largest size up front to keep
+ * cudaMalloc off the call path of later calls on `stream`. */
+gb_status gb_workspace_reserve(size_t bytes, void *stream);
 
 /* ------------------------------------------------------------ inputs */
 /* Seeded counter-based generator (bit-identical to the oracle's): element
@@ -100,8 +108,8 @@ typedef struct gb_gemm_opts {
                               irr_thinB_sgemm V1.2), 0 -> two-level sum        */
     int32_t alpha_on_b;    /* ORDERED: alpha pre-scales op(B) (thinB V1.2)
                               instead of op(A) (sgemm V1.3.x)                  */
-    int32_t ozaki_slices;  /* OZAKI: slices per operand (2..8), 0 -> from
-                              target_err                                      */
+    int32_t ozaki_slices;  /* OZAKI: 7-bit slices per operand (2..9), 0 ->
+                              the fewest meeting target_err                   */
     double  target_err;    /* OZAKI: normwise error target, 0 -> 2^-52         */
     int32_t reserved[4];
 } gb_gemm_opts;
@@ -144,6 +152,30 @@ gb_status gb_sgemm_skinny_noalloc(char transA, char transB, int64_t M, int64_t N
 /* Algorithm that GB_ALGO_AUTO picks for a shape (for logging/tests). */
 int gb_gemm_pick_algo(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K);
 
+/* ------------------------------------------------------ grouped GEMM */
+/* One GEMM of a batch (same meaning as the gb_sgemm / gb_dgemm arguments). */
+typedef struct gb_gemm_desc {
+    int32_t dtype_bits;      /* 32 (FP32) or 64 (FP64)                       */
+    char    transA, transB;  /* 'N' or 'T'                                   */
+    char    pad[2];
+    int32_t semantics;       /* gb_semantics                                 */
+    int32_t reserved;
+    int64_t M, N, K;
+    double  alpha, beta;
+    const void *A; int64_t lda;
+    const void *B; int64_t ldb;
+    void       *C; int64_t ldc;
+} gb_gemm_desc;
+
+/* Run n independent GEMMs of any shapes, modes, semantics and dtypes
+ * (FP32 / FP64 mixed) in one launch of a persistent grouped kernel: the
+ * descriptors become a device work list and every CTA pulls 64 x 64 C tiles
+ * from the whole batch, so many small problems fill the GPU together.  No
+ * reference counterpart (the reference runs one problem per DSP cluster);
+ * it is the batching layer of the serving path.  n <= 4096.  Asynchronous
+ * on `stream`; the descriptors are copied before the call returns. */
+gb_status gb_gemm_batch(const gb_gemm_desc *descs, int n, void *stream);
+
 /* ------------------------------------------------------ transpose */
 /* B (N x M, ldb >= M) = A^T, A is M x N (lda >= N).  Bit-exact copy.
  * Replaces transpose/device_code/kernel.c:2002 transpose_float_32x32_dbuf
@@ -169,6 +201,83 @@ typedef enum gb_stencil_order {
  * chosen order. */
 gb_status gb_stencil2d_f64(int64_t M, int64_t N, double *A, double *B, int iters, int order, void *stream);
 gb_status gb_stencil2d_f32(int64_t M, int64_t N, float *A, float *B, int iters, int order, void *stream);
+
+/* ---------------------------------------------------------- serving */
+/* A request loop over the kernels above, for streams of independent
+ * problems: operands stay device-resident (the caller owns them), requests
+ * are admitted while the bytes of all in-flight requests fit an HBM budget
+ * (FIFO; a request larger than the whole budget is rejected with
+ * GB_ERR_OOM), small GEMMs admitted together run in one grouped launch
+ * (replayed from CUDA graphs), the rest run one launch each with the
+ * algorithm the autotune table picks, over a pool of streams.  Latency is
+ * measured from submit to the completion callback on the stream.  No
+ * reference counterpart (the reference host runs one kernel at a time). */
+typedef enum gb_op { GB_OP_GEMM = 0, GB_OP_TRANSPOSE = 1, GB_OP_STENCIL = 2 } gb_op;
+
+typedef struct gb_request {
+    int32_t op;              /* gb_op                                                 */
+    int32_t dtype_bits;      /* 32 or 64                                              */
+    char    transA, transB;  /* GEMM modes                                            */
+    char    pad[2];
+    int32_t algo;            /* GEMM gb_algo; AUTO = autotune table, then heuristic    */
+    int32_t semantics;       /* GEMM gb_semantics                                     */
+    int32_t iters, order;    /* stencil sweeps and gb_stencil_order                   */
+    int32_t reserved;
+    int64_t M, N, K;         /* GEMM op(A) M x K, op(B) K x N; transpose A M x N;
+                                stencil interior M x N                                */
+    double  alpha, beta;     /* GEMM                                                  */
+    const void *A; int64_t lda;   /* GEMM A / transpose source / stencil grid A      */
+    void       *B; int64_t ldb;   /* GEMM B / transpose destination                  */
+    void       *C; int64_t ldc;   /* GEMM C / stencil grid B                         */
+    uint64_t bytes;          /* HBM charge while in flight (0: its operand bytes)     */
+    uint64_t tag;            /* returned by gb_server_poll                            */
+} gb_request;
+
+typedef struct gb_server_config {
+    uint64_t hbm_budget_bytes;  /* admission budget (default 48 GiB)                  */
+    uint64_t workspace_bytes;   /* scratch reserved per stream at creation (0: grow)  */
+    double   group_max_work;    /* GEMMs with M*N*K <= this, min(M,N) > 64 and algo
+                                   AUTO go to grouped launches (default 512^3)        */
+    int32_t  streams;           /* device streams (default 4)                         */
+    int32_t  max_batch;         /* GEMMs per grouped launch (default 256)             */
+    int32_t  max_inflight;      /* requests in flight at once (default 2^20)          */
+    int32_t  use_graphs;        /* replay grouped launches from CUDA graphs (1)       */
+    int32_t  use_grouped;       /* group small GEMMs (1); 0 = one launch per request  */
+    int32_t  dry_run;           /* admission and bookkeeping only, no device work     */
+} gb_server_config;
+
+typedef struct gb_server_stats {
+    int64_t  submitted, completed, rejected, failed, waiting, inflight;
+    uint64_t inflight_bytes;
+    int64_t  launches, grouped_launches, grouped_requests;
+    double   p50_s, p99_s, mean_s, req_per_s;
+} gb_server_stats;
+
+typedef struct gb_server gb_server;
+
+void      gb_server_config_init(gb_server_config *cfg);
+gb_status gb_server_create(const gb_server_config *cfg, gb_server **out);
+/* Queue a request (returns at once; the operands must stay valid until the
+ * request's tag is returned by gb_server_poll or gb_server_drain returns). */
+gb_status gb_server_submit(gb_server *s, const gb_request *req);
+/* Completed requests since the last poll: tags and latencies (seconds). */
+int       gb_server_poll(gb_server *s, uint64_t *tags, double *latency_s, int max);
+/* Wait until every submitted request completed (timeout_s <= 0: no limit). */
+gb_status gb_server_drain(gb_server *s, double timeout_s);
+gb_status gb_server_get_stats(gb_server *s, gb_server_stats *out);
+void      gb_server_destroy(gb_server *s);
+
+/* Autotuner: time the candidate algorithms for a GEMM shape on scratch
+ * operands and record the fastest for its (dtype, modes, log2 M, log2 N,
+ * log2 K) bucket; GB_ALGO_AUTO requests through the server use the table.
+ * FP32 candidates: SIMT, BF16X3 (K >= 64), SKINNY (min(M,N) <= 64); FP64:
+ * ORDERED, OZAKI (slices for FP64-level error), SKINNY. */
+gb_status gb_autotune_gemm(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
+                           int *best_algo, double *best_ms);
+gb_status gb_autotune_set(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K, int algo);
+int       gb_autotune_get(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K);
+gb_status gb_autotune_save(const char *path);
+gb_status gb_autotune_load(const char *path);
 
 /* --------------------------------------------------- launch by name */
 /* The reference host drives the device by kernel name with packed

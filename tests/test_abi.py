@@ -67,7 +67,7 @@ def test_dgemm_rejects_bad_arguments(L):
     o = gbblas.opts()
     st = L.gb_dgemm(b"N", b"N", 4, 4, 4, 1.0, 8, 2, 8, 4, 0.0, 8, 4, ctypes.byref(o))
     assert st == gbblas.ERR_INVALID_ARG and b"lda" in L.gb_last_error()
-    o = gbblas.opts(algo=gbblas.ALGO_OZAKI, ozaki_slices=11)
+    o = gbblas.opts(algo=gbblas.ALGO_OZAKI, ozaki_slices=10)
     st = L.gb_dgemm(b"N", b"N", 4, 4, 4, 1.0, 8, 4, 8, 4, 0.0, 8, 4, ctypes.byref(o))
     assert st == gbblas.ERR_INVALID_ARG and b"ozaki_slices" in L.gb_last_error()
 
@@ -101,6 +101,9 @@ def test_null_kernels_are_noops(L):
 
 def test_auto_algorithm_choice(L):
     assert gbblas.pick_algo(32, "N", "N", 262144, 8, 4096) == gbblas.ALGO_SKINNY
-    assert gbblas.pick_algo(64, "T", "T", 16, 262144, 4096) == gbblas.ALGO_SKINNY
+    assert gbblas.pick_algo(64, "T", "T", 16, 262144, 4096) == gbblas.ALGO_OZAKI
+    assert gbblas.pick_algo(64, "T", "T", 16, 2000, 1000) == gbblas.ALGO_SKINNY
     assert gbblas.pick_algo(64, "N", "N", 512, 512, 512) == gbblas.ALGO_ORDERED
-    assert gbblas.pick_algo(32, "N", "N", 4096, 4096, 4096) != gbblas.ALGO_SKINNY
+    assert gbblas.pick_algo(64, "N", "N", 1024, 1024, 1024) == gbblas.ALGO_OZAKI
+    assert gbblas.pick_algo(32, "N", "N", 4096, 4096, 4096) == gbblas.ALGO_BF16X3
+    assert gbblas.pick_algo(32, "N", "N", 256, 256, 256) == gbblas.ALGO_SIMT

@@ -83,18 +83,19 @@ def test_ozaki_error_falls_with_slices(torch, kind, mode):
     C0 = oracle.fill(M, N, 43, kind=kind)
     rows, cols = np.arange(0, M, 3), np.arange(0, N, 3)
     errs = {}
-    for s in (4, 5, 6, 7, 8):
+    for s in (4, 5, 6, 7, 8, 9):
         dC = dev(C0)
         gbblas.dgemm(ta, tb, M, N, K, 1.0, dev(A), ac, dev(B), bc, 1.0, dC, N, algo=gbblas.ALGO_OZAKI,
                      ozaki_slices=s)
         errs[s], _ = oracle.normwise_error(host(dC), ta, tb, M, N, K, 1.0, A, ac, B, bc, 1.0, C0, N, rows, cols)
     assert errs[8] <= 2 * K * 2.0 ** -53, errs
     assert errs[4] > errs[6] > errs[8] or errs[8] < 1e-15, errs
-    # native FP64 (ordered DFMA) for comparison: Ozaki at 8 slices is no worse than ~4x it
+    # native FP64 (ordered DFMA) for comparison: Ozaki at 9 slices is no worse than it
     dC = dev(C0)
     gbblas.dgemm(ta, tb, M, N, K, 1.0, dev(A), ac, dev(B), bc, 1.0, dC, N, algo=gbblas.ALGO_ORDERED)
     native, _ = oracle.normwise_error(host(dC), ta, tb, M, N, K, 1.0, A, ac, B, bc, 1.0, C0, N, rows, cols)
     assert errs[8] <= 4 * native + 1e-17, (errs, native)
+    assert errs[9] <= native, (errs, native)
 
 
 @pytest.mark.parametrize("sem", [0, 1, 2])
@@ -118,3 +119,18 @@ def test_ozaki_zero_rows_and_columns(torch):
     dC = dev(np.zeros((M, N)))
     gbblas.dgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=gbblas.ALGO_OZAKI, ozaki_slices=3)
     assert np.array_equal(host(dC), A @ B)
+
+
+def test_ozaki_k_chunked_matches_unchunked_error(torch):
+    """K long enough that the slices are cut into K chunks (workspace cap):
+    still FP64-level against Dot2."""
+    import gbblas
+    M, N, K = 640, 64, 400000          # 9 slices x (640 + 128) x K x 2 B > 4 GiB
+    A = oracle.fill(M, K, 61)
+    B = oracle.fill(K, N, 62)
+    C0 = oracle.fill(M, N, 63)
+    dC = dev(C0)
+    gbblas.dgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, -1.0, dC, N, algo=gbblas.ALGO_OZAKI, ozaki_slices=9)
+    rows, cols = np.arange(0, M, 20), np.arange(0, N, 4)
+    err, _ = oracle.normwise_error(host(dC), "N", "N", M, N, K, 1.0, A, K, B, N, -1.0, C0, N, rows, cols)
+    assert err <= 2 * K * 2.0 ** -53, err

@@ -1,0 +1,189 @@
+"""Grouped persistent kernel and the serving loop on the GPU.
+
+* gb_gemm_batch: mixed FP32 / FP64, shapes, modes and semantics in one
+  launch; every result against the Dot2 oracle (normwise <= 2*K*u).
+* Server: a mixed request stream (small grouped GEMMs, large FP32 -> 3xBF16,
+  FP64 -> Ozaki, skinny, transpose, Jacobi) gives each request the same result
+  in the mix as alone -- bit-identical for transpose and Jacobi and for GEMMs
+  that take the same kernel, within the normwise GEMM tolerance otherwise --
+  with grouping + CUDA graphs on and with one launch per request.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gpu_util import dev, host, op_shape, torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return torch_cuda()
+
+
+def _gemm_case(rng, bits, M, N, K, mode, seed):
+    dt = np.float64 if bits == 64 else np.float32
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A = oracle.fill(ar, ac, seed, dtype=dt)
+    B = oracle.fill(br, bc, seed + 1, dtype=dt)
+    C = oracle.fill(M, N, seed + 2, dtype=dt)
+    return A, ac, B, bc, C
+
+
+def _err(got, mode, M, N, K, alpha, A, lda, B, ldb, beta, C0, ldc):
+    rows = np.arange(0, M, max(1, M // 50))
+    cols = np.arange(0, N, max(1, N // 50))
+    return oracle.normwise_error(got, mode[0], mode[1], M, N, K, alpha, A, lda, B, ldb, beta, C0, ldc, rows, cols)[0]
+
+
+def test_gemm_batch_mixed(torch):
+    import gbblas
+    rng = np.random.default_rng(5)
+    cases, descs, keep = [], [], []
+    for i in range(24):
+        bits = 64 if i % 3 == 0 else 32
+        M, N, K = (int(x) for x in rng.integers(1, 300, size=3))
+        mode = "NT"[i % 2] + "NT"[(i // 2) % 2]
+        sem = i % 3
+        alpha, beta = float(rng.uniform(-2, 2)), float(rng.uniform(-2, 2))
+        A, lda, B, ldb, C0 = _gemm_case(rng, bits, M, N, K, mode, 100 + 10 * i)
+        dA, dB, dC = dev(A), dev(B), dev(C0)
+        keep += [dA, dB, dC]
+        descs.append(gbblas.gemm_desc(mode[0], mode[1], M, N, K, alpha, dA, lda, dB, ldb, beta, dC, N, bits, sem))
+        cases.append((bits, mode, M, N, K, alpha, A, lda, B, ldb, beta, C0, dC, sem))
+    gbblas.gemm_batch(descs)
+    for bits, mode, M, N, K, alpha, A, lda, B, ldb, beta, C0, dC, sem in cases:
+        got = host(dC).astype(np.float64)
+        if sem == gbblas.SEM_BLAS:
+            e = _err(got, mode, M, N, K, alpha, A, lda, B, ldb, beta, C0, N)
+        else:   # scalar beta: compare alpha*AB against the oracle after removing the scalar terms
+            base = C0.astype(np.float64) if sem == gbblas.SEM_ACCUM_SCALAR_BETA else 0.0
+            e = _err(got - base - beta, mode, M, N, K, alpha, A, lda, B, ldb, 0.0, None, N)
+        u = 2.0 ** -53 if bits == 64 else 2.0 ** -24
+        assert e <= 2 * max(K, 1) * u + 1e-300, (bits, mode, M, N, K, sem, e)
+
+
+def _requests(rng):
+    """(kind, bits, shape) of a mixed stream covering every route of the server."""
+    reqs = []
+    for i in range(12):
+        n = int(rng.integers(64, 300))
+        reqs.append(("gemm", 32 if i % 3 else 64, (n, n + 5, n + 9), "NT"[i % 2] + "NT"[(i // 2) % 2]))
+    reqs.append(("gemm", 32, (1024, 1024, 1024), "NN"))     # 3xBF16 by AUTO
+    reqs.append(("gemm", 64, (700, 600, 800), "TN"))       # Ozaki by AUTO
+    reqs.append(("gemm", 32, (3000, 16, 2000), "NN"))      # skinny thinB
+    reqs.append(("gemm", 32, (8, 5000, 1500), "TT"))       # skinny shortA
+    reqs.append(("gemm", 64, (2500, 8, 900), "NT"))        # skinny FP64
+    reqs.append(("transpose", 32, (700, 333), None))
+    reqs.append(("transpose", 64, (257, 1030), None))
+    reqs.append(("stencil", 32, (300, 200), 17))
+    reqs.append(("stencil", 64, (129, 250), 4))
+    return reqs
+
+
+def _materialize(reqs):
+    import gbblas
+    out = []
+    for j, (kind, bits, shape, extra) in enumerate(reqs):
+        dt = np.float64 if bits == 64 else np.float32
+        if kind == "gemm":
+            M, N, K = shape
+            A, lda, B, ldb, C0 = _gemm_case(None, bits, M, N, K, extra, 500 + 10 * j)
+            out.append(dict(kind=kind, bits=bits, shape=shape, mode=extra, A=A, lda=lda, B=B, ldb=ldb, C0=C0,
+                            alpha=0.5 + j * 0.01, beta=-1.25))
+        elif kind == "transpose":
+            M, N = shape
+            out.append(dict(kind=kind, bits=bits, shape=shape, A=oracle.fill(M, N, 900 + j, dtype=dt)))
+        else:
+            M, N = shape
+            G = np.ones((M + 2, N + 2), dtype=dt)
+            G[1:-1, 1:-1] = oracle.fill(M, N, 950 + j, kind=1, dtype=dt)
+            out.append(dict(kind=kind, bits=bits, shape=shape, iters=extra, G=G))
+    return out
+
+
+def _device_set(items):
+    dv = []
+    for it in items:
+        if it["kind"] == "gemm":
+            dv.append(dict(A=dev(it["A"]), B=dev(it["B"]), C=dev(it["C0"])))
+        elif it["kind"] == "transpose":
+            M, N = it["shape"]
+            dv.append(dict(A=dev(it["A"]), B=dev(np.zeros((N, M), dtype=it["A"].dtype))))
+        else:
+            dv.append(dict(A=dev(it["G"]), B=dev(it["G"])))
+    return dv
+
+
+def _as_request(it, d, tag):
+    import gbblas
+    if it["kind"] == "gemm":
+        M, N, K = it["shape"]
+        return gbblas.request(gbblas.OP_GEMM, it["bits"], M, N, K, A=d["A"], lda=it["lda"], B=d["B"], ldb=it["ldb"],
+                              C=d["C"], ldc=N, ta=it["mode"][0], tb=it["mode"][1], alpha=it["alpha"],
+                              beta=it["beta"], tag=tag)
+    if it["kind"] == "transpose":
+        M, N = it["shape"]
+        return gbblas.request(gbblas.OP_TRANSPOSE, it["bits"], M, N, A=d["A"], lda=N, B=d["B"], ldb=M, tag=tag)
+    M, N = it["shape"]
+    return gbblas.request(gbblas.OP_STENCIL, it["bits"], M, N, A=d["A"], C=d["B"], iters=it["iters"], tag=tag)
+
+
+def _result(it, d):
+    if it["kind"] == "gemm":
+        return host(d["C"])
+    if it["kind"] == "transpose":
+        return host(d["B"])
+    return host(d["B"] if it["iters"] % 2 else d["A"])
+
+
+@pytest.mark.parametrize("grouped,graphs,streams", [(1, 1, 4), (0, 0, 1)])
+def test_server_results_same_alone_and_in_mix(torch, grouped, graphs, streams):
+    import gbblas
+    rng = np.random.default_rng(11)
+    items = _materialize(_requests(rng))
+    # alone: each request through its own server, drained before the next
+    alone = []
+    with gbblas.Server(streams=1, use_grouped=grouped, use_graphs=graphs) as s:
+        for j, it in enumerate(items):
+            d = _device_set([it])[0]
+            s.submit(_as_request(it, d, j))
+            s.drain(60.0)
+            alone.append(_result(it, d))
+    # in the mix: everything submitted at once
+    dvs = _device_set(items)
+    with gbblas.Server(streams=streams, use_grouped=grouped, use_graphs=graphs) as s:
+        for j, (it, d) in enumerate(zip(items, dvs)):
+            s.submit(_as_request(it, d, j))
+        s.drain(120.0)
+        st = s.stats()
+        done = sorted(t for t, _ in s.poll())
+    assert st["completed"] == len(items) and st["failed"] == 0 and done == list(range(len(items)))
+    if grouped:
+        assert st["grouped_requests"] >= 6 and st["grouped_launches"] >= 1
+    for j, (it, d) in enumerate(zip(items, dvs)):
+        mix = _result(it, d)
+        if it["kind"] != "gemm":
+            assert mix.tobytes() == alone[j].tobytes(), (j, it["kind"])
+            continue
+        M, N, K = it["shape"]
+        u = 2.0 ** -53 if it["bits"] == 64 else 2.0 ** -24
+        e_mix = _err(mix.astype(np.float64), it["mode"], M, N, K, it["alpha"], it["A"], it["lda"], it["B"], it["ldb"],
+                     it["beta"], it["C0"], N)
+        e_alone = _err(alone[j].astype(np.float64), it["mode"], M, N, K, it["alpha"], it["A"], it["lda"], it["B"],
+                       it["ldb"], it["beta"], it["C0"], N)
+        assert e_mix <= 2 * K * u and e_alone <= 2 * K * u, (j, it["shape"], e_mix, e_alone)
+        if not grouped:   # same kernel either way: identical bits
+            assert mix.tobytes() == alone[j].tobytes(), j
+
+
+def test_autotune_picks_a_working_algorithm(torch):
+    import gbblas
+    best, ms = gbblas.autotune_gemm(32, "N", "N", 1024, 1024, 1024)
+    assert best in (gbblas.ALGO_SIMT, gbblas.ALGO_BF16X3) and ms > 0
+    assert gbblas.lib().gb_autotune_get(32, b"N", b"N", 1024, 1024, 1024) == best
+    best64, _ = gbblas.autotune_gemm(64, "N", "N", 600, 600, 600)
+    assert best64 in (gbblas.ALGO_ORDERED, gbblas.ALGO_OZAKI)

@@ -70,9 +70,15 @@ def test_noalloc_matches_skinny_entry_point_two_calls(torch):
 def test_noalloc_rejects_plans_beyond_the_fixed_scratch(torch):
     import gbblas
     L = gbblas.lib()
-    # the plan is a 16-way split over 5000 rows x 64 columns of FP32 partials = 20.5 MB > 16 MiB
-    M, N, K = 5000, 64, 400000
-    z = torch.zeros(1, dtype=torch.float32, device="cuda:0")
-    st = _noalloc(L, "N", "N", M, N, K, 1.0, z, K, z, N, 0.0, z, N)
+    # thinB with op(A) stored K x M (the K-major kernel, 256 rows per CTA):
+    # 5000 rows make 20 row tiles, so the plan splits K 16 ways and needs
+    # 16 x 5000 x 64 x 4 B = 20.5 MB of partials > 16 MiB.  The buffers are
+    # full size, so the call is memory-safe even if a plan ever fits.
+    M, N, K = 5000, 64, 4096
+    A = torch.zeros((K, M), dtype=torch.float32, device="cuda:0")
+    B = torch.zeros((K, N), dtype=torch.float32, device="cuda:0")
+    C = torch.zeros((M, N), dtype=torch.float32, device="cuda:0")
+    st = _noalloc(L, "T", "N", M, N, K, 1.0, A, M, B, N, 0.0, C, N)
     assert st == gbblas.ERR_INVALID_ARG
     assert b"16777216" in L.gb_last_error()
+    assert L.gb_sync(None) == gbblas.OK
