@@ -611,9 +611,11 @@ def run_skinny(ctx):
     C = torch.empty((M, N), dtype=dt, device=ctx.dev)
     gb.fill(C, M, N, N, 25, 0, bits, stream=ctx.stream)
 
+    skinny_algo = {"skinny": gb.ALGO_SKINNY, "auto": gb.ALGO_AUTO, "bf16x3": gb.ALGO_BF16X3}[args.skinny_algo]
+
     def gemm(mode):
         A, lda, B, ldb = ops[mode]
-        gb.gemm(mode[0], mode[1], M, N, K, 1.0, A, lda, B, ldb, 1.0, C, N, bits, algo=gb.ALGO_SKINNY,
+        gb.gemm(mode[0], mode[1], M, N, K, 1.0, A, lda, B, ldb, 1.0, C, N, bits, algo=skinny_algo,
                 stream=ctx.stream)
 
     for _ in range(args.warmup):
@@ -655,7 +657,7 @@ def run_skinny(ctx):
 
     e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 3)), len(MODES) * nbytes_alg, 1e9)
     config = {"workload": "%s FP%d M=%d N=%d K=%d, NN/NT/TN/TT, U[-1,1] seed 2" % (args.workload, bits, M, N, K),
-              "M": M, "N": N, "K": K, "modes": list(MODES), "algo": "skinny",
+              "M": M, "N": N, "K": K, "modes": list(MODES), "algo": args.skinny_algo,
               "bytes_per_gemm": nbytes_alg, "parallelism": "replicas x%d" % ctx.world,
               "l2": "inputs larger than L2 (large operand %d MB)" % (s * big * K // 10 ** 6)}
     line = base_line(ctx, "HBM GB/s (%s)" % args.workload, value, "GB/s", ms, args.steps, "f%d" % bits, config)
@@ -982,6 +984,7 @@ def main():
     ap.add_argument("--algo", default="best", choices=["best", "bf16x3", "simt"])
     ap.add_argument("--bits", type=int, default=32, choices=[32, 64])
     ap.add_argument("--n", type=int, default=8, help="small dimension of thinb/shorta")
+    ap.add_argument("--skinny-algo", default="auto", choices=["auto", "skinny", "bf16x3"])
     ap.add_argument("--iters", type=int, default=200, help="jacobi sweeps")
     ap.add_argument("--slices", type=int, default=0, help="dgemm: Ozaki slices (0: fewest matching native error)")
     ap.add_argument("--size", type=int, default=0, help="dgemm: M=N=K (default 8192)")

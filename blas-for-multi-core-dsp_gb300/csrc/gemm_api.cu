@@ -53,11 +53,16 @@ int pick(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
     const int64_t large = M < N ? N : M;
     const double work = (double)M * (double)N * (double)K;
     if (bits == 64) {
+        // Ozaki pads the small side of a skinny product to 128: below 32 the
+        // native FP64 streaming kernel is faster
+        const bool skinny = small <= 64 && large >= 4 * small && large >= 1024;
+        if (skinny && small < 32) return GB_ALGO_SKINNY;
         if (work > 134217728.0) return GB_ALGO_OZAKI;   // 2^27 = 512^3
-        if (small <= 64 && large >= 4 * small && large >= 1024) return GB_ALGO_SKINNY;
+        if (skinny) return GB_ALGO_SKINNY;
         return GB_ALGO_ORDERED;
     }
-    if (small <= 64 && large >= 4 * small && large >= 1024) return GB_ALGO_SKINNY;
+    if (small <= 64 && large >= 4 * small && large >= 1024)   // FP32 skinny: FFMA streaming up to 16,
+        return (small > 16 && K >= 64) ? GB_ALGO_BF16X3 : GB_ALGO_SKINNY;   // tensor cores beyond
     if (K >= 64 && work > 134217728.0) return GB_ALGO_BF16X3;
     return GB_ALGO_SIMT;
 }

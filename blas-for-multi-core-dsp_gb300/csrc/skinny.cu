@@ -14,11 +14,13 @@
 //
 // Two kernels, by the layout of X:
 //  * X row-major (K contiguous): each warp streams R rows along K with
-//    16-byte loads (lane l holds k = 32*V*step + V*l .. +V-1), multiplies by
-//    the W slab kept lane-contiguous in shared memory (conflict-free), and
-//    reduces across lanes with shuffles at the end.
-//  * X K-major (rows contiguous): each thread owns R rows, loads are
-//    coalesced across lanes, W is read by broadcast from shared memory.
+//    16-byte loads (lane l holds k = 32*V*step + V*l .. +V-1), the next
+//    step's loads in flight while the current step is multiplied by W read
+//    straight from L1 (every CTA reads the same small W); lanes reduce with
+//    shuffles at the end.  No shared memory, no block barriers.
+//  * X K-major (rows contiguous): each thread owns groups of 4 consecutive
+//    rows loaded 16 bytes at a time, W is staged per K slab in shared memory
+//    and read by broadcast.
 // Split-K over CTAs when the row count alone cannot fill the GPU; partial
 // sums go to scratch and a second kernel applies alpha/beta.
 #include "gb_common.cuh"
@@ -40,21 +42,25 @@ struct SkParams {
     void *part;                           // splits x rows x NB partials (split-K only)
 };
 
-// row-major X: R rows per warp, W slab of SLAB k's (<= 32 KB of shared memory)
+// row-major X: R rows per warp, lane l covers k = 32*V*step + V*l .. +V-1
 template <typename T, int NB>
 struct RowCfg {
     static constexpr int V = 16 / (int)sizeof(T);   // elements per 16-byte load
     static constexpr int KS = 32 * V;               // k per warp step
-    static constexpr int R = NB <= 8 ? 8 : NB <= 16 ? 4 : NB <= 32 ? 2 : 1;
-    static constexpr int STEPS = (32768 / (int)sizeof(T) / NB) / KS;
-    static constexpr int SLAB = STEPS * KS;
+    static constexpr int R = NB <= 8 ? 8 : NB <= 16 ? 4 : 1;
     static constexpr int BR = (NT / 32) * R;        // rows per CTA
 };
 
-// K-major X: R rows per thread
+// K-major X: each thread owns G groups of VR consecutive rows (one vector
+// load across rows), sized so R * NB stays near 64 accumulators; a CTA
+// covers NT * VR * G rows
 template <typename T, int NB>
 struct ColCfg {
-    static constexpr int R = NB <= 16 ? 4 : NB <= 32 ? 2 : 1;
+    static constexpr int R0 = (64 * 4 / (int)sizeof(T)) / NB;      // accumulator budget in rows
+    static constexpr int VMAX = 16 / (int)sizeof(T);
+    static constexpr int VR = R0 >= VMAX ? VMAX : (R0 >= 2 ? 2 : 1);   // rows per vector load
+    static constexpr int G = R0 / VR >= 2 ? 2 : 1;
+    static constexpr int R = VR * G;                // rows per thread
     static constexpr int SLAB = 32768 / (int)sizeof(T) / NB;
     static constexpr int BR = NT * R;
     static constexpr int U = 4;                     // k unroll (loads in flight)
@@ -91,12 +97,104 @@ __device__ __forceinline__ void stage_w(const SkParams &p, T *Ws, int64_t k0, in
     }
 }
 
-template <typename T, int NB, bool VEC>
+template <typename T, int V>
+struct VecT;
+template <>
+struct VecT<float, 4> {
+    __device__ static void load(const float *p, float *o) {
+        float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+        o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+    }
+};
+template <>
+struct VecT<double, 2> {
+    __device__ static void load(const double *p, double *o) {
+        double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+        o[0] = v.x; o[1] = v.y;
+    }
+};
+template <>
+struct VecT<float, 2> {
+    __device__ static void load(const float *p, float *o) {
+        float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+        o[0] = v.x; o[1] = v.y;
+    }
+};
+template <typename T>
+struct VecT<T, 1> {
+    __device__ static void load(const T *p, T *o) { o[0] = __ldg(p); }
+};
+
+// X rows [r0, r0+R) at k = kb .. kb+V-1 into xv (zero beyond rows / kend).
+template <typename T, int R, int V, bool VEC>
+__device__ __forceinline__ void load_x_rows(const SkParams &p, const T *X, int64_t r0, int64_t kb, int64_t kend,
+                                            T (&xv)[R][V]) {
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int64_t row = r0 + i;
+        const T *xp = X + row * p.ldx + kb;
+        if (VEC && row < p.rows && kb + V <= kend) {
+            VecT<T, V>::load(xp, xv[i]);
+        } else {
+#pragma unroll
+            for (int q = 0; q < V; q++) xv[i][q] = (row < p.rows && kb + q < kend) ? xp[q] : T(0);
+        }
+    }
+}
+
+// acc += X(rows, kb..kb+V-1) * W(kb..kb+V-1, :).  W comes from L1 / L2 (it
+// is small and every CTA reads it): 16-byte loads along W's contiguous
+// dimension when WVEC, else guarded scalar loads.
+template <typename T, int NB, int R, int V, bool WVEC>
+__device__ __forceinline__ void fma_step(const SkParams &p, const T *W, int64_t kb, int64_t kend, const T (&xv)[R][V],
+                                         T (&acc)[R][NB]) {
+    if (WVEC && kb + V <= kend) {
+        if (p.tw) {            // W stored n x K: V consecutive k of column j
+#pragma unroll
+            for (int j = 0; j < NB; j++) {
+                T w[V];
+                VecT<T, V>::load(W + (int64_t)j * p.ldw + kb, w);
+#pragma unroll
+                for (int q = 0; q < V; q++)
+#pragma unroll
+                    for (int i = 0; i < R; i++) acc[i][j] = fma(xv[i][q], w[q], acc[i][j]);
+                if (NB > 16 && (j & 15) == 15) asm volatile("" ::: "memory");   // bound load hoisting
+            }
+        } else {               // W stored K x n (n == NB): row k holds NB consecutive values
+#pragma unroll
+            for (int q = 0; q < V; q++) {
+#pragma unroll
+                for (int j0 = 0; j0 < NB; j0 += V) {
+                    T w[V];
+                    VecT<T, V>::load(W + (kb + q) * p.ldw + j0, w);
+#pragma unroll
+                    for (int jj = 0; jj < V; jj++)
+#pragma unroll
+                        for (int i = 0; i < R; i++) acc[i][j0 + jj] = fma(xv[i][q], w[jj], acc[i][j0 + jj]);
+                    if (NB > 16 && (j0 & 15) == 16 - V) asm volatile("" ::: "memory");
+                }
+            }
+        }
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < V; q++) {
+        const int64_t k = kb + q;
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            T w = T(0);
+            if (k < kend && j < p.n) w = p.tw ? __ldg(W + (int64_t)j * p.ldw + k) : __ldg(W + k * p.ldw + j);
+#pragma unroll
+            for (int i = 0; i < R; i++) acc[i][j] = fma(xv[i][q], w, acc[i][j]);
+        }
+    }
+}
+
+template <typename T, int NB, bool VEC, bool WVEC>
 __global__ void __launch_bounds__(NT) skinny_rows_kernel(SkParams p) {
     using C = RowCfg<T, NB>;
     constexpr int V = C::V, KS = C::KS, R = C::R;
-    __shared__ __align__(16) T Ws[C::SLAB * NB];   // [step][q][j][lane]
-    const T *X = (const T *)p.X;
+    const T *X = (const T *)p.X, *W = (const T *)p.W;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int64_t r0 = (int64_t)blockIdx.x * C::BR + warp * R;
     const int split = blockIdx.y;
@@ -109,52 +207,20 @@ __global__ void __launch_bounds__(NT) skinny_rows_kernel(SkParams p) {
 #pragma unroll
         for (int j = 0; j < NB; j++) acc[i][j] = T(0);
 
-    for (int64_t k0 = kbeg; k0 < kend; k0 += C::SLAB) {
-        const int cnt = (int)((kend - k0) < C::SLAB ? (kend - k0) : C::SLAB);
-        __syncthreads();
-        // Ws[((s*V + q)*NB + j)*32 + l] holds W(k0 + s*KS + l*V + q, j)
-        stage_w<T, NB>(p, Ws, k0, C::SLAB, kend, [](int e, int &kk, int &j) {
-            const int l = e % 32, r1 = e / 32;
-            j = r1 % NB;
-            const int r2 = r1 / NB, q = r2 % V, st = r2 / V;
-            kk = st * KS + l * V + q;
-        });
-        __syncthreads();
-        const int steps = (cnt + KS - 1) / KS;
-        for (int s = 0; s < steps; s++) {
-            const int64_t kb = k0 + (int64_t)s * KS + lane * V;
-            T xv[R][V];
-#pragma unroll
-            for (int i = 0; i < R; i++) {
-                const int64_t row = r0 + i;
-                const T *xp = X + row * p.ldx + kb;
-                if (VEC && row < p.rows && kb + V <= kend) {
-                    if (sizeof(T) == 4) {
-                        float4 v = __ldg(reinterpret_cast<const float4 *>(xp));
-                        reinterpret_cast<float *>(xv[i])[0] = v.x;
-                        reinterpret_cast<float *>(xv[i])[1] = v.y;
-                        reinterpret_cast<float *>(xv[i])[2] = v.z;
-                        reinterpret_cast<float *>(xv[i])[3] = v.w;
-                    } else {
-                        double2 v = __ldg(reinterpret_cast<const double2 *>(xp));
-                        reinterpret_cast<double *>(xv[i])[0] = v.x;
-                        reinterpret_cast<double *>(xv[i])[1] = v.y;
-                    }
-                } else {
-#pragma unroll
-                    for (int q = 0; q < V; q++) xv[i][q] = (row < p.rows && kb + q < kend) ? xp[q] : T(0);
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < V; q++)
-#pragma unroll
-                for (int j = 0; j < NB; j++) {
-                    const T w = Ws[((s * V + q) * NB + j) * 32 + lane];
-#pragma unroll
-                    for (int i = 0; i < R; i++) acc[i][j] = fma(xv[i][q], w, acc[i][j]);
-                }
-        }
+    // two register buffers, the next step's X loads in flight while the
+    // current step's FMAs run
+    const int64_t nsteps = (kend - kbeg + KS - 1) / KS;
+    T xa[R][V], xb[R][V];
+    const int64_t kl = kbeg + lane * V;
+    if (nsteps > 0) load_x_rows<T, R, V, VEC>(p, X, r0, kl, kend, xa);
+    int64_t st = 0;
+    for (; st + 1 < nsteps; st += 2) {
+        load_x_rows<T, R, V, VEC>(p, X, r0, kl + (st + 1) * KS, kend, xb);
+        fma_step<T, NB, R, V, WVEC>(p, W, kl + st * KS, kend, xa, acc);
+        if (st + 2 < nsteps) load_x_rows<T, R, V, VEC>(p, X, r0, kl + (st + 2) * KS, kend, xa);
+        fma_step<T, NB, R, V, WVEC>(p, W, kl + (st + 1) * KS, kend, xb, acc);
     }
+    if (st < nsteps) fma_step<T, NB, R, V, WVEC>(p, W, kl + st * KS, kend, xa, acc);
 
 #pragma unroll
     for (int i = 0; i < R; i++)
@@ -180,18 +246,18 @@ __global__ void __launch_bounds__(NT) skinny_rows_kernel(SkParams p) {
     }
 }
 
-template <typename T, int NB>
+template <typename T, int NB, bool VEC>
 __global__ void __launch_bounds__(NT) skinny_cols_kernel(SkParams p) {
     using C = ColCfg<T, NB>;
-    constexpr int R = C::R, U = C::U;
-    __shared__ __align__(16) T Ws[C::SLAB * NB];   // [k][j]
+    constexpr int VR = C::VR, G = C::G, R = C::R, U = C::U;
+    __shared__ __align__(16) T Ws[C::SLAB * NB];   // [k][j], read by broadcast
     const T *X = (const T *)p.X;
     const int tid = threadIdx.x;
-    const int64_t r0 = (int64_t)blockIdx.x * C::BR;
+    const int64_t cta0 = (int64_t)blockIdx.x * C::BR;
     const int split = blockIdx.y;
     const int64_t kbeg = (int64_t)split * p.kchunk;
     const int64_t kend = kbeg + p.kchunk < p.K ? kbeg + p.kchunk : p.K;
-
+    // rows of group g: cta0 + (g*NT + tid)*VR .. +VR-1 (consecutive threads, consecutive 16-byte chunks)
     T acc[R][NB];
 #pragma unroll
     for (int i = 0; i < R; i++)
@@ -211,9 +277,16 @@ __global__ void __launch_bounds__(NT) skinny_cols_kernel(SkParams p) {
 #pragma unroll
             for (int u = 0; u < U; u++)
 #pragma unroll
-                for (int i = 0; i < R; i++) {
-                    const int64_t row = r0 + tid + i * NT;
-                    x[u][i] = (kk + u < cnt && row < p.rows) ? __ldg(X + (k0 + kk + u) * p.ldx + row) : T(0);
+                for (int g = 0; g < G; g++) {
+                    const int64_t rb = cta0 + ((int64_t)g * NT + tid) * VR;
+                    const T *xp = X + (k0 + kk + u) * p.ldx + rb;
+                    const bool kin = kk + u < cnt;
+                    if (VEC && kin && rb + VR <= p.rows) {
+                        VecT<T, VR>::load(xp, &x[u][g * VR]);
+                    } else {
+#pragma unroll
+                        for (int v = 0; v < VR; v++) x[u][g * VR + v] = (kin && rb + v < p.rows) ? xp[v] : T(0);
+                    }
                 }
 #pragma unroll
             for (int u = 0; u < U; u++)
@@ -227,19 +300,22 @@ __global__ void __launch_bounds__(NT) skinny_cols_kernel(SkParams p) {
     }
 
 #pragma unroll
-    for (int i = 0; i < R; i++) {
-        const int64_t row = r0 + tid + i * NT;
-        if (row >= p.rows) continue;
-        if (p.splits > 1) {
-            T *part = (T *)p.part + ((int64_t)split * p.rows + row) * NB;
+    for (int g = 0; g < G; g++)
 #pragma unroll
-            for (int j = 0; j < NB; j++) part[j] = acc[i][j];
-            continue;
+        for (int v = 0; v < VR; v++) {
+            const int i = g * VR + v;
+            const int64_t row = cta0 + ((int64_t)g * NT + tid) * VR + v;
+            if (row >= p.rows) continue;
+            if (p.splits > 1) {
+                T *part = (T *)p.part + ((int64_t)split * p.rows + row) * NB;
+#pragma unroll
+                for (int j = 0; j < NB; j++) part[j] = acc[i][j];
+                continue;
+            }
+#pragma unroll
+            for (int j = 0; j < NB; j++)
+                if (j < p.n) epilogue_store<T>(p, row, j, acc[i][j]);
         }
-#pragma unroll
-        for (int j = 0; j < NB; j++)
-            if (j < p.n) epilogue_store<T>(p, row, j, acc[i][j]);
-    }
 }
 
 template <typename T, int NB>
@@ -256,7 +332,7 @@ __global__ void skinny_reduce_kernel(SkParams p) {
 
 // Launch plan shared by the workspace path and the fixed-scratch path.
 struct Plan {
-    bool rows_kernel, vec;
+    bool rows_kernel, vec, wvec;
     int64_t rtiles;
     size_t part_bytes;
 };
@@ -265,7 +341,7 @@ template <typename T, int NB>
 gb_status make_plan(SkParams &p, Plan &pl) {
     pl.rows_kernel = !p.tx;
     const int64_t br = pl.rows_kernel ? RowCfg<T, NB>::BR : ColCfg<T, NB>::BR;
-    const int64_t gran = pl.rows_kernel ? RowCfg<T, NB>::KS : 32;
+    const int64_t gran = pl.rows_kernel ? RowCfg<T, NB>::KS : ColCfg<T, NB>::U;
     pl.rtiles = ceil_div(p.rows, br);
     if (pl.rtiles > 0x7fffffff) return set_status(GB_ERR_UNSUPPORTED, "skinny: too many rows");
     // split K until the grid covers ~2 waves of the GPU
@@ -276,7 +352,16 @@ gb_status make_plan(SkParams &p, Plan &pl) {
     p.splits = (int)ceil_div(p.K, p.kchunk);
     if (p.splits < 1) p.splits = 1;
     constexpr int V = RowCfg<T, NB>::V;
-    pl.vec = pl.rows_kernel && (p.ldx % V == 0) && ((uintptr_t)p.X % 16 == 0);
+    if (pl.rows_kernel) {
+        pl.vec = (p.ldx % V == 0) && ((uintptr_t)p.X % 16 == 0);
+        // W vector loads: n x K storage needs ldw % V == 0; K x n storage
+        // additionally needs the full NB columns present (n == NB)
+        pl.wvec = (p.ldw % V == 0) && ((uintptr_t)p.W % 16 == 0) && (p.tw || p.n == NB);
+    } else {
+        constexpr int VR = ColCfg<T, NB>::VR;
+        pl.vec = (p.ldx % VR == 0) && ((uintptr_t)p.X % 16 == 0);
+        pl.wvec = false;
+    }
     pl.part_bytes = p.splits > 1 ? (size_t)p.splits * p.rows * NB * sizeof(T) : 0;
     return ok();
 }
@@ -285,10 +370,12 @@ template <typename T, int NB>
 gb_status launch_plan(const SkParams &p, const Plan &pl, cudaStream_t st) {
     dim3 grid((unsigned)pl.rtiles, (unsigned)p.splits);
     if (pl.rows_kernel) {
-        if (pl.vec) skinny_rows_kernel<T, NB, true><<<grid, NT, 0, st>>>(p);
-        else skinny_rows_kernel<T, NB, false><<<grid, NT, 0, st>>>(p);
+        if (pl.vec && pl.wvec) skinny_rows_kernel<T, NB, true, true><<<grid, NT, 0, st>>>(p);
+        else if (pl.vec) skinny_rows_kernel<T, NB, true, false><<<grid, NT, 0, st>>>(p);
+        else skinny_rows_kernel<T, NB, false, false><<<grid, NT, 0, st>>>(p);
     } else {
-        skinny_cols_kernel<T, NB><<<grid, NT, 0, st>>>(p);
+        if (pl.vec) skinny_cols_kernel<T, NB, true><<<grid, NT, 0, st>>>(p);
+        else skinny_cols_kernel<T, NB, false><<<grid, NT, 0, st>>>(p);
     }
     GB_LAUNCH_CHECK("skinny kernel");
     if (p.splits > 1) {

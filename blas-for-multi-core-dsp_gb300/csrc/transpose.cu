@@ -37,6 +37,51 @@ __global__ void __launch_bounds__(TILE * ROWS) transpose_kernel(const T *__restr
     }
 }
 
+// FP32: each thread moves 2 x 2 blocks, so the global reads (two rows of A)
+// and writes (two rows of B) are 8-byte accesses like the FP64 kernel's.
+// Needs lda, ldb even and 8-byte aligned bases; edges fall back to scalars.
+constexpr int T2 = 64;
+__global__ void __launch_bounds__(256) transpose2x2_kernel(const float *__restrict__ A, int64_t lda,
+                                                           float *__restrict__ B, int64_t ldb, int64_t M, int64_t N) {
+    __shared__ float tile[T2][T2 + 1];
+    const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;   // 32 x 8
+    const int64_t r0 = (int64_t)blockIdx.y * T2, c0 = (int64_t)blockIdx.x * T2;
+    const bool full = r0 + T2 <= M && c0 + T2 <= N;
+#pragma unroll
+    for (int i = 0; i < T2; i += 16) {
+        const int rr = ty * 2 + i, cc = tx * 2;
+        const int64_t r = r0 + rr, c = c0 + cc;
+        if (full) {
+            float2 u = *reinterpret_cast<const float2 *>(A + r * lda + c);
+            float2 v = *reinterpret_cast<const float2 *>(A + (r + 1) * lda + c);
+            tile[rr][cc] = u.x; tile[rr][cc + 1] = u.y;
+            tile[rr + 1][cc] = v.x; tile[rr + 1][cc + 1] = v.y;
+        } else {
+#pragma unroll
+            for (int a = 0; a < 2; a++)
+#pragma unroll
+                for (int b = 0; b < 2; b++)
+                    if (r + a < M && c + b < N) tile[rr + a][cc + b] = A[(r + a) * lda + c + b];
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < T2; i += 16) {
+        const int bc = ty * 2 + i, br = tx * 2;   // B row c0+bc (+1), columns r0+br (+1)
+        const int64_t row = c0 + bc, col = r0 + br;
+        if (full) {
+            *reinterpret_cast<float2 *>(B + row * ldb + col) = make_float2(tile[br][bc], tile[br + 1][bc]);
+            *reinterpret_cast<float2 *>(B + (row + 1) * ldb + col) = make_float2(tile[br][bc + 1], tile[br + 1][bc + 1]);
+        } else {
+#pragma unroll
+            for (int a = 0; a < 2; a++)
+#pragma unroll
+                for (int b = 0; b < 2; b++)
+                    if (row + a < N && col + b < M) B[(row + a) * ldb + col + b] = tile[br + b][bc + a];
+        }
+    }
+}
+
 template <typename T>
 gb_status transpose(int64_t M, int64_t N, const T *A, int64_t lda, T *B, int64_t ldb, void *stream) {
     GB_CHECK_ARG(M >= 0 && N >= 0, "transpose: negative size");
@@ -47,6 +92,11 @@ gb_status transpose(int64_t M, int64_t N, const T *A, int64_t lda, T *B, int64_t
     GB_CHECK_ARG((const void *)A != (const void *)B, "transpose: in-place transpose is not supported");
     dim3 grid((unsigned)ceil_div(N, TILE), (unsigned)ceil_div(M, TILE));
     GB_CHECK_ARG(grid.y <= 65535u, "transpose: M too large");
+    if (sizeof(T) == 4 && lda % 2 == 0 && ldb % 2 == 0 && (uintptr_t)A % 8 == 0 && (uintptr_t)B % 8 == 0) {
+        transpose2x2_kernel<<<grid, 256, 0, as_stream(stream)>>>((const float *)A, lda, (float *)B, ldb, M, N);
+        GB_LAUNCH_CHECK("transpose2x2_kernel");
+        return ok();
+    }
     transpose_kernel<T><<<grid, dim3(TILE, ROWS), 0, as_stream(stream)>>>(A, lda, B, ldb, M, N);
     GB_LAUNCH_CHECK("transpose_kernel");
     return ok();
