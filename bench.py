@@ -187,7 +187,14 @@ class Ctx:
         clocks = sampler.stop()
         ms = self.max_over_ranks(t0.elapsed_time(t1))
         kms = statistics.mean(a.elapsed_time(b) for a, b in evs) if evs else None
+        self.last_evs = evs
         return ms, kms, clocks, int(launches)
+
+    def per_mode_ms(self, modes):
+        """Mean launch time per mode when each step records one event pair per mode."""
+        evs = getattr(self, "last_evs", [])
+        return {m: statistics.mean(a.elapsed_time(b) for a, b in evs[i::len(modes)])
+                for i, m in enumerate(modes)} if evs else {}
 
     def finish(self, line):
         if self.dist:
@@ -344,7 +351,7 @@ def run_sgemm(ctx):
             if e.status != gb.ERR_UNSUPPORTED:
                 raise
             algo_name = "simt"
-    algo = {"bf16x3": gb.ALGO_BF16X3, "simt": gb.ALGO_SIMT}[algo_name]
+    algo = {"bf16x3": gb.ALGO_BF16X3, "bf16x6": gb.ALGO_BF16X6, "simt": gb.ALGO_SIMT}[algo_name]
 
     errors = {}
     try:
@@ -354,8 +361,8 @@ def run_sgemm(ctx):
         cols = np.sort(rng.choice(N, 128, replace=False))
         hb = {k: v.cpu().numpy() for k, v in bufs.items() if k != "C"}
         c0 = C0.cpu().numpy()
-        for an, aid in (("simt", gb.ALGO_SIMT), ("bf16x3", gb.ALGO_BF16X3)):
-            if an == "bf16x3" and algo_name != "bf16x3":
+        for an, aid in (("simt", gb.ALGO_SIMT), ("bf16x3", gb.ALGO_BF16X3), ("bf16x6", gb.ALGO_BF16X6)):
+            if an != "simt" and algo_name == "simt":
                 continue
             worst = 0.0
             for mode in MODES:
@@ -386,6 +393,7 @@ def run_sgemm(ctx):
             evs.append((a, b))
 
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
+    by_mode = ctx.per_mode_ms(MODES)
     value = ctx.world * args.steps * len(MODES) * flops / (ms * 1e-3) / 1e12
 
     compare = {}
@@ -401,6 +409,19 @@ def run_sgemm(ctx):
         torch.cuda.synchronize()
         compare["simt_tflops"] = 2 * len(MODES) * flops / (s0.elapsed_time(s1) * 1e-3) / 1e12
         compare["speedup_vs_simt"] = value / ctx.world / compare["simt_tflops"]
+        other = "bf16x6" if algo_name == "bf16x3" else "bf16x3"
+        oid = gb.ALGO_BF16X6 if other == "bf16x6" else gb.ALGO_BF16X3
+        for mode in MODES:
+            gemm(mode, oid)
+        s0.record(ctx.stream)
+        for _ in range(2):
+            for mode in MODES:
+                gemm(mode, oid)
+        s1.record(ctx.stream)
+        torch.cuda.synchronize()
+        compare[other + "_tflops"] = 2 * len(MODES) * flops / (s0.elapsed_time(s1) * 1e-3) / 1e12
+        compare[other + "_note"] = ("six BF16 products per FP32 product (3-piece split): FP32-level error"
+                                    if other == "bf16x6" else "three BF16 products per FP32 product")
 
     pin = {k: v.cpu().pin_memory() for k, v in bufs.items()}
     hostC = torch.empty((M, LD), dtype=torch.float32).pin_memory()
@@ -421,11 +442,13 @@ def run_sgemm(ctx):
     e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 5)), len(MODES) * flops, 1e12)
 
     kernel_tflops = flops / (kms * 1e-3) / 1e12
-    if algo_name == "bf16x3":
-        roof = {"bound": "tensor", "achieved": kernel_tflops, "peak": ctx.peaks["bf16_tflops"] / 3.0,
-                "unit": "TFLOP/s", "peak_note": "BF16 dense %s burst peak / 3 (three BF16 products per FP32 "
-                "product); achieved = 2MNK / mean duration of one gb_sgemm call (split + MMA kernels)" % ctx.peak_src}
-        kname = "sgemm_bf16x3_4096"
+    if algo_name in ("bf16x3", "bf16x6"):
+        npr = 3 if algo_name == "bf16x3" else 6
+        roof = {"bound": "tensor", "achieved": kernel_tflops, "peak": ctx.peaks["bf16_tflops"] / npr,
+                "unit": "TFLOP/s", "peak_note": "BF16 dense %s burst peak / %d (%d BF16 products per FP32 "
+                "product); achieved = 2MNK / mean duration of one gb_sgemm call (split + MMA kernels)"
+                % (ctx.peak_src, npr, npr)}
+        kname = "sgemm_%s_4096" % algo_name
     else:
         roof = {"bound": "fp32-simt", "achieved": kernel_tflops, "peak": FP32_SIMT_PEAK, "unit": "TFLOP/s",
                 "peak_note": "nominal FFMA peak 152 SMs x 128 lanes x 2 x 2.07 GHz (no measured FP32 peak)"}
@@ -433,6 +456,7 @@ def run_sgemm(ctx):
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["traffic"] = profile_traffic(kname)
     roof["kernel_ms"] = kms
+    roof["kernel_ms_by_mode"] = by_mode
 
     config = {"workload": "SGEMM 4096^3, ld 4112, alpha 1.5, beta -0.5, NN/NT/TN/TT, U[-1,1] seed 1",
               "M": M, "N": N, "K": K, "ld": LD, "alpha": ALPHA, "beta": BETA, "modes": list(MODES),
@@ -594,7 +618,7 @@ def run_skinny(ctx):
     bits = args.bits
     dt = torch.float64 if bits == 64 else torch.float32
     s = bits // 8
-    small, big, K = args.n, 262144, 4096
+    small, big, K = args.n, args.rows, 4096
     thin = args.workload == "thinb"
     M, N = (big, small) if thin else (small, big)
     nbytes_alg = s * (M * K + K * N + 2 * M * N)
@@ -637,7 +661,7 @@ def run_skinny(ctx):
     cpeak = FP64_PEAK if bits == 64 else FP32_SIMT_PEAK
     roof = bw_roof(ctx, nbytes_alg / (kms * 1e-3) / 1e9, None, "%s_%s_n%d" % (args.workload, "f%d" % bits, small),
                    {"compute_tflops": tflops, "compute_peak_tflops": cpeak,
-                    "compute_frac": tflops / cpeak, "kernel_ms": kms,
+                    "compute_frac": tflops / cpeak, "kernel_ms": kms, "kernel_ms_by_mode": ctx.per_mode_ms(MODES),
                     "peak_note_compute": "nominal %s peak" % ("FP64" if bits == 64 else "FP32 FFMA")})
     hostbufs = {m: (ops[m][0].cpu().pin_memory(), ops[m][2].cpu().pin_memory()) for m in MODES}
     hostC = C.cpu().pin_memory()
@@ -675,7 +699,7 @@ def run_transpose(ctx):
     bits = args.bits
     dt = torch.float64 if bits == 64 else torch.float32
     s = bits // 8
-    M, N = 30000, 17000
+    M, N = (int(x) for x in args.shape.split("x"))
     A = torch.empty((M, N), dtype=dt, device=ctx.dev)
     gb.fill(A, M, N, N, 2, 0, bits, stream=ctx.stream)
     B = torch.empty((N, M), dtype=dt, device=ctx.dev)
@@ -697,7 +721,7 @@ def run_transpose(ctx):
 
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
     value = ctx.world * args.steps * nbytes / (ms * 1e-3) / 1e9
-    roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "transpose_f%d_30000x17000" % bits, {"kernel_ms": kms})
+    roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "transpose_f%d_%s" % (bits, args.shape), {"kernel_ms": kms})
     hA = A.cpu().pin_memory()
     hB = torch.empty_like(B, device="cpu").pin_memory()
 
@@ -708,7 +732,7 @@ def run_transpose(ctx):
         return A.numel() * s, B.numel() * s
 
     e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 3)), nbytes, 1e9)
-    config = {"workload": "transpose 30000 x 17000 FP%d, bit-exact" % bits, "M": M, "N": N,
+    config = {"workload": "transpose %d x %d FP%d, bit-exact" % (M, N, bits), "M": M, "N": N,
               "parallelism": "replicas x%d" % ctx.world, "l2": "inputs larger than L2"}
     line = base_line(ctx, "HBM GB/s (transpose)", value, "GB/s", ms, args.steps, "f%d" % bits, config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
@@ -981,10 +1005,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="sgemm",
                     choices=["sgemm", "dgemm", "thinb", "shorta", "transpose", "jacobi", "serve"])
-    ap.add_argument("--algo", default="best", choices=["best", "bf16x3", "simt"])
+    ap.add_argument("--algo", default="best", choices=["best", "bf16x3", "bf16x6", "simt"])
     ap.add_argument("--bits", type=int, default=32, choices=[32, 64])
     ap.add_argument("--n", type=int, default=8, help="small dimension of thinb/shorta")
     ap.add_argument("--skinny-algo", default="auto", choices=["auto", "skinny", "bf16x3"])
+    ap.add_argument("--rows", type=int, default=262144, help="thinb/shorta: the large dimension")
+    ap.add_argument("--shape", default="30000x17000", help="transpose: MxN")
     ap.add_argument("--iters", type=int, default=200, help="jacobi sweeps")
     ap.add_argument("--slices", type=int, default=0, help="dgemm: Ozaki slices (0: fewest matching native error)")
     ap.add_argument("--size", type=int, default=0, help="dgemm: M=N=K (default 8192)")

@@ -22,6 +22,8 @@
 //     and write C row-contiguously with alpha/beta applied.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include "gb_common.cuh"
 #include "sm100_ptx.cuh"
@@ -67,15 +69,33 @@ bool make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint64_t
     return r == CUDA_SUCCESS;
 }
 
+// 2-D FP32 tensor [outer][inner], box box_inner x box_outer, no swizzle or
+// 128-byte swizzle (box_inner * 4 must then be 128).
+bool make_tmap_f32(CUtensorMap *map, const void *base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                   uint32_t box_inner, uint32_t box_outer, bool sw128) {
+    PFN_encodeTiled enc = encode_fn();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {row_bytes};
+    cuuint32_t box[2] = {box_inner, box_outer};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, sw128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 namespace {
 
 // ------------------------------------------------------------------ split
-// out_hi/out_lo: rows x kp (K-major).  Source element (r, k):
+// out_hi/out_lo(/out_lo2): rows x kp (K-major).  Source element (r, k):
 // trans ? X[k*ldx + r] : X[r*ldx + k].  32x32 tiles through shared memory
-// so both the read and the write are coalesced in either layout.
+// so both the read and the write are coalesced in either layout.  With
+// out_lo2 the value is cut in three BF16 pieces (hi, mid, lo: 24 bits).
 __global__ void __launch_bounds__(256) split_kernel(const float *__restrict__ X, int64_t ldx, int trans, int64_t rows,
                                                     int64_t K, int64_t kp, __nv_bfloat16 *__restrict__ out_hi,
-                                                    __nv_bfloat16 *__restrict__ out_lo) {
+                                                    __nv_bfloat16 *__restrict__ out_lo,
+                                                    __nv_bfloat16 *__restrict__ out_lo2) {
     __shared__ float tile[32][33];
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;   // 32 x 8
     const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
@@ -99,27 +119,40 @@ __global__ void __launch_bounds__(256) split_kernel(const float *__restrict__ X,
         if (r < rows && k < kp) {
             float x = tile[tx][ty + i];
             __nv_bfloat16 h = __float2bfloat16_rn(x);
-            __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+            const float rem = x - __bfloat162float(h);   // exact
+            __nv_bfloat16 l = __float2bfloat16_rn(rem);
             out_hi[r * kp + k] = h;
             out_lo[r * kp + k] = l;
+            if (out_lo2) out_lo2[r * kp + k] = __float2bfloat16_rn(rem - __bfloat162float(l));
         }
     }
 }
 
 // ------------------------------------------------------------------- gemm
-// Persistent: one CTA per SM walks the 128 x 256 C tiles in a grouped order
+// Persistent: one CTA per SM walks the 128 x BN C tiles in a grouped order
 // (GROUP_M tile rows at a time, so neighbouring CTAs share A and B tiles in
 // L2).  K in blocks of 32 (one 64-byte swizzle atom), 4 shared-memory stages
-// of 48 KB.  Two TMEM accumulators of 256 columns: the epilogue of tile i
-// (warps 2-5) overlaps the MMAs of tile i+1 (warp 1).
-constexpr int BM = 128, BN = 256, BK = 32, STAGES = 4, GROUP_M = 8;
+// of 48 KB holding NP BF16 pieces of the A and B tiles (NP = 2: hi, lo with
+// BN = 256; NP = 3: hi, mid, lo with BN = 128).  Two TMEM accumulators of BN
+// columns: the epilogue of tile i (warps 2-5) overlaps the MMAs of tile i+1
+// (warp 1).
+constexpr int BM = 128, BK = 32, STAGES = 4, GROUP_M = 8;
 constexpr int A_TILE = BM * BK * 2;            // 8 KB
-constexpr int B_TILE = BN * BK * 2;            // 16 KB
-constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;
 constexpr int EPI_BYTES = 4 * 32 * 33 * 4;     // per-warp 32 x 32 staging, padded
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int NT = 192;
-constexpr uint32_t ACC_COLS = 256, TMEM_COLS = 512;
+
+template <int NP, int BN>
+struct TwoPass {
+    static constexpr int B_TILE = BN * BK * 2;
+    static constexpr int STAGE_BYTES = NP * A_TILE + NP * B_TILE;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr uint32_t ACC_COLS = BN, TMEM_COLS = 2 * BN;
+};
+
+// tensor maps of the A and B pieces (hi, lo[, lo2])
+struct PieceMaps {
+    CUtensorMap a[3], b[3];
+};
 
 struct EpiParams {
     float *C;
@@ -129,6 +162,7 @@ struct EpiParams {
     int num_kb;
     int tiles_m, tiles_n;
     int *err;
+    int chunk_kb;    // k-blocks per accumulator chunk (folding form)
 };
 
 __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int &tm, int &tn) {
@@ -141,10 +175,22 @@ __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int
     tn = r / gm;
 }
 
-__global__ void __launch_bounds__(NT, 1)
-    bf16x3_gemm_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
-                       const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
-                       EpiParams p) {
+// FOLD: the tensor cores add each MMA into the FP32 accumulator with an
+// error of about one unit in the last place of the accumulator, so over a
+// long K the error grows with the number of MMAs and with the size of the
+// running sum.  With FOLD the accumulator is restarted every chunk_kb
+// k-blocks (chunk_kb * 32 values of K) and the epilogue warps add each chunk
+// into an FP32 running total held in registers (round-to-nearest), and the
+// most significant product hi*hi is accumulated apart from the small
+// cross products, so only the hi*hi MMAs add into a large accumulator.
+// TMEM: two chunk buffers of 256 columns (hi*hi at +0, the rest at +128),
+// BN = 128; the MMAs of chunk c+1 overlap the fold of chunk c.
+template <int NP, int BN, bool FOLD>
+__global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constant__ PieceMaps maps, EpiParams p) {
+    using CF = TwoPass<NP, BN>;
+    static_assert(!FOLD || BN == 128, "the folding form keeps a 128-column total per thread");
+    constexpr int B_TILE = CF::B_TILE, STAGE_BYTES = CF::STAGE_BYTES;
+    constexpr uint32_t ACC_COLS = FOLD ? 256 : CF::ACC_COLS, TMEM_COLS = FOLD ? 512 : CF::TMEM_COLS;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     float *epi = reinterpret_cast<float *>(smem + STAGES * STAGE_BYTES);
@@ -156,6 +202,8 @@ __global__ void __launch_bounds__(NT, 1)
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int num_tiles = p.tiles_m * p.tiles_n;
+    const int chunk_kb = FOLD ? p.chunk_kb : p.num_kb;
+    const int nchunks = (p.num_kb + chunk_kb - 1) / chunk_kb;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
@@ -167,10 +215,10 @@ __global__ void __launch_bounds__(NT, 1)
             ptx::mbar_init(&acc_empty[b], 4);   // one arrive per epilogue warp
         }
         ptx::fence_mbar_init();
-        ptx::tma_prefetch_desc(&tmAh);
-        ptx::tma_prefetch_desc(&tmAl);
-        ptx::tma_prefetch_desc(&tmBh);
-        ptx::tma_prefetch_desc(&tmBl);
+        for (int i = 0; i < NP; i++) {
+            ptx::tma_prefetch_desc(&maps.a[i]);
+            ptx::tma_prefetch_desc(&maps.b[i]);
+        }
     }
     if (warp == 1) ptx::tmem_alloc(tmem_slot, TMEM_COLS);
     ptx::tc_fence_before();
@@ -194,66 +242,119 @@ __global__ void __launch_bounds__(NT, 1)
                     }
                     uint8_t *st = smem + s * STAGE_BYTES;
                     ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-                    ptx::tma_load_2d(st, &tmAh, &full[s], kb * BK, m0);
-                    ptx::tma_load_2d(st + A_TILE, &tmAl, &full[s], kb * BK, m0);
-                    ptx::tma_load_2d(st + 2 * A_TILE, &tmBh, &full[s], kb * BK, n0);
-                    ptx::tma_load_2d(st + 2 * A_TILE + B_TILE, &tmBl, &full[s], kb * BK, n0);
+#pragma unroll
+                    for (int i = 0; i < NP; i++) {
+                        ptx::tma_load_2d(st + i * A_TILE, &maps.a[i], &full[s], kb * BK, m0);
+                        ptx::tma_load_2d(st + NP * A_TILE + i * B_TILE, &maps.b[i], &full[s], kb * BK, n0);
+                    }
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {   // MMA issuer
             constexpr uint32_t idesc = ptx::idesc_bf16_f32(BM, BN);
-            int kbg = 0, it = 0;
+            int kbg = 0, ch = 0;   // running k-block and accumulator-chunk counters
+            (void)B_TILE;
             bool go = true;
-            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x, it++) {
-                const int b = it & 1;
-                if (it >= 2 && !ptx::mbar_wait(&acc_empty[b], ((it >> 1) & 1) ^ 1, p.err, 2)) break;
-                ptx::tc_fence_after();
-                const uint32_t acc = tmem + (uint32_t)(b * ACC_COLS);
-                for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
-                    const int s = kbg % STAGES;
-                    if (!ptx::mbar_wait(&full[s], (kbg / STAGES) & 1, p.err, 3)) { go = false; break; }
-                    ptx::tc_fence_after();
-                    const uint32_t st = ptx::smem_u32(smem + s * STAGE_BYTES);
-                    const uint64_t ah = ptx::sdesc_kmajor_sw64(st);
-                    const uint64_t al = ptx::sdesc_kmajor_sw64(st + A_TILE);
-                    const uint64_t bh = ptx::sdesc_kmajor_sw64(st + 2 * A_TILE);
-                    const uint64_t bl = ptx::sdesc_kmajor_sw64(st + 2 * A_TILE + B_TILE);
-#pragma unroll
-                    for (int k = 0; k < BK / 16; k++) {
-                        // advance 16 BF16 = 32 bytes along K inside the 64-byte swizzle atom
-                        const uint64_t dk = (uint64_t)((k * 32) >> 4);
-                        ptx::umma_f16(acc, al + dk, bh + dk, idesc, (kb | k) != 0);
-                        ptx::umma_f16(acc, ah + dk, bl + dk, idesc, 1);
-                        ptx::umma_f16(acc, ah + dk, bh + dk, idesc, 1);
+            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+                for (int c = 0; c < nchunks && go; c++, ch++) {
+                    const int b = ch & 1;
+                    if (ch >= 2 && !ptx::mbar_wait(&acc_empty[b], ((ch >> 1) & 1) ^ 1, p.err, 2)) {
+                        go = false;
+                        break;
                     }
-                    ptx::umma_commit(&empty[s]);
+                    ptx::tc_fence_after();
+                    const uint32_t acc = tmem + (uint32_t)(b * ACC_COLS);
+                    const uint32_t acc_lo = FOLD ? acc + 128u : acc;   // cross products
+                    const int kb1 = (c + 1) * chunk_kb < p.num_kb ? (c + 1) * chunk_kb : p.num_kb;
+                    for (int kb = c * chunk_kb; kb < kb1; kb++, kbg++) {
+                        const int s = kbg % STAGES;
+                        if (!ptx::mbar_wait(&full[s], (kbg / STAGES) & 1, p.err, 3)) { go = false; break; }
+                        ptx::tc_fence_after();
+                        const uint32_t st = ptx::smem_u32(smem + s * STAGE_BYTES);
+                        uint64_t ad[NP], bd[NP];
+#pragma unroll
+                        for (int i = 0; i < NP; i++) {
+                            ad[i] = ptx::sdesc_kmajor_sw64(st + i * A_TILE);
+                            bd[i] = ptx::sdesc_kmajor_sw64(st + NP * A_TILE + i * B_TILE);
+                        }
+                        const bool first = kb == c * chunk_kb;
+#pragma unroll
+                        for (int k = 0; k < BK / 16; k++) {
+                            // advance 16 BF16 = 32 bytes along K inside the 64-byte swizzle atom
+                            const uint64_t dk = (uint64_t)((k * 32) >> 4);
+                            // piece products (i, j) with i + j < NP, least significant first
+#pragma unroll
+                            for (int d = NP - 1; d >= 0; d--)
+#pragma unroll
+                                for (int i = d; i >= 0; i--) {
+                                    const bool lead = FOLD ? (d == NP - 1 && i == d) || d == 0 : d == NP - 1 && i == d;
+                                    ptx::umma_f16(d == 0 ? acc : acc_lo, ad[i] + dk, bd[d - i] + dk, idesc,
+                                                  !(first && k == 0 && lead));
+                                }
+                        }
+                        ptx::umma_commit(&empty[s]);
+                    }
+                    if (go) ptx::umma_commit(&acc_full[b]);
                 }
-                if (go) ptx::umma_commit(&acc_full[b]);
             }
         }
     } else {               // epilogue: warps 2..5 own TMEM lane quarters (warp % 4)
         const int q = warp % 4;
         float *stage = epi + q * 32 * 33;
-        int it = 0;
-        for (int t = blockIdx.x; t < num_tiles; t += gridDim.x, it++) {
-            const int b = it & 1;
-            if (!ptx::mbar_wait(&acc_full[b], (it >> 1) & 1, p.err, 4)) break;
-            ptx::tc_fence_after();
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        int ch = 0;
+        float total[FOLD ? BN : 1];
+        bool go = true;
+        for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
             int tm, tn;
             tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
             const int64_t row0 = (int64_t)tm * BM + q * 32;
             const int64_t n0 = (int64_t)tn * BN;
+            uint32_t accb = 0;
+            if (FOLD) {
+#pragma unroll
+                for (int j = 0; j < (FOLD ? BN : 1); j++) total[j] = 0.f;
+                for (int c = 0; c < nchunks; c++, ch++) {
+                    const int b = ch & 1;
+                    if (!ptx::mbar_wait(&acc_full[b], (ch >> 1) & 1, p.err, 4)) { go = false; break; }
+                    ptx::tc_fence_after();
+#pragma unroll
+                    for (int g = 0; g < (FOLD ? BN : 32) / 32; g++) {
+                        uint32_t rh[32], rl[32];
+                        const uint32_t a = tmem + (uint32_t)(b * ACC_COLS) + lane_off + (uint32_t)(g * 32);
+                        ptx::tmem_ld_32x32b_x32(a, rh);
+                        ptx::tmem_ld_32x32b_x32(a + 128u, rl);
+                        ptx::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 32; j++)
+                            total[g * 32 + j] += __uint_as_float(rh[j]) + __uint_as_float(rl[j]);
+                    }
+                    ptx::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
+                }
+                if (!go) break;
+            } else {
+                const int b = ch & 1;
+                if (!ptx::mbar_wait(&acc_full[b], (ch >> 1) & 1, p.err, 4)) break;
+                ptx::tc_fence_after();
+                accb = (uint32_t)(b * ACC_COLS);
+            }
+#pragma unroll
             for (int c = 0; c < BN; c += 32) {
-                uint32_t r[32];
-                ptx::tmem_ld_32x32b_x32(tmem + (uint32_t)(b * ACC_COLS) + ((uint32_t)(q * 32) << 16) + (uint32_t)c,
-                                        r);
-                ptx::tmem_ld_wait();
                 // thread `lane` holds row row0+lane, columns c..c+31: transpose through
                 // shared memory so each store instruction writes one row contiguously
+                if (FOLD) {
 #pragma unroll
-                for (int j = 0; j < 32; j++) stage[lane * 33 + j] = __uint_as_float(r[j]);
+                    for (int j = 0; j < 32; j++) stage[lane * 33 + j] = total[(FOLD ? c : 0) + j];
+                } else {
+                    uint32_t r[32];
+                    ptx::tmem_ld_32x32b_x32(tmem + accb + lane_off + (uint32_t)c, r);
+                    ptx::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; j++) stage[lane * 33 + j] = __uint_as_float(r[j]);
+                }
                 __syncwarp();
                 const int64_t col = n0 + c + lane;
                 if (col < p.N) {
@@ -279,9 +380,12 @@ __global__ void __launch_bounds__(NT, 1)
                 }
                 __syncwarp();
             }
-            ptx::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
+            if (!FOLD) {
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&acc_empty[ch & 1]);
+                ch++;
+            }
         }
     }
 
@@ -293,20 +397,391 @@ __global__ void __launch_bounds__(NT, 1)
     }
 }
 
+
+// ============================================================ fused split
+// The same 3xBF16 product without a separate split pass: TMA brings FP32
+// tiles of op(A) (128 x 32) and op(B)^T (BN x 32) straight from the caller's
+// matrices in whichever layout they are stored; 8 converter warps split each
+// value into hi/lo BF16 and write them in the 64-byte-swizzled K-major layout
+// the UMMA descriptors read (then fence the async proxy); the MMA and
+// epilogue warps are those of the two-kernel form.  Roles: warp 0 TMA,
+// warp 1 MMA, warps 2-5 epilogue, warps 6-13 converters.
+namespace fused {
+
+constexpr int BM = 128, BK = 32, GROUP_M = 8, NT = 448, NCONV = 8;
+
+template <int BN>
+struct Cfg {
+    static constexpr int A32 = BM * BK * 4;                 // FP32 staging (16 KB)
+    static constexpr int B32 = BN * BK * 4;
+    static constexpr int ABF = BM * BK * 2;                 // one BF16 tile (8 KB)
+    static constexpr int BBF = BN * BK * 2;
+    static constexpr int STAGE32 = A32 + B32;
+    static constexpr int STAGEBF = 2 * ABF + 2 * BBF;
+    static constexpr int STAGES = (200 * 1024) / (STAGE32 + STAGEBF) >= 4 ? 4
+                                  : (200 * 1024) / (STAGE32 + STAGEBF);
+    static constexpr int EPI = 4 * 32 * 33 * 4;
+    static constexpr int SMEM = STAGES * (STAGE32 + STAGEBF) + EPI + 1024 + 512;
+    static constexpr uint32_t TMEM_COLS = 2 * BN;
+};
+
+struct Params {
+    float *C;
+    int64_t M, N, ldc;
+    float alpha, beta;
+    int semantics;
+    int num_kb;
+    int tiles_m, tiles_n;
+    int a_kmajor, b_kmajor;      // FP32 staging layout of op(A) / op(B)^T
+    int *err;
+};
+
+__device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int &tm, int &tn) {
+    const int per_group = GROUP_M * tiles_n;
+    const int g = t / per_group;
+    const int first_m = g * GROUP_M;
+    const int gm = min(GROUP_M, tiles_m - first_m);
+    const int r = t - g * per_group;
+    tm = first_m + r % gm;
+    tn = r / gm;
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(a)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(b)) << 16);
+}
+
+// Split one 8-value K chunk of row r into the hi and lo BF16 tiles
+// (64-byte swizzle: 16-byte chunk c of row r sits at chunk c ^ ((r % 8) / 2)).
+__device__ __forceinline__ void split_store(const float (&v)[8], uint8_t *hi, uint8_t *lo, int r, int c) {
+    float h[8], l[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        h[j] = __bfloat162float(__float2bfloat16_rn(v[j]));
+        l[j] = v[j] - h[j];
+    }
+    const uint32_t off = (uint32_t)(r >> 3) * 512u + (uint32_t)(r & 7) * 64u + (uint32_t)((c ^ ((r & 7) >> 1)) << 4);
+    *reinterpret_cast<uint4 *>(hi + off) =
+        make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+    *reinterpret_cast<uint4 *>(lo + off) =
+        make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]), pack_bf16(l[6], l[7]));
+}
+
+// Convert a ROWS x 32 FP32 staging tile into hi/lo BF16 tiles.  K-major
+// staging is TMA-swizzled (128-byte rows, 16-byte piece p of row r at
+// p ^ (r % 8)); MN-major staging is [32][ROWS] plain.
+template <int ROWS>
+__device__ __forceinline__ void convert_tile(const uint8_t *src, bool kmajor, uint8_t *hi, uint8_t *lo, int ctid) {
+    constexpr int CHUNKS = ROWS * (BK / 8);
+    for (int q = ctid; q < CHUNKS; q += NCONV * 32) {
+        float v[8];
+        int r, c;
+        if (kmajor) {
+            r = q >> 2;
+            c = q & 3;
+            const uint8_t *row = src + (r >> 3) * 1024 + (r & 7) * 128;
+            const float4 a = *reinterpret_cast<const float4 *>(row + (((2 * c) ^ (r & 7)) << 4));
+            const float4 b = *reinterpret_cast<const float4 *>(row + (((2 * c + 1) ^ (r & 7)) << 4));
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+            v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        } else {
+            c = q / ROWS;
+            r = q - c * ROWS;
+            const float *col = reinterpret_cast<const float *>(src) + (c * 8) * ROWS + r;
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = col[j * ROWS];
+        }
+        split_store(v, hi, lo, r, c);
+    }
+}
+
+template <int BN>
+__global__ void __launch_bounds__(NT, 1)
+    bf16x3_fused_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, Params p) {
+    using C = Cfg<BN>;
+    constexpr int S = C::STAGES;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t *st32 = smem;                                  // S x (A32 + B32)
+    uint8_t *stbf = smem + S * C::STAGE32;                 // S x (Ahi, Alo, Bhi, Blo)
+    float *epi = reinterpret_cast<float *>(stbf + S * C::STAGEBF);
+    uint64_t *f32_full = reinterpret_cast<uint64_t *>(reinterpret_cast<uint8_t *>(epi) + C::EPI);
+    uint64_t *f32_empty = f32_full + S;
+    uint64_t *bf_full = f32_empty + S;
+    uint64_t *bf_empty = bf_full + S;
+    uint64_t *acc_full = bf_empty + S;
+    uint64_t *acc_empty = acc_full + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int num_tiles = p.tiles_m * p.tiles_n;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            ptx::mbar_init(&f32_full[s], 1);
+            ptx::mbar_init(&f32_empty[s], NCONV);
+            ptx::mbar_init(&bf_full[s], NCONV);
+            ptx::mbar_init(&bf_empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            ptx::mbar_init(&acc_full[b], 1);
+            ptx::mbar_init(&acc_empty[b], 4);
+        }
+        ptx::fence_mbar_init();
+        ptx::tma_prefetch_desc(&tmA);
+        ptx::tma_prefetch_desc(&tmB);
+    }
+    if (warp == 1) ptx::tmem_alloc(tmem_slot, C::TMEM_COLS);
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {   // TMA producer: FP32 tiles in their stored layout
+            int kbg = 0;
+            bool go = true;
+            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+                int tm, tn;
+                tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+                const int m0 = tm * BM, n0 = tn * BN;
+                for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
+                    const int s = kbg % S;
+                    if (kbg >= S && !ptx::mbar_wait(&f32_empty[s], ((kbg / S) & 1) ^ 1, p.err, 21)) {
+                        go = false;
+                        break;
+                    }
+                    uint8_t *a = st32 + s * C::STAGE32;
+                    ptx::mbar_arrive_expect_tx(&f32_full[s], C::STAGE32);
+                    if (p.a_kmajor) ptx::tma_load_2d(a, &tmA, &f32_full[s], kb * BK, m0);
+                    else ptx::tma_load_2d(a, &tmA, &f32_full[s], m0, kb * BK);
+                    if (p.b_kmajor) ptx::tma_load_2d(a + C::A32, &tmB, &f32_full[s], kb * BK, n0);
+                    else ptx::tma_load_2d(a + C::A32, &tmB, &f32_full[s], n0, kb * BK);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer
+            constexpr uint32_t idesc = ptx::idesc_bf16_f32(BM, BN);
+            int kbg = 0, it = 0;
+            bool go = true;
+            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x, it++) {
+                const int b = it & 1;
+                if (it >= 2 && !ptx::mbar_wait(&acc_empty[b], ((it >> 1) & 1) ^ 1, p.err, 22)) break;
+                ptx::tc_fence_after();
+                const uint32_t acc = tmem + (uint32_t)(b * BN);
+                for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
+                    const int s = kbg % S;
+                    if (!ptx::mbar_wait(&bf_full[s], (kbg / S) & 1, p.err, 23)) { go = false; break; }
+                    ptx::tc_fence_after();
+                    const uint32_t st = ptx::smem_u32(stbf + s * C::STAGEBF);
+                    const uint64_t ah = ptx::sdesc_kmajor_sw64(st);
+                    const uint64_t al = ptx::sdesc_kmajor_sw64(st + C::ABF);
+                    const uint64_t bh = ptx::sdesc_kmajor_sw64(st + 2 * C::ABF);
+                    const uint64_t bl = ptx::sdesc_kmajor_sw64(st + 2 * C::ABF + C::BBF);
+#pragma unroll
+                    for (int k = 0; k < BK / 16; k++) {
+                        const uint64_t dk = (uint64_t)((k * 32) >> 4);
+                        ptx::umma_f16(acc, al + dk, bh + dk, idesc, (kb | k) != 0);
+                        ptx::umma_f16(acc, ah + dk, bl + dk, idesc, 1);
+                        ptx::umma_f16(acc, ah + dk, bh + dk, idesc, 1);
+                    }
+                    ptx::umma_commit(&bf_empty[s]);
+                }
+                if (go) ptx::umma_commit(&acc_full[b]);
+            }
+        }
+    } else if (warp < 6) {   // epilogue: TMEM lane quarter q = warp % 4
+        const int q = warp % 4;
+        float *stage = epi + q * 32 * 33;
+        int it = 0;
+        for (int t = blockIdx.x; t < num_tiles; t += gridDim.x, it++) {
+            const int b = it & 1;
+            if (!ptx::mbar_wait(&acc_full[b], (it >> 1) & 1, p.err, 24)) break;
+            ptx::tc_fence_after();
+            int tm, tn;
+            tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+            const int64_t row0 = (int64_t)tm * BM + q * 32;
+            const int64_t n0 = (int64_t)tn * BN;
+            for (int c = 0; c < BN; c += 32) {
+                uint32_t r[32];
+                ptx::tmem_ld_32x32b_x32(tmem + (uint32_t)(b * BN) + ((uint32_t)(q * 32) << 16) + (uint32_t)c, r);
+                ptx::tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 32; j++) stage[lane * 33 + j] = __uint_as_float(r[j]);
+                __syncwarp();
+                const int64_t col = n0 + c + lane;
+                if (col < p.N) {
+                    const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
+                    if (p.semantics == GB_SEM_SCALAR_BETA || (p.semantics == GB_SEM_BLAS && p.beta == 0.f)) {
+                        const float add = p.semantics == GB_SEM_SCALAR_BETA ? p.beta : 0.f;
+                        for (int rr = 0; rr < rows; rr++)
+                            p.C[(row0 + rr) * p.ldc + col] = p.alpha * stage[rr * 33 + lane] + add;
+                    } else {
+                        float cin[32];
+#pragma unroll
+                        for (int rr = 0; rr < 32; rr++) cin[rr] = rr < rows ? p.C[(row0 + rr) * p.ldc + col] : 0.f;
+#pragma unroll
+                        for (int rr = 0; rr < 32; rr++) {
+                            if (rr < rows) {
+                                float v = p.alpha * stage[rr * 33 + lane];
+                                v = p.semantics == GB_SEM_BLAS ? fmaf(p.beta, cin[rr], v) : cin[rr] + (v + p.beta);
+                                p.C[(row0 + rr) * p.ldc + col] = v;
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
+        }
+    } else {                 // converters: FP32 staging -> hi/lo BF16 tiles
+        const int ctid = threadIdx.x - 6 * 32;
+        int kbg = 0;
+        for (int t = blockIdx.x; t < num_tiles; t += gridDim.x) {
+            bool go = true;
+            for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
+                const int s = kbg % S;
+                if (!ptx::mbar_wait(&f32_full[s], (kbg / S) & 1, p.err, 25)) { go = false; break; }
+                if (kbg >= S && !ptx::mbar_wait(&bf_empty[s], ((kbg / S) & 1) ^ 1, p.err, 26)) { go = false; break; }
+                const uint8_t *a32 = st32 + s * C::STAGE32;
+                uint8_t *bf = stbf + s * C::STAGEBF;
+                convert_tile<BM>(a32, p.a_kmajor, bf, bf + C::ABF, ctid);
+                convert_tile<BN>(a32 + C::A32, p.b_kmajor, bf + 2 * C::ABF, bf + 2 * C::ABF + C::BBF, ctid);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) {
+                    ptx::mbar_arrive(&f32_empty[s]);
+                    ptx::mbar_arrive(&bf_full[s]);
+                }
+            }
+            if (!go) break;
+        }
+    }
+
+    ptx::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem, C::TMEM_COLS);
+    }
+}
+
+template <int BN>
+gb_status launch(const GemmArgs &g, int *err) {
+    using C = Cfg<BN>;
+    CUtensorMap tA, tB;
+    // op(A) (M x K): K-major when A is row-major (ta = 0); op(B)^T (N x K):
+    // K-major when B is stored N x K (tb = 1)
+    bool okm;
+    if (!g.ta) okm = make_tmap_f32(&tA, g.A, g.K, g.M, g.lda * 4, BK, BM, true);
+    else okm = make_tmap_f32(&tA, g.A, g.M, g.K, g.lda * 4, BM, BK, false);
+    if (g.tb) okm = okm && make_tmap_f32(&tB, g.B, g.K, g.N, g.ldb * 4, BK, BN, true);
+    else okm = okm && make_tmap_f32(&tB, g.B, g.N, g.K, g.ldb * 4, BN, BK, false);
+    if (!okm) return set_status(GB_ERR_CUDA, "bf16x3: cuTensorMapEncodeTiled (FP32) failed");
+    static bool attr[2] = {false, false};
+    if (!attr[0]) {
+        GB_CUDA_TRY(cudaFuncSetAttribute(bf16x3_fused_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         C::SMEM));
+        attr[0] = true;
+    }
+    Params p;
+    p.C = (float *)g.C; p.M = g.M; p.N = g.N; p.ldc = g.ldc;
+    p.alpha = (float)g.alpha; p.beta = (float)g.beta; p.semantics = g.semantics;
+    p.num_kb = (int)ceil_div(g.K, BK);
+    p.tiles_m = (int)ceil_div(g.M, BM);
+    p.tiles_n = (int)ceil_div(g.N, BN);
+    p.a_kmajor = g.ta ? 0 : 1;
+    p.b_kmajor = g.tb ? 1 : 0;
+    p.err = err;
+    const int tiles = p.tiles_m * p.tiles_n;
+    const int grid = tiles < sm_count() ? tiles : sm_count();
+    bf16x3_fused_kernel<BN><<<grid, NT, C::SMEM, g.stream>>>(tA, tB, p);
+    GB_LAUNCH_CHECK("bf16x3_fused_kernel");
+    return ok();
+}
+
+}  // namespace fused
 }  // namespace
+
+static gb_status two_pass(const GemmArgs &g, int np, int fold_kb);
+
+// Accumulator chunk (k-blocks of 32) from the environment, for measurement.
+static int env_chunk(const char *name, int dflt) {
+    const char *v = getenv(name);
+    if (!v || !*v) return dflt;
+    const int c = atoi(v);
+    return c < 0 ? 0 : c;
+}
 
 gb_status launch_sgemm_bf16x3(const GemmArgs &g) {
     if (g.M == 0 || g.N == 0) return ok();
     if (g.M > 0x7fffffff / 2 || g.N > 0x7fffffff / 2 || g.K > 0x7fffffff / 2)
         return set_status(GB_ERR_UNSUPPORTED, "bf16x3: dimension too large");
+    {
+        // fused split: FP32 TMA straight from A and B (16-byte aligned bases,
+        // row strides a multiple of 16 bytes)
+        // row strides a multiple of 16 bytes).  Used for skinny products
+        // (min(M, N) <= 64), where a separate split pass would double the
+        // HBM traffic of the streamed operand; large square products keep the
+        // two-pass form, whose MMA loop is not slowed by the converters.
+        const bool aligned = (g.lda % 4 == 0) && (g.ldb % 4 == 0) && ((uintptr_t)g.A % 16 == 0) &&
+                             ((uintptr_t)g.B % 16 == 0);
+        const bool skinny = g.M <= 64 || g.N <= 64;
+        const char *force = getenv("GB_BF16X3_PATH");   // "fused" / "two-pass": testing and measurement
+        const bool use_fused = force ? (force[0] == 'f') : skinny;
+        if (aligned && use_fused) {
+            int *e = error_word();
+            if (!e) return set_status(GB_ERR_OOM, "bf16x3: no device error word");
+            if (g.N <= 32) return fused::launch<32>(g, e);
+            if (g.N <= 64) return fused::launch<64>(g, e);
+            if (g.N <= 128) return fused::launch<128>(g, e);
+            return fused::launch<256>(g, e);
+        }
+    }
+    return two_pass(g, 2, env_chunk("GB_BF16X3_FOLD", 0));
+}
+
+gb_status launch_sgemm_bf16x6(const GemmArgs &g) {
+    if (g.M == 0 || g.N == 0) return ok();
+    if (g.M > 0x7fffffff / 2 || g.N > 0x7fffffff / 2 || g.K > 0x7fffffff / 2)
+        return set_status(GB_ERR_UNSUPPORTED, "bf16x6: dimension too large");
+    return two_pass(g, 3, env_chunk("GB_BF16X6_CHUNK", 8));
+}
+
+template <int NP, int BN, bool FOLD>
+static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64_t kp, int *err, int fold_kb) {
+    using CF = TwoPass<NP, BN>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        GB_CUDA_TRY(cudaFuncSetAttribute(bf16x3_gemm_kernel<NP, BN, FOLD>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM_BYTES));
+        attr_set = true;
+    }
+    const int tiles_m = (int)ceil_div(g.M, BM), tiles_n = (int)ceil_div(g.N, BN);
+    EpiParams p{(float *)g.C, g.M, g.N, g.ldc, (float)g.alpha, (float)g.beta, g.semantics, (int)(kp / BK),
+                tiles_m, tiles_n, err, FOLD ? fold_kb : 1};
+    const int tiles = tiles_m * tiles_n;
+    const int grid = tiles < sm_count() ? tiles : sm_count();
+    bf16x3_gemm_kernel<NP, BN, FOLD><<<grid, NT, CF::SMEM_BYTES, g.stream>>>(maps, p);
+    GB_LAUNCH_CHECK("bf16x3_gemm_kernel");
+    return ok();
+}
+
+// Split pass (NP BF16 pieces per operand, K-major) + MMA kernel; fold_kb > 0
+// selects the folding form with that accumulator chunk (in k-blocks of 32).
+static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
     const int64_t kp = ceil_div(g.K, 64) * 64;   // multiple of BK, zero-padded
     const size_t a_bytes = (size_t)g.M * kp * 2, b_bytes = (size_t)g.N * kp * 2;
-    uint8_t *ws = (uint8_t *)workspace(2 * a_bytes + 2 * b_bytes + 4096, g.stream);
+    uint8_t *ws = (uint8_t *)workspace(np * (a_bytes + b_bytes) + 4096, g.stream);
     if (!ws) return (gb_status)gb_get_last_status();
-    __nv_bfloat16 *ah = (__nv_bfloat16 *)ws;
-    __nv_bfloat16 *al = (__nv_bfloat16 *)(ws + a_bytes);
-    __nv_bfloat16 *bh = (__nv_bfloat16 *)(ws + 2 * a_bytes);
-    __nv_bfloat16 *bl = (__nv_bfloat16 *)(ws + 2 * a_bytes + b_bytes);
+    __nv_bfloat16 *ap[3], *bp[3];
+    for (int i = 0; i < np; i++) {
+        ap[i] = (__nv_bfloat16 *)(ws + i * a_bytes);
+        bp[i] = (__nv_bfloat16 *)(ws + np * a_bytes + i * b_bytes);
+    }
     int *err = error_word();
     if (!err) return set_status(GB_ERR_OOM, "bf16x3: no device error word");
 
@@ -315,31 +790,27 @@ gb_status launch_sgemm_bf16x3(const GemmArgs &g) {
     dim3 sgA((unsigned)ceil_div(kp, 32), (unsigned)ceil_div(g.M, 32));
     dim3 sgB((unsigned)ceil_div(kp, 32), (unsigned)ceil_div(g.N, 32));
     if (sgA.y > 65535u || sgB.y > 65535u) return set_status(GB_ERR_UNSUPPORTED, "bf16x3: M or N too large");
-    split_kernel<<<sgA, 256, 0, g.stream>>>((const float *)g.A, g.lda, g.ta ? 1 : 0, g.M, g.K, kp, ah, al);
+    split_kernel<<<sgA, 256, 0, g.stream>>>((const float *)g.A, g.lda, g.ta ? 1 : 0, g.M, g.K, kp, ap[0], ap[1],
+                                            np == 3 ? ap[2] : nullptr);
     GB_LAUNCH_CHECK("bf16x3 split A");
-    split_kernel<<<sgB, 256, 0, g.stream>>>((const float *)g.B, g.ldb, g.tb ? 0 : 1, g.N, g.K, kp, bh, bl);
+    split_kernel<<<sgB, 256, 0, g.stream>>>((const float *)g.B, g.ldb, g.tb ? 0 : 1, g.N, g.K, kp, bp[0], bp[1],
+                                            np == 3 ? bp[2] : nullptr);
     GB_LAUNCH_CHECK("bf16x3 split B");
 
-    CUtensorMap tAh, tAl, tBh, tBl;
-    bool okm = make_tmap_bf16(&tAh, ah, kp, g.M, kp * 2, BK, BM, 64) &&
-               make_tmap_bf16(&tAl, al, kp, g.M, kp * 2, BK, BM, 64) &&
-               make_tmap_bf16(&tBh, bh, kp, g.N, kp * 2, BK, BN, 64) &&
-               make_tmap_bf16(&tBl, bl, kp, g.N, kp * 2, BK, BN, 64);
-    if (!okm) return set_status(GB_ERR_CUDA, "bf16x3: cuTensorMapEncodeTiled failed");
-
-    static bool attr_set = false;
-    if (!attr_set) {
-        GB_CUDA_TRY(cudaFuncSetAttribute(bf16x3_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        attr_set = true;
+    const int bn = (np == 3 || fold_kb > 0) ? 128 : 256;
+    PieceMaps maps;
+    memset(&maps, 0, sizeof(maps));
+    bool okm = true;
+    for (int i = 0; i < np; i++) {
+        okm = okm && make_tmap_bf16(&maps.a[i], ap[i], kp, g.M, kp * 2, BK, BM, 64);
+        okm = okm && make_tmap_bf16(&maps.b[i], bp[i], kp, g.N, kp * 2, BK, bn, 64);
     }
-    const int tiles_m = (int)ceil_div(g.M, BM), tiles_n = (int)ceil_div(g.N, BN);
-    EpiParams p{(float *)g.C, g.M, g.N, g.ldc, (float)g.alpha, (float)g.beta, g.semantics, (int)(kp / BK),
-                tiles_m, tiles_n, err};
-    const int tiles = tiles_m * tiles_n;
-    const int grid = tiles < sm_count() ? tiles : sm_count();
-    bf16x3_gemm_kernel<<<grid, NT, SMEM_BYTES, g.stream>>>(tAh, tAl, tBh, tBl, p);
-    GB_LAUNCH_CHECK("bf16x3_gemm_kernel");
-    return ok();
+    if (!okm) return set_status(GB_ERR_CUDA, "bf16x3: cuTensorMapEncodeTiled failed");
+    if (np == 3)
+        return fold_kb > 0 ? two_pass_launch<3, 128, true>(g, maps, kp, err, fold_kb)
+                           : two_pass_launch<3, 128, false>(g, maps, kp, err, 0);
+    return fold_kb > 0 ? two_pass_launch<2, 128, true>(g, maps, kp, err, fold_kb)
+                       : two_pass_launch<2, 256, false>(g, maps, kp, err, 0);
 }
 
 }  // namespace gb

@@ -24,8 +24,13 @@
 // Split-K over CTAs when the row count alone cannot fill the GPU; partial
 // sums go to scratch and a second kernel applies alpha/beta.
 #include "gb_common.cuh"
+#include "sm100_ptx.cuh"
 
 namespace gb {
+
+bool make_tmap_f32(CUtensorMap *map, const void *base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                   uint32_t box_inner, uint32_t box_outer, bool sw128);
+
 namespace {
 
 constexpr int NT = 256;
@@ -318,6 +323,167 @@ __global__ void __launch_bounds__(NT) skinny_cols_kernel(SkParams p) {
         }
 }
 
+// ---------------------------------------------------------------------------
+// FP32, n <= 8: the large operand streamed by TMA.  Persistent CTAs (one per
+// SM) walk units of 256 rows x one K range; a producer warp keeps 6 stages of
+// 256 x 32 X values (32 KB, plus the matching 32 x NS slice of W) in flight,
+// so the memory system sees ~200 KB of outstanding reads per SM whatever
+// the register use; 8 consumer warps own one row each per thread and run
+// the whole K range of it (FMAs in k order, no cross-thread reduction).
+// X row-major arrives as 128-byte-swizzled 32-float rows (conflict-free
+// 16-byte reads across 8 consecutive rows); X K-major as [32 k][256 rows].
+// W is read by broadcast in either of its layouts.  Partial sums of a split
+// K range go to scratch for skinny_reduce_kernel.
+namespace thin {
+
+constexpr int BR = 256, BK = 32, STAGES = 6, NCW = 8, NTH = (NCW + 1) * 32;
+constexpr int XS = BR * BK * 4;     // 32 KB
+constexpr int WS = 1024;            // W slice (BK x NS floats), padded to keep stages 1 KB aligned
+constexpr int STAGE = XS + WS;
+constexpr int SMEM = STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/;
+
+struct TParams {
+    int64_t rows, K;
+    int n, splits, kchunk_kb, rtiles;
+    void *C; int64_t cs_r, cs_c;
+    float alpha, beta;
+    int semantics;
+    float *part;
+    int *err;
+};
+
+template <int NS, bool XCOLS, bool WT>
+__global__ void __launch_bounds__(NTH, 1) thin_tma_kernel(const __grid_constant__ CUtensorMap tmx,
+                                                          const __grid_constant__ CUtensorMap tmw, TParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE);
+    uint64_t *empty = full + STAGES;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int nkb = (int)((p.K + BK - 1) / BK);
+    const int units = p.rtiles * p.splits;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            ptx::mbar_init(&full[s], 1);
+            ptx::mbar_init(&empty[s], NCW);
+        }
+        ptx::fence_mbar_init();
+        ptx::tma_prefetch_desc(&tmx);
+        ptx::tma_prefetch_desc(&tmw);
+    }
+    __syncthreads();
+
+    if (warp == NCW) {   // producer
+        if (lane == 0) {
+            int g = 0;
+            for (int u = blockIdx.x; u < units; u += gridDim.x) {
+                const int rt = u / p.splits, sp = u - rt * p.splits;
+                const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
+                const int r0 = rt * BR;
+                for (int kb = kb0; kb < kb1; kb++, g++) {
+                    const int s = g % STAGES;
+                    if (g >= STAGES && !ptx::mbar_wait(&empty[s], ((g / STAGES) & 1) ^ 1, p.err, 41)) return;
+                    uint8_t *st = smem + s * STAGE;
+                    ptx::mbar_arrive_expect_tx(&full[s], XS + BK * NS * 4);
+                    if (XCOLS) ptx::tma_load_2d(st, &tmx, &full[s], r0, kb * BK);
+                    else ptx::tma_load_2d(st, &tmx, &full[s], kb * BK, r0);
+                    if (WT) ptx::tma_load_2d(st + XS, &tmw, &full[s], kb * BK, 0);
+                    else ptx::tma_load_2d(st + XS, &tmw, &full[s], 0, kb * BK);
+                }
+            }
+        }
+        return;
+    }
+
+    const int t = threadIdx.x;   // consumer: row r0 + t
+    int g = 0;
+    for (int u = blockIdx.x; u < units; u += gridDim.x) {
+        const int rt = u / p.splits, sp = u - rt * p.splits;
+        const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
+        float acc[NS];
+#pragma unroll
+        for (int j = 0; j < NS; j++) acc[j] = 0.f;
+        bool go = true;
+        for (int kb = kb0; kb < kb1; kb++, g++) {
+            const int s = g % STAGES;
+            if (!ptx::mbar_wait(&full[s], (g / STAGES) & 1, p.err, 42)) { go = false; break; }
+            const uint8_t *st = smem + s * STAGE;
+            const float *ws = reinterpret_cast<const float *>(st + XS);
+            // two halves of 16 k, so the W reads the compiler hoists stay in registers
+#pragma unroll 1
+            for (int h = 0; h < BK; h += 16) {
+                float x[16];
+                if (XCOLS) {
+                    const float *xs = reinterpret_cast<const float *>(st);
+#pragma unroll
+                    for (int kk = 0; kk < 16; kk++) x[kk] = xs[(h + kk) * BR + t];
+                } else {
+                    const uint8_t *row = st + t * 128;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        const float4 v = *reinterpret_cast<const float4 *>(row + (((h / 4 + c) ^ (t & 7)) << 4));
+                        x[4 * c] = v.x; x[4 * c + 1] = v.y; x[4 * c + 2] = v.z; x[4 * c + 3] = v.w;
+                    }
+                }
+                if (WT) {   // ws[j][kk]
+#pragma unroll
+                    for (int k4 = 0; k4 < 16; k4 += 4) {
+#pragma unroll
+                        for (int j = 0; j < NS; j++) {
+                            const float4 w = *reinterpret_cast<const float4 *>(ws + j * BK + h + k4);
+                            acc[j] = fmaf(x[k4], w.x, acc[j]);
+                            acc[j] = fmaf(x[k4 + 1], w.y, acc[j]);
+                            acc[j] = fmaf(x[k4 + 2], w.z, acc[j]);
+                            acc[j] = fmaf(x[k4 + 3], w.w, acc[j]);
+                        }
+                    }
+                } else {    // ws[kk][j]
+#pragma unroll
+                    for (int kk = 0; kk < 16; kk++) {
+#pragma unroll
+                        for (int j4 = 0; j4 < NS; j4 += 4) {
+                            const float4 w = *reinterpret_cast<const float4 *>(ws + (h + kk) * NS + j4);
+                            acc[j4] = fmaf(x[kk], w.x, acc[j4]);
+                            acc[j4 + 1] = fmaf(x[kk], w.y, acc[j4 + 1]);
+                            acc[j4 + 2] = fmaf(x[kk], w.z, acc[j4 + 2]);
+                            acc[j4 + 3] = fmaf(x[kk], w.w, acc[j4 + 3]);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&empty[s]);
+        }
+        if (!go) break;
+        const int64_t row = (int64_t)rt * BR + t;
+        if (row < p.rows) {
+            if (p.splits > 1) {
+                float *pp = p.part + ((int64_t)sp * p.rows + row) * 8;
+#pragma unroll
+                for (int j = 0; j < NS; j++) pp[j] = acc[j];
+            } else {
+                float *c = (float *)p.C + row * p.cs_r;
+#pragma unroll
+                for (int j = 0; j < NS; j++) {
+                    if (j >= p.n) break;
+                    float *cp = c + (int64_t)j * p.cs_c;
+                    float v = p.alpha * acc[j];
+                    if (p.semantics == GB_SEM_BLAS) {
+                        if (p.beta != 0.f) v = fmaf(p.beta, *cp, v);
+                    } else if (p.semantics == GB_SEM_SCALAR_BETA) {
+                        v = v + p.beta;
+                    } else {
+                        v = *cp + (v + p.beta);
+                    }
+                    *cp = v;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace thin
+
 template <typename T, int NB>
 __global__ void skinny_reduce_kernel(SkParams p) {
     const int64_t total = p.rows * p.n;
@@ -333,12 +499,40 @@ __global__ void skinny_reduce_kernel(SkParams p) {
 // Launch plan shared by the workspace path and the fixed-scratch path.
 struct Plan {
     bool rows_kernel, vec, wvec;
+    bool tma;                 // FP32 n <= 8 with TMA-compatible layouts: thin::thin_tma_kernel
     int64_t rtiles;
     size_t part_bytes;
 };
 
+// TMA needs 16-byte aligned bases and row strides that are multiples of 16
+// bytes; GB_SKINNY_TMA=0 turns the streamed kernel off (for measurement).
+template <typename T, int NB>
+bool tma_eligible(const SkParams &p) {
+    if (sizeof(T) != 4 || NB != 8) return false;
+    const char *e = getenv("GB_SKINNY_TMA");
+    if (e && e[0] == '0') return false;
+    return p.K > 0 && p.rows < (int64_t(1) << 31) && p.K < (int64_t(1) << 31) && p.ldx % 4 == 0 && p.ldw % 4 == 0 &&
+           (uintptr_t)p.X % 16 == 0 && (uintptr_t)p.W % 16 == 0;
+}
+
 template <typename T, int NB>
 gb_status make_plan(SkParams &p, Plan &pl) {
+    pl.tma = tma_eligible<T, NB>(p);
+    if (pl.tma) {
+        // units of 256 rows x a K range; split K until there are ~4 units per SM
+        pl.rows_kernel = !p.tx;
+        pl.vec = pl.wvec = true;
+        pl.rtiles = ceil_div(p.rows, thin::BR);
+        const int64_t nkb = ceil_div(p.K, thin::BK);
+        int splits = 1;
+        while (pl.rtiles * splits < 4 * (int64_t)sm_count() && nkb / (splits * 2) >= 16 && splits < 64) splits *= 2;
+        const int64_t ckb = ceil_div(nkb, splits);
+        p.kchunk = ckb * thin::BK;
+        p.splits = (int)ceil_div(nkb, ckb);
+        if (p.splits < 1) p.splits = 1;
+        pl.part_bytes = p.splits > 1 ? (size_t)p.splits * p.rows * NB * sizeof(T) : 0;
+        return ok();
+    }
     pl.rows_kernel = !p.tx;
     const int64_t br = pl.rows_kernel ? RowCfg<T, NB>::BR : ColCfg<T, NB>::BR;
     const int64_t gran = pl.rows_kernel ? RowCfg<T, NB>::KS : ColCfg<T, NB>::U;
@@ -366,8 +560,61 @@ gb_status make_plan(SkParams &p, Plan &pl) {
     return ok();
 }
 
+template <int NS, bool XCOLS, bool WT>
+gb_status launch_thin(const CUtensorMap &tx, const CUtensorMap &tw, const thin::TParams &tp, int grid,
+                      cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        GB_CUDA_TRY(cudaFuncSetAttribute(thin::thin_tma_kernel<NS, XCOLS, WT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, thin::SMEM));
+        attr = true;
+    }
+    thin::thin_tma_kernel<NS, XCOLS, WT><<<grid, thin::NTH, thin::SMEM, st>>>(tx, tw, tp);
+    GB_LAUNCH_CHECK("thin_tma_kernel");
+    return ok();
+}
+
 template <typename T, int NB>
 gb_status launch_plan(const SkParams &p, const Plan &pl, cudaStream_t st) {
+    if (pl.tma) {
+        const int ns = p.n <= 4 ? 4 : 8;
+        CUtensorMap tx, tw;
+        bool okm = p.tx ? make_tmap_f32(&tx, p.X, (uint64_t)p.rows, (uint64_t)p.K, (uint64_t)p.ldx * 4, thin::BR,
+                                        thin::BK, false)
+                        : make_tmap_f32(&tx, p.X, (uint64_t)p.K, (uint64_t)p.rows, (uint64_t)p.ldx * 4, thin::BK,
+                                        thin::BR, true);
+        okm = okm && (p.tw ? make_tmap_f32(&tw, p.W, (uint64_t)p.K, (uint64_t)p.n, (uint64_t)p.ldw * 4, thin::BK,
+                                           (uint32_t)ns, false)
+                           : make_tmap_f32(&tw, p.W, (uint64_t)p.n, (uint64_t)p.K, (uint64_t)p.ldw * 4,
+                                           (uint32_t)ns, thin::BK, false));
+        if (!okm) return set_status(GB_ERR_CUDA, "skinny: cuTensorMapEncodeTiled failed");
+        int *err = error_word();
+        if (!err) return set_status(GB_ERR_OOM, "skinny: no device error word");
+        thin::TParams tp{p.rows, p.K, p.n, p.splits, (int)(p.kchunk / thin::BK), (int)pl.rtiles, p.C, p.cs_r,
+                         p.cs_c, (float)p.alpha, (float)p.beta, p.semantics, (float *)p.part, err};
+        const int64_t units = pl.rtiles * p.splits;
+        const int grid = (int)(units < sm_count() ? units : sm_count());
+        gb_status s;
+        const int sel = (ns == 8 ? 4 : 0) | (p.tx ? 2 : 0) | (p.tw ? 1 : 0);
+        switch (sel) {
+            case 0: s = launch_thin<4, false, false>(tx, tw, tp, grid, st); break;
+            case 1: s = launch_thin<4, false, true>(tx, tw, tp, grid, st); break;
+            case 2: s = launch_thin<4, true, false>(tx, tw, tp, grid, st); break;
+            case 3: s = launch_thin<4, true, true>(tx, tw, tp, grid, st); break;
+            case 4: s = launch_thin<8, false, false>(tx, tw, tp, grid, st); break;
+            case 5: s = launch_thin<8, false, true>(tx, tw, tp, grid, st); break;
+            case 6: s = launch_thin<8, true, false>(tx, tw, tp, grid, st); break;
+            default: s = launch_thin<8, true, true>(tx, tw, tp, grid, st); break;
+        }
+        if (s != GB_OK) return s;
+        if (p.splits > 1) {
+            int blocks = (int)(ceil_div(p.rows * p.n, 256) < 4 * sm_count() ? ceil_div(p.rows * p.n, 256)
+                                                                             : 4 * sm_count());
+            skinny_reduce_kernel<T, NB><<<blocks, 256, 0, st>>>(p);
+            GB_LAUNCH_CHECK("skinny_reduce_kernel");
+        }
+        return ok();
+    }
     dim3 grid((unsigned)pl.rtiles, (unsigned)p.splits);
     if (pl.rows_kernel) {
         if (pl.vec && pl.wvec) skinny_rows_kernel<T, NB, true, true><<<grid, NT, 0, st>>>(p);

@@ -84,7 +84,9 @@ typedef enum gb_algo {
     GB_ALGO_DMMA = 3,     /* FP64 tensor pipe (mma.sync m8n8k4 f64)             */
     GB_ALGO_BF16X3 = 4,   /* SGEMM as hi*hi+hi*lo+lo*hi BF16 on tcgen05, FP32 acc */
     GB_ALGO_OZAKI = 5,    /* DGEMM from exact integer slices on tensor cores    */
-    GB_ALGO_SKINNY = 6    /* tiny M (shortA) / tiny N (thinB) streaming kernels */
+    GB_ALGO_SKINNY = 6,   /* tiny M (shortA) / tiny N (thinB) streaming kernels */
+    GB_ALGO_BF16X6 = 7    /* SGEMM from 3 BF16 pieces (6 products) on tcgen05:
+                             FP32-level error at half the BF16X3 rate        */
 } gb_algo;
 
 typedef enum gb_semantics {

@@ -90,3 +90,142 @@ def test_bf16x3_scalar_beta_semantics(torch, sem):
     dC = dev(C0)
     gbblas.sgemm("N", "N", M, N, K, 1.5, dev(A), K, dev(B), N, 3.0, dC, N, algo=gbblas.ALGO_BF16X3, semantics=sem)
     assert np.array_equal(host(dC), want.astype(np.float32))
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("M,N,K", [(300, 16, 128), (257, 40, 96), (1000, 100, 64), (129, 300, 160), (640, 8, 4096)])
+def test_bf16x3_fused_tile_widths_exact(torch, mode, M, N, K):
+    """Aligned leading dimensions can take the fused-split kernel (forced
+    here); N picks the 32/64/128/256-wide tile.  Small integers: exact."""
+    import os
+    import gbblas
+    os.environ["GB_BF16X3_PATH"] = "fused"
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    pa, pb = (-ac) % 4, (-bc) % 4            # pad leading dimensions to a multiple of 4
+    A, B, C0 = _ints(ar, ac, 7, ld=ac + pa), _ints(br, bc, 8, ld=bc + pb), _ints(M, N, 9)
+    opA = A[:, :ac].T if ta == "T" else A[:, :ac]
+    opB = B[:, :bc].T if tb == "T" else B[:, :bc]
+    want = (-1.0 * (opA.astype(np.float64) @ opB.astype(np.float64)) + 0.5 * C0).astype(np.float32)
+    dC = dev(C0)
+    try:
+        gbblas.sgemm(ta, tb, M, N, K, -1.0, dev(A), ac + pa, dev(B), bc + pb, 0.5, dC, N, algo=gbblas.ALGO_BF16X3)
+    finally:
+        os.environ.pop("GB_BF16X3_PATH", None)
+    got = host(dC)
+    assert np.array_equal(got, want), (mode, np.argwhere(got != want)[:4])
+
+
+def test_bf16x3_fused_matches_two_pass(torch):
+    import os
+    import gbblas
+    M, N, K = 700, 520, 2000
+    A = oracle.fill(M, K, 51, dtype=np.float32)
+    B = oracle.fill(N, K, 52, dtype=np.float32)
+    C0 = oracle.fill(M, N, 53, dtype=np.float32)
+    outs = []
+    for path in ("fused", "two-pass"):
+        os.environ["GB_BF16X3_PATH"] = path
+        try:
+            dC = dev(C0)
+            gbblas.sgemm("N", "T", M, N, K, 1.25, dev(A), K, dev(B), K, -0.75, dC, N, algo=gbblas.ALGO_BF16X3)
+            outs.append(host(dC))
+        finally:
+            os.environ.pop("GB_BF16X3_PATH", None)
+    # same products, same per-K-step MMA order: identical results
+    assert outs[0].tobytes() == outs[1].tobytes()
+
+
+# ---------------------------------------------------------------- BF16X6
+# Three BF16 pieces per operand (hi, mid, lo: 24 significand bits, so any
+# FP32 value of normal range is carried exactly) and the six piece products
+# of combined weight >= 2^-16.  The dropped products (mid*lo, lo*mid, lo*lo)
+# and the representation residue sum to about 2^-25 relative, below u32, so
+# the error is the FP32 accumulation's own.
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (130, 300, 70), (7, 9, 5), (1030, 700, 96)])
+def test_bf16x6_exact_on_integers(torch, mode, M, N, K):
+    import gbblas
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A, B = _ints(ar, ac, 11), _ints(br, bc, 12)
+    C0 = _ints(M, N, 13)
+    opA = A.T if ta == "T" else A
+    opB = B.T if tb == "T" else B
+    want = (2.0 * (opA.astype(np.float64) @ opB.astype(np.float64)) - 1.0 * C0).astype(np.float32)
+    dC = dev(C0)
+    gbblas.sgemm(ta, tb, M, N, K, 2.0, dev(A), ac, dev(B), bc, -1.0, dC, N, algo=gbblas.ALGO_BF16X6)
+    got = host(dC)
+    assert np.array_equal(got, want), (mode, np.argwhere(got != want)[:5])
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_bf16x6_carries_24_bits(torch, mode):
+    """A holds 20-bit integers (hi + lo alone carry 16 bits): only the
+    three-piece split reproduces the products exactly."""
+    import gbblas
+    ta, tb = mode
+    M, N, K = 256, 384, 8
+    rng = np.random.default_rng(14)
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A = rng.integers(-(1 << 19), 1 << 19, size=(ar, ac)).astype(np.float32)
+    B = rng.integers(-3, 4, size=(br, bc)).astype(np.float32)
+    opA = A.T if ta == "T" else A
+    opB = B.T if tb == "T" else B
+    want = (opA.astype(np.float64) @ opB.astype(np.float64)).astype(np.float32)   # |sum| < 2^24: exact
+    dC = dev(np.zeros((M, N), np.float32))
+    gbblas.sgemm(ta, tb, M, N, K, 1.0, dev(A), ac, dev(B), bc, 0.0, dC, N, algo=gbblas.ALGO_BF16X6)
+    got = host(dC)
+    assert np.array_equal(got, want), (mode, np.argwhere(got != want)[:5])
+    dC3 = dev(np.zeros((M, N), np.float32))
+    gbblas.sgemm(ta, tb, M, N, K, 1.0, dev(A), ac, dev(B), bc, 0.0, dC3, N, algo=gbblas.ALGO_BF16X3)
+    assert not np.array_equal(host(dC3), want)   # two pieces lose the low bits
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("M,N,K,pad", [(384, 512, 1040, 16), (333, 257, 515, 3), (1, 1, 1, 0), (129, 1000, 4096, 8),
+                                       (64, 64, 3, 1)])
+def test_bf16x6_normwise_fp32_level(torch, mode, M, N, K, pad):
+    """Unlike BF16X3 there is no split floor: the FP32 bound holds at any K."""
+    import gbblas
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A = oracle.fill(ar, ac, 41, dtype=np.float32, ld=ac + pad)
+    B = oracle.fill(br, bc, 42, dtype=np.float32, ld=bc + pad)
+    C0 = oracle.fill(M, N, 43, dtype=np.float32, ld=N + pad)
+    dC = dev(C0)
+    gbblas.sgemm(ta, tb, M, N, K, 1.5, dev(A), ac + pad, dev(B), bc + pad, -0.5, dC, N + pad,
+                 algo=gbblas.ALGO_BF16X6)
+    got = host(dC)
+    rows = np.arange(0, M, max(1, M // 97))
+    cols = np.arange(0, N, max(1, N // 97))
+    err, _ = oracle.normwise_error(got, ta, tb, M, N, K, 1.5, A, ac + pad, B, bc + pad, -0.5, C0, N + pad,
+                                   rows, cols)
+    assert err <= (2 * K + 4) * 2.0 ** -24, err
+    if pad:
+        assert np.array_equal(got[:, N:], C0[:, N:])
+
+
+def test_bf16x6_error_tracks_simt(torch):
+    """At K = 4096 the six-product result is as accurate as plain FFMA
+    (within 2x), and an order of magnitude better than three products."""
+    import gbblas
+    M = N = 512
+    K = 4096
+    A = oracle.fill(M, K, 61, dtype=np.float32)
+    B = oracle.fill(K, N, 62, dtype=np.float32)
+    C0 = np.zeros((M, N), np.float32)
+    rows = np.arange(0, M, 8)
+    cols = np.arange(0, N, 8)
+    errs = {}
+    for name, algo in (("simt", gbblas.ALGO_SIMT), ("x3", gbblas.ALGO_BF16X3), ("x6", gbblas.ALGO_BF16X6)):
+        dC = dev(C0)
+        gbblas.sgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=algo)
+        errs[name], _ = oracle.normwise_error(host(dC), "N", "N", M, N, K, 1.0, A, K, B, N, 0.0, C0, N, rows, cols)
+    assert errs["x6"] <= 2 * errs["simt"], errs
+    assert errs["x6"] * 4 <= errs["x3"], errs
