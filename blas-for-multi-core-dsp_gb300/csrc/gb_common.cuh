@@ -93,6 +93,24 @@ gb_status launch_sgemm_bf16x6(const GemmArgs &g);
 gb_status launch_dgemm_ozaki(const GemmArgs &g, int slices);
 // Slice count (2..8) whose truncation error meets a normwise target for this K.
 int ozaki_pick_slices(double target_err, int64_t K);
+// Skinny FP32 product on the tensor cores (skinny_tc.cu): X rows x K (tx:
+// stored K x rows), W K x n (tw: stored n x K), 8 < n <= nb in {16, 32, 64}.
+struct ThinTcArgs {
+    int64_t rows, K;
+    const float *X; int64_t ldx; int tx;
+    const float *W; int64_t ldw; int tw;
+    int n, nb;
+    float *C; int64_t cs_r, cs_c;
+    float alpha, beta;
+    int semantics;
+    int splits; int64_t kchunk; int64_t rtiles;   // units of 128 rows x kchunk
+    float *part;                                   // splits x rows x nb partials (splits > 1)
+    void *wpieces;                                 // thin_tc_wpieces_bytes(nb, K) of scratch
+    cudaStream_t stream;
+};
+size_t thin_tc_wpieces_bytes(int nb, int64_t K);
+gb_status launch_thin_tc(const ThinTcArgs &a);
+
 gb_status launch_skinny_f32(const GemmArgs &g);
 gb_status launch_skinny_f64(const GemmArgs &g);
 // C = beta*C (beta==0: C = 0) or C = C + beta (scalar) epilogue-only path (K == 0)

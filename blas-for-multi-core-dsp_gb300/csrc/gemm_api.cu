@@ -61,8 +61,9 @@ int pick(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
         if (skinny) return GB_ALGO_SKINNY;
         return GB_ALGO_ORDERED;
     }
-    if (small <= 64 && large >= 4 * small && large >= 1024)   // FP32 skinny: FFMA streaming up to 8,
-        return (small > 8 && K >= 64) ? GB_ALGO_BF16X3 : GB_ALGO_SKINNY;    // fused-split tensor cores beyond
+    // FP32 skinny: the skinny path streams X once (FFMA up to n = 8, 3xBF16
+    // with X split in flight into tensor memory beyond)
+    if (small <= 64 && large >= 4 * small && large >= 1024) return GB_ALGO_SKINNY;
     if (K >= 64 && work > 134217728.0) return GB_ALGO_BF16X3;
     return GB_ALGO_SIMT;
 }

@@ -45,6 +45,7 @@ struct SkParams {
     int semantics;
     int splits; int64_t kchunk;           // split-K
     void *part;                           // splits x rows x NB partials (split-K only)
+    void *wpieces;                        // BF16 pieces of W (tensor-core form only)
 };
 
 // row-major X: R rows per warp, lane l covers k = 32*V*step + V*l .. +V-1
@@ -325,22 +326,37 @@ __global__ void __launch_bounds__(NT) skinny_cols_kernel(SkParams p) {
 
 // ---------------------------------------------------------------------------
 // FP32, n <= 8: the large operand streamed by TMA.  Persistent CTAs (one per
-// SM) walk units of 256 rows x one K range; a producer warp keeps 6 stages of
-// 256 x 32 X values (32 KB, plus the matching 32 x NS slice of W) in flight,
-// so the memory system sees ~200 KB of outstanding reads per SM whatever
-// the register use; 8 consumer warps own one row each per thread and run
-// the whole K range of it (FMAs in k order, no cross-thread reduction).
+// SM) walk units of BR rows x one K range; a producer warp keeps the stages
+// (BR x 32 X values plus the matching 32 x NS slice of W) in flight, so the
+// memory system sees ~200 KB of outstanding reads per SM whatever the
+// register use; consumer threads own R rows each and run the whole K range
+// of them (FMAs in k order, no cross-thread reduction).
 // X row-major arrives as 128-byte-swizzled 32-float rows (conflict-free
-// 16-byte reads across 8 consecutive rows); X K-major as [32 k][256 rows].
-// W is read by broadcast in either of its layouts.  Partial sums of a split
-// K range go to scratch for skinny_reduce_kernel.
+// 16-byte reads across 8 consecutive rows); X K-major as [32 k][256 rows]
+// boxes.  W is read by broadcast in either of its layouts; a broadcast read
+// still costs a shared-memory wavefront per value, so for n = 8 each thread
+// keeps R = 4 rows to share every W value across four rows (that keeps the
+// shared-memory pipe near half load at full HBM rate), for n <= 4 one row.
+// Partial sums of a split K range go to scratch for skinny_reduce_kernel.
 namespace thin {
 
-constexpr int BR = 256, BK = 32, STAGES = 6, NCW = 8, NTH = (NCW + 1) * 32;
-constexpr int XS = BR * BK * 4;     // 32 KB
+constexpr int BK = 32;
 constexpr int WS = 1024;            // W slice (BK x NS floats), padded to keep stages 1 KB aligned
-constexpr int STAGE = XS + WS;
-constexpr int SMEM = STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/;
+
+template <int R>
+struct TCfg {
+    static constexpr int NCW = R == 1 ? 8 : 4;                 // consumer warps
+    static constexpr int NTH = (NCW + 1) * 32;
+    static constexpr int BR = NCW * 32 * R;                    // rows per unit: 256 or 512
+    static constexpr int NBOX = BR / 256;                      // TMA boxes of 256 rows per stage
+    static constexpr int XS = BR * BK * 4;                     // 32 or 64 KB
+    static constexpr int STAGE = XS + WS;
+    static constexpr int STAGES = R == 1 ? 6 : 3;
+    static constexpr int SMEM = STAGES * STAGE + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+template <int NS>
+__host__ __device__ constexpr int rows_per_thread() { return NS > 4 ? 4 : 1; }
 
 struct TParams {
     int64_t rows, K;
@@ -353,8 +369,12 @@ struct TParams {
 };
 
 template <int NS, bool XCOLS, bool WT>
-__global__ void __launch_bounds__(NTH, 1) thin_tma_kernel(const __grid_constant__ CUtensorMap tmx,
-                                                          const __grid_constant__ CUtensorMap tmw, TParams p) {
+__global__ void __launch_bounds__(TCfg<rows_per_thread<NS>()>::NTH, 1)
+    thin_tma_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, TParams p) {
+    constexpr int R = rows_per_thread<NS>();
+    using CF = TCfg<R>;
+    constexpr int NCW = CF::NCW, BR = CF::BR, STAGES = CF::STAGES, STAGE = CF::STAGE, XS = CF::XS;
+    constexpr int TPR = NCW * 32;   // threads per row slot
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE);
@@ -385,8 +405,11 @@ __global__ void __launch_bounds__(NTH, 1) thin_tma_kernel(const __grid_constant_
                     if (g >= STAGES && !ptx::mbar_wait(&empty[s], ((g / STAGES) & 1) ^ 1, p.err, 41)) return;
                     uint8_t *st = smem + s * STAGE;
                     ptx::mbar_arrive_expect_tx(&full[s], XS + BK * NS * 4);
-                    if (XCOLS) ptx::tma_load_2d(st, &tmx, &full[s], r0, kb * BK);
-                    else ptx::tma_load_2d(st, &tmx, &full[s], kb * BK, r0);
+#pragma unroll
+                    for (int bx = 0; bx < CF::NBOX; bx++) {
+                        if (XCOLS) ptx::tma_load_2d(st + bx * 32768, &tmx, &full[s], r0 + bx * 256, kb * BK);
+                        else ptx::tma_load_2d(st + bx * 32768, &tmx, &full[s], kb * BK, r0 + bx * 256);
+                    }
                     if (WT) ptx::tma_load_2d(st + XS, &tmw, &full[s], kb * BK, 0);
                     else ptx::tma_load_2d(st + XS, &tmw, &full[s], 0, kb * BK);
                 }
@@ -395,14 +418,17 @@ __global__ void __launch_bounds__(NTH, 1) thin_tma_kernel(const __grid_constant_
         return;
     }
 
-    const int t = threadIdx.x;   // consumer: row r0 + t
+    // consumer thread t: rows r0 + t + i*TPR, i < R (row slot i: 32 consecutive rows per warp)
+    const int t = threadIdx.x;
     int g = 0;
     for (int u = blockIdx.x; u < units; u += gridDim.x) {
         const int rt = u / p.splits, sp = u - rt * p.splits;
         const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
-        float acc[NS];
+        float acc[R][NS];
 #pragma unroll
-        for (int j = 0; j < NS; j++) acc[j] = 0.f;
+        for (int i = 0; i < R; i++)
+#pragma unroll
+            for (int j = 0; j < NS; j++) acc[i][j] = 0.f;
         bool go = true;
         for (int kb = kb0; kb < kb1; kb++, g++) {
             const int s = g % STAGES;
@@ -412,17 +438,23 @@ __global__ void __launch_bounds__(NTH, 1) thin_tma_kernel(const __grid_constant_
             // two halves of 16 k, so the W reads the compiler hoists stay in registers
 #pragma unroll 1
             for (int h = 0; h < BK; h += 16) {
-                float x[16];
-                if (XCOLS) {
-                    const float *xs = reinterpret_cast<const float *>(st);
+                float x[R][16];
 #pragma unroll
-                    for (int kk = 0; kk < 16; kk++) x[kk] = xs[(h + kk) * BR + t];
-                } else {
-                    const uint8_t *row = st + t * 128;
+                for (int i = 0; i < R; i++) {
+                    const int lr = t + i * TPR;                       // row within the unit
+                    const uint8_t *box = st + (lr >> 8) * 32768;      // its 256-row TMA box
+                    const int br = lr & 255;
+                    if (XCOLS) {
+                        const float *xs = reinterpret_cast<const float *>(box);
 #pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        const float4 v = *reinterpret_cast<const float4 *>(row + (((h / 4 + c) ^ (t & 7)) << 4));
-                        x[4 * c] = v.x; x[4 * c + 1] = v.y; x[4 * c + 2] = v.z; x[4 * c + 3] = v.w;
+                        for (int kk = 0; kk < 16; kk++) x[i][kk] = xs[(h + kk) * 256 + br];
+                    } else {
+                        const uint8_t *row = box + br * 128;
+#pragma unroll
+                        for (int c = 0; c < 4; c++) {
+                            const float4 v = *reinterpret_cast<const float4 *>(row + (((h / 4 + c) ^ (br & 7)) << 4));
+                            x[i][4 * c] = v.x; x[i][4 * c + 1] = v.y; x[i][4 * c + 2] = v.z; x[i][4 * c + 3] = v.w;
+                        }
                     }
                 }
                 if (WT) {   // ws[j][kk]
@@ -431,10 +463,13 @@ __global__ void __launch_bounds__(NTH, 1) thin_tma_kernel(const __grid_constant_
 #pragma unroll
                         for (int j = 0; j < NS; j++) {
                             const float4 w = *reinterpret_cast<const float4 *>(ws + j * BK + h + k4);
-                            acc[j] = fmaf(x[k4], w.x, acc[j]);
-                            acc[j] = fmaf(x[k4 + 1], w.y, acc[j]);
-                            acc[j] = fmaf(x[k4 + 2], w.z, acc[j]);
-                            acc[j] = fmaf(x[k4 + 3], w.w, acc[j]);
+#pragma unroll
+                            for (int i = 0; i < R; i++) {
+                                acc[i][j] = fmaf(x[i][k4], w.x, acc[i][j]);
+                                acc[i][j] = fmaf(x[i][k4 + 1], w.y, acc[i][j]);
+                                acc[i][j] = fmaf(x[i][k4 + 2], w.z, acc[i][j]);
+                                acc[i][j] = fmaf(x[i][k4 + 3], w.w, acc[i][j]);
+                            }
                         }
                     }
                 } else {    // ws[kk][j]
@@ -443,10 +478,13 @@ __global__ void __launch_bounds__(NTH, 1) thin_tma_kernel(const __grid_constant_
 #pragma unroll
                         for (int j4 = 0; j4 < NS; j4 += 4) {
                             const float4 w = *reinterpret_cast<const float4 *>(ws + (h + kk) * NS + j4);
-                            acc[j4] = fmaf(x[kk], w.x, acc[j4]);
-                            acc[j4 + 1] = fmaf(x[kk], w.y, acc[j4 + 1]);
-                            acc[j4 + 2] = fmaf(x[kk], w.z, acc[j4 + 2]);
-                            acc[j4 + 3] = fmaf(x[kk], w.w, acc[j4 + 3]);
+#pragma unroll
+                            for (int i = 0; i < R; i++) {
+                                acc[i][j4] = fmaf(x[i][kk], w.x, acc[i][j4]);
+                                acc[i][j4 + 1] = fmaf(x[i][kk], w.y, acc[i][j4 + 1]);
+                                acc[i][j4 + 2] = fmaf(x[i][kk], w.z, acc[i][j4 + 2]);
+                                acc[i][j4 + 3] = fmaf(x[i][kk], w.w, acc[i][j4 + 3]);
+                            }
                         }
                     }
                 }
@@ -455,28 +493,30 @@ __global__ void __launch_bounds__(NTH, 1) thin_tma_kernel(const __grid_constant_
             if (lane == 0) ptx::mbar_arrive(&empty[s]);
         }
         if (!go) break;
-        const int64_t row = (int64_t)rt * BR + t;
-        if (row < p.rows) {
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+            const int64_t row = (int64_t)rt * BR + t + i * TPR;
+            if (row >= p.rows) continue;
             if (p.splits > 1) {
                 float *pp = p.part + ((int64_t)sp * p.rows + row) * 8;
 #pragma unroll
-                for (int j = 0; j < NS; j++) pp[j] = acc[j];
-            } else {
-                float *c = (float *)p.C + row * p.cs_r;
+                for (int j = 0; j < NS; j++) pp[j] = acc[i][j];
+                continue;
+            }
+            float *c = (float *)p.C + row * p.cs_r;
 #pragma unroll
-                for (int j = 0; j < NS; j++) {
-                    if (j >= p.n) break;
-                    float *cp = c + (int64_t)j * p.cs_c;
-                    float v = p.alpha * acc[j];
-                    if (p.semantics == GB_SEM_BLAS) {
-                        if (p.beta != 0.f) v = fmaf(p.beta, *cp, v);
-                    } else if (p.semantics == GB_SEM_SCALAR_BETA) {
-                        v = v + p.beta;
-                    } else {
-                        v = *cp + (v + p.beta);
-                    }
-                    *cp = v;
+            for (int j = 0; j < NS; j++) {
+                if (j >= p.n) break;
+                float *cp = c + (int64_t)j * p.cs_c;
+                float v = p.alpha * acc[i][j];
+                if (p.semantics == GB_SEM_BLAS) {
+                    if (p.beta != 0.f) v = fmaf(p.beta, *cp, v);
+                } else if (p.semantics == GB_SEM_SCALAR_BETA) {
+                    v = v + p.beta;
+                } else {
+                    v = *cp + (v + p.beta);
                 }
+                *cp = v;
             }
         }
     }
@@ -500,8 +540,10 @@ __global__ void skinny_reduce_kernel(SkParams p) {
 struct Plan {
     bool rows_kernel, vec, wvec;
     bool tma;                 // FP32 n <= 8 with TMA-compatible layouts: thin::thin_tma_kernel
+    bool tc;                  // FP32 8 < n <= 64, K >= 64: 3xBF16 on the tensor cores (skinny_tc.cu)
     int64_t rtiles;
     size_t part_bytes;
+    size_t w_bytes;           // scratch for the BF16 pieces of W (tc)
 };
 
 // TMA needs 16-byte aligned bases and row strides that are multiples of 16
@@ -515,17 +557,47 @@ bool tma_eligible(const SkParams &p) {
            (uintptr_t)p.X % 16 == 0 && (uintptr_t)p.W % 16 == 0;
 }
 
+// The tensor-core form: X read by TMA (16-byte aligned, ldx % 4 == 0), any
+// W layout (it is split into BF16 pieces first); GB_SKINNY_TC=0 turns it off.
 template <typename T, int NB>
-gb_status make_plan(SkParams &p, Plan &pl) {
+bool tc_eligible(const SkParams &p) {
+    if (sizeof(T) != 4 || NB < 16 || p.n <= 8 || p.K < 64) return false;
+    const char *e = getenv("GB_SKINNY_TC");
+    if (e && e[0] == '0') return false;
+    return p.rows < (int64_t(1) << 31) && p.K < (int64_t(1) << 30) && p.ldx % 4 == 0 && (uintptr_t)p.X % 16 == 0;
+}
+
+template <typename T, int NB>
+gb_status make_plan(SkParams &p, Plan &pl, bool allow_tc = true) {
+    pl.w_bytes = 0;
+    pl.tc = allow_tc && tc_eligible<T, NB>(p);
+    if (pl.tc) {
+        // units of 128 rows x a K range; split K until there are ~4 units per SM
+        pl.tma = false;
+        pl.rows_kernel = !p.tx;
+        pl.vec = pl.wvec = true;
+        pl.rtiles = ceil_div(p.rows, 128);
+        const int64_t nkb = ceil_div(p.K, 32);
+        int splits = 1;
+        while (pl.rtiles * splits < 4 * (int64_t)sm_count() && nkb / (splits * 2) >= 16 && splits < 64) splits *= 2;
+        const int64_t ckb = ceil_div(nkb, splits);
+        p.kchunk = ckb * 32;
+        p.splits = (int)ceil_div(nkb, ckb);
+        pl.part_bytes = p.splits > 1 ? (size_t)p.splits * p.rows * NB * sizeof(T) : 0;
+        pl.w_bytes = thin_tc_wpieces_bytes(NB, p.K);
+        return ok();
+    }
     pl.tma = tma_eligible<T, NB>(p);
     if (pl.tma) {
         // units of 256 rows x a K range; split K until there are ~4 units per SM
         pl.rows_kernel = !p.tx;
         pl.vec = pl.wvec = true;
-        pl.rtiles = ceil_div(p.rows, thin::BR);
+        const int br = p.n > 4 ? thin::TCfg<4>::BR : thin::TCfg<1>::BR;
+        pl.rtiles = ceil_div(p.rows, br);
         const int64_t nkb = ceil_div(p.K, thin::BK);
+        // split K until there are ~6 units per SM (tail balance of the persistent grid)
         int splits = 1;
-        while (pl.rtiles * splits < 4 * (int64_t)sm_count() && nkb / (splits * 2) >= 16 && splits < 64) splits *= 2;
+        while (pl.rtiles * splits < 6 * (int64_t)sm_count() && nkb / (splits * 2) >= 16 && splits < 64) splits *= 2;
         const int64_t ckb = ceil_div(nkb, splits);
         p.kchunk = ckb * thin::BK;
         p.splits = (int)ceil_div(nkb, ckb);
@@ -563,26 +635,41 @@ gb_status make_plan(SkParams &p, Plan &pl) {
 template <int NS, bool XCOLS, bool WT>
 gb_status launch_thin(const CUtensorMap &tx, const CUtensorMap &tw, const thin::TParams &tp, int grid,
                       cudaStream_t st) {
+    using CF = thin::TCfg<thin::rows_per_thread<NS>()>;
     static bool attr = false;
     if (!attr) {
         GB_CUDA_TRY(cudaFuncSetAttribute(thin::thin_tma_kernel<NS, XCOLS, WT>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, thin::SMEM));
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM));
         attr = true;
     }
-    thin::thin_tma_kernel<NS, XCOLS, WT><<<grid, thin::NTH, thin::SMEM, st>>>(tx, tw, tp);
+    thin::thin_tma_kernel<NS, XCOLS, WT><<<grid, CF::NTH, CF::SMEM, st>>>(tx, tw, tp);
     GB_LAUNCH_CHECK("thin_tma_kernel");
     return ok();
 }
 
 template <typename T, int NB>
 gb_status launch_plan(const SkParams &p, const Plan &pl, cudaStream_t st) {
+    if (pl.tc) {
+        ThinTcArgs a{p.rows, p.K, (const float *)p.X, p.ldx, p.tx, (const float *)p.W, p.ldw, p.tw, p.n, NB,
+                     (float *)p.C, p.cs_r, p.cs_c, (float)p.alpha, (float)p.beta, p.semantics, p.splits, p.kchunk,
+                     pl.rtiles, (float *)p.part, p.wpieces, st};
+        gb_status s = launch_thin_tc(a);
+        if (s != GB_OK) return s;
+        if (p.splits > 1) {
+            int blocks = (int)(ceil_div(p.rows * p.n, 256) < 4 * sm_count() ? ceil_div(p.rows * p.n, 256)
+                                                                             : 4 * sm_count());
+            skinny_reduce_kernel<T, NB><<<blocks, 256, 0, st>>>(p);
+            GB_LAUNCH_CHECK("skinny_reduce_kernel");
+        }
+        return ok();
+    }
     if (pl.tma) {
         const int ns = p.n <= 4 ? 4 : 8;
         CUtensorMap tx, tw;
-        bool okm = p.tx ? make_tmap_f32(&tx, p.X, (uint64_t)p.rows, (uint64_t)p.K, (uint64_t)p.ldx * 4, thin::BR,
+        bool okm = p.tx ? make_tmap_f32(&tx, p.X, (uint64_t)p.rows, (uint64_t)p.K, (uint64_t)p.ldx * 4, 256,
                                         thin::BK, false)
                         : make_tmap_f32(&tx, p.X, (uint64_t)p.K, (uint64_t)p.rows, (uint64_t)p.ldx * 4, thin::BK,
-                                        thin::BR, true);
+                                        256, true);
         okm = okm && (p.tw ? make_tmap_f32(&tw, p.W, (uint64_t)p.K, (uint64_t)p.n, (uint64_t)p.ldw * 4, thin::BK,
                                            (uint32_t)ns, false)
                            : make_tmap_f32(&tw, p.W, (uint64_t)p.n, (uint64_t)p.K, (uint64_t)p.ldw * 4,
@@ -638,9 +725,13 @@ gb_status run(SkParams p, cudaStream_t st) {
     Plan pl;
     gb_status s = make_plan<T, NB>(p, pl);
     if (s != GB_OK) return s;
-    if (pl.part_bytes) {
-        p.part = workspace(pl.part_bytes, st);
-        if (!p.part) return (gb_status)gb_get_last_status();
+    if (pl.part_bytes || pl.w_bytes) {
+        // one workspace block: partials, then the W pieces (256-byte aligned)
+        const size_t off = (pl.part_bytes + 255) / 256 * 256;
+        uint8_t *ws = (uint8_t *)workspace(off + pl.w_bytes, st);
+        if (!ws) return (gb_status)gb_get_last_status();
+        p.part = pl.part_bytes ? ws : nullptr;
+        p.wpieces = pl.w_bytes ? ws + off : nullptr;
     }
     return launch_plan<T, NB>(p, pl, st);
 }
@@ -682,8 +773,10 @@ gb_status launch_skinny_f64(const GemmArgs &g) { return dispatch<double>(g); }
 
 // ---------------------------------------------------------------------------
 // gb_sgemm_skinny_noalloc: the FP32 skinny GEMM for callers that cannot
-// allocate device memory on the call path.  It is the same kernels with the
-// same split-K plan as the GB_ALGO_SKINNY path above, but the split-K
+// allocate device memory on the call path.  It is the FFMA kernels with the
+// same split-K plan as the GB_ALGO_SKINNY path above (for 8 < n <= 64 that
+// path runs on the tensor cores instead, whose W pieces need scratch of
+// their own, so here n > 8 keeps the FFMA streaming kernels), but the split-K
 // partial sums live in a fixed array of device memory reserved when the
 // library is loaded, so the call itself never calls cudaMalloc / cudaFree or
 // any allocating routine.
@@ -728,7 +821,7 @@ gb_status noalloc_scratch(void **out) {
 template <int NB>
 gb_status run_noalloc(SkParams p, cudaStream_t st) {
     Plan pl;
-    gb_status s = make_plan<float, NB>(p, pl);
+    gb_status s = make_plan<float, NB>(p, pl, /*allow_tc=*/false);
     if (s != GB_OK) return s;
     if (pl.part_bytes) {
         if (pl.part_bytes > kNoAllocScratchBytes)

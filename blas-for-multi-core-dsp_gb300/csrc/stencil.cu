@@ -112,6 +112,92 @@ __global__ void __launch_bounds__(NT) stencil_tb_kernel(const T *__restrict__ sr
     }
 }
 
+// FP32 form: a warp owns whole 128-float rows of the tile, a lane four
+// consecutive columns.  Per output row a thread does one 16-byte shared load
+// (the row below), two shuffles (left / right neighbours of its middle row)
+// and one 16-byte shared store for four points; (top, middle) stay in
+// registers down the warp's row band.  The tile is 128 columns wide including
+// the halo of t cells on each side, so a CTA writes TW = 128 - 2t columns.
+// Columns 0 and 127 of the tile are never inside a sweep's valid region, so
+// the shuffle values the edge lanes receive there are never used.
+constexpr int V4_P = 128, V4_TH = 64;
+
+template <int ORDER>
+__global__ void __launch_bounds__(NT) stencil_v4_kernel(const float *__restrict__ src, float *__restrict__ dst,
+                                                        int64_t M, int64_t N, int tsweeps) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int H = V4_TH + 2 * tsweeps, TW = V4_P - 2 * tsweeps;
+    float *cur = reinterpret_cast<float *>(smem_raw);
+    float *nxt = cur + H * V4_P;
+    const int64_t ld = N + 2;
+    const int64_t R0 = 1 + (int64_t)blockIdx.y * V4_TH - tsweeps;   // padded coords of local (0,0)
+    const int64_t C0 = 1 + (int64_t)blockIdx.x * TW - tsweeps;
+    const int lane = threadIdx.x % 32, band = threadIdx.x / 32;
+
+    for (int lr = band; lr < H; lr += NT / 32) {
+        const int64_t r = R0 + lr;
+        if (r < 0 || r > M + 1) continue;
+        const float *srow = src + r * ld;
+        for (int lc = lane; lc < V4_P; lc += 32) {
+            const int64_t c = C0 + lc;
+            if (c >= 0 && c <= N + 1) cur[lr * V4_P + lc] = srow[c];
+        }
+    }
+    __syncthreads();
+
+    // this lane's four columns: fixed when on (or beyond) the grid boundary
+    bool cfix[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int64_t gc = C0 + 4 * lane + q;
+        cfix[q] = gc <= 0 || gc >= N + 1;
+    }
+    using O = SOps<float>;
+    for (int s = 1; s <= tsweeps; s++) {
+        const int h = H - 2 * s;
+        const int per = (h + NT / 32 - 1) / (NT / 32);
+        const int rbeg = s + band * per;
+        const int rend = min(rbeg + per, H - s);
+        if (rbeg < rend) {   // warp-uniform
+            const float4 *cp = reinterpret_cast<const float4 *>(cur + rbeg * V4_P) + lane;
+            float4 *np = reinterpret_cast<float4 *>(nxt + rbeg * V4_P) + lane;
+            float4 top = cp[-V4_P / 4], mid = cp[0];
+            int64_t gr = R0 + rbeg;
+            for (int lr = rbeg; lr < rend; lr++, cp += V4_P / 4, np += V4_P / 4, gr++) {
+                const float4 down = cp[V4_P / 4];
+                const float left0 = __shfl_up_sync(0xffffffffu, mid.w, 1);
+                const float right3 = __shfl_down_sync(0xffffffffu, mid.x, 1);
+                const bool rfix = gr <= 0 || gr >= M + 1;
+                float4 v;
+                v.x = update<float, ORDER>(top.x, left0, mid.y, down.x, mid.x, gr - 1);
+                v.y = update<float, ORDER>(top.y, mid.x, mid.z, down.y, mid.y, gr - 1);
+                v.z = update<float, ORDER>(top.z, mid.y, mid.w, down.z, mid.z, gr - 1);
+                v.w = update<float, ORDER>(top.w, mid.z, right3, down.w, mid.w, gr - 1);
+                if (rfix || cfix[0]) v.x = mid.x;
+                if (rfix || cfix[1]) v.y = mid.y;
+                if (rfix || cfix[2]) v.z = mid.z;
+                if (rfix || cfix[3]) v.w = mid.w;
+                *np = v;
+                top = mid;
+                mid = down;
+            }
+        }
+        __syncthreads();
+        float *tmp = cur; cur = nxt; nxt = tmp;
+    }
+    (void)O::fifth;
+
+    for (int lr = tsweeps + band; lr < tsweeps + V4_TH; lr += NT / 32) {
+        const int64_t r = R0 + lr;
+        if (r < 1 || r > M) continue;
+        float *drow = dst + r * ld;
+        for (int lc = tsweeps + lane; lc < tsweeps + TW; lc += 32) {
+            const int64_t c = C0 + lc;
+            if (c >= 1 && c <= N) drow[c] = cur[lr * V4_P + lc];
+        }
+    }
+}
+
 template <typename T>
 gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *stream) {
     GB_CHECK_ARG(M >= 0 && N >= 0, "stencil2d: negative size");
@@ -121,6 +207,8 @@ gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *
     GB_CHECK_ARG(A && B && A != B, "stencil2d: A and B must be distinct device buffers");
     // tile and temporal depth: FP32 is HBM-bound (block 8 sweeps); FP64 is
     // bound by the FP64 pipe, where recomputing halos only costs, so t = 1.
+    const char *v4env = getenv("GB_STENCIL_V4");
+    const bool v4 = sizeof(T) == 4 && !(v4env && v4env[0] == '0');
     const int tmax = sizeof(T) == 4 ? 8 : 1;
     const int TH = sizeof(T) == 4 ? 64 : 32, TW = sizeof(T) == 4 ? 128 : 64;
     // launches L with L == iters (mod 2) so the result lands in B for odd
@@ -137,6 +225,30 @@ gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *
         if (rem) t += 1;
         const T *src = (l % 2 == 0) ? A : B;
         T *dst = (l % 2 == 0) ? B : A;
+        if (v4) {
+            const size_t sm4 = 2 * (size_t)(V4_TH + 2 * t) * V4_P * sizeof(float);
+            dim3 g4((unsigned)ceil_div(N, V4_P - 2 * t), (unsigned)ceil_div(M, V4_TH));
+            GB_CHECK_ARG(g4.y <= 65535u, "stencil2d: M too large");
+            const float *s4 = (const float *)src;
+            float *d4 = (float *)dst;
+            switch (order) {
+                case 0:
+                    cudaFuncSetAttribute(stencil_v4_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+                    stencil_v4_kernel<0><<<g4, NT, sm4, st>>>(s4, d4, M, N, t);
+                    break;
+                case 1:
+                    cudaFuncSetAttribute(stencil_v4_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+                    stencil_v4_kernel<1><<<g4, NT, sm4, st>>>(s4, d4, M, N, t);
+                    break;
+                default:
+                    cudaFuncSetAttribute(stencil_v4_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
+                    stencil_v4_kernel<2><<<g4, NT, sm4, st>>>(s4, d4, M, N, t);
+                    break;
+            }
+            GB_LAUNCH_CHECK("stencil_v4_kernel");
+            done += t;
+            continue;
+        }
         size_t smem = 2 * (size_t)(TH + 2 * t) * (TW + 2 * t) * sizeof(T);
         switch (order) {
             case 0:

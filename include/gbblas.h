@@ -135,9 +135,11 @@ gb_status gb_dgemm(char transA, char transB, int64_t M, int64_t N, int64_t K,
  * path -- a serving loop that admits work against a fixed HBM budget, a host
  * framework whose device memory belongs to its own pool allocator, or code
  * that must not trigger the device-wide synchronisation cudaFree implies.
- * It computes exactly what gb_sgemm with GB_ALGO_SKINNY computes (same
- * kernels, same split-K plan; thinB when N <= M, else shortA), with
- * min(M, N) <= 64 and K >= 1, but keeps the split-K partial sums in a fixed
+ * For min(M, N) <= 8 it computes exactly what gb_sgemm with GB_ALGO_SKINNY
+ * computes (same kernels, same split-K plan; thinB when N <= M, else
+ * shortA); for 8 < min(M, N) <= 64, where GB_ALGO_SKINNY runs 3xBF16 on the
+ * tensor cores, it runs the FP32 FFMA streaming kernels (FP32 rounding, the
+ * same 2*K*u normwise bound).  K >= 1.  It keeps the split-K partial sums in a fixed
  * 16 MiB array of device memory that every GPU loading the library reserves
  * until the process exits.  A call whose split-K plan needs more than 16 MiB
  * (splits x max(M, N) x padded min(M, N) x 4 bytes) is rejected with

@@ -65,7 +65,8 @@ def test_stencil_golden_one_sweep(torch, M, N):
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("order", [0, 1, 2])
-@pytest.mark.parametrize("M,N,iters", [(1, 1, 1), (33, 47, 2), (64, 130, 7), (200, 333, 17), (129, 64, 20)])
+@pytest.mark.parametrize("M,N,iters", [(1, 1, 1), (33, 47, 2), (64, 130, 7), (200, 333, 17), (129, 64, 20),
+                                      (300, 500, 30), (257, 1000, 16), (130, 113, 9)])
 def test_stencil_iterations_bit_exact(torch, dtype, order, M, N, iters):
     import gbblas
     A = np.ones((M + 2, N + 2), dtype=dtype)            # Dirichlet boundary 1.0

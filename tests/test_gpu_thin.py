@@ -1,5 +1,7 @@
-"""The TMA-streamed FP32 skinny kernel (n = min(M, N) <= 8, 16-byte aligned
-operands with leading dimensions a multiple of 4) against the oracle.
+"""The streamed FP32 skinny kernels against the oracle: the TMA/FFMA kernel
+(n = min(M, N) <= 8) and the tensor-core kernel (8 < n <= 64, K >= 64, X
+split into BF16 hi/lo in tensor memory), both for 16-byte aligned operands
+with leading dimensions a multiple of 4.
 
 * Small-integer inputs: every product and partial sum is an integer below
   2^24, so any summation order gives the exact result -- this pins the
@@ -41,7 +43,8 @@ def _ld(c):
 @pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("kind", ["thinB", "shortA"])
 @pytest.mark.parametrize("small,big,K", [(8, 3001, 1037), (1, 700, 96), (3, 1000, 33), (5, 257, 4099),
-                                         (4, 60, 3000), (8, 513, 20000)])
+                                         (4, 60, 3000), (8, 513, 20000), (12, 3001, 1037), (16, 700, 96),
+                                         (40, 1000, 640), (64, 257, 4099), (33, 60, 3000), (64, 2000, 64)])
 @pytest.mark.parametrize("sem", [0, 1, 2])
 def test_thin_exact_on_integers(torch, mode, kind, small, big, K, sem):
     import gbblas
@@ -73,7 +76,7 @@ def test_thin_exact_on_integers(torch, mode, kind, small, big, K, sem):
 
 @pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("kind", ["thinB", "shortA"])
-@pytest.mark.parametrize("small", [2, 8])
+@pytest.mark.parametrize("small", [2, 8, 16, 64])
 def test_thin_normwise_and_matches_unstreamed(torch, mode, kind, small):
     import gbblas
     ta, tb = mode
@@ -86,14 +89,15 @@ def test_thin_normwise_and_matches_unstreamed(torch, mode, kind, small):
     B = oracle.fill(br, bc, 72, dtype=np.float32, ld=ldb)
     C0 = oracle.fill(M, N, 73, dtype=np.float32, ld=ldc)
     outs = []
-    for tma in ("1", "0"):
-        os.environ["GB_SKINNY_TMA"] = tma
+    for on in ("1", "0"):
+        os.environ["GB_SKINNY_TMA"] = os.environ["GB_SKINNY_TC"] = on
         try:
             dC = dev(C0)
             gbblas.sgemm(ta, tb, M, N, K, 0.5, dev(A), lda, dev(B), ldb, -1.0, dC, ldc, algo=gbblas.ALGO_SKINNY)
             outs.append(host(dC))
         finally:
             os.environ.pop("GB_SKINNY_TMA", None)
+            os.environ.pop("GB_SKINNY_TC", None)
     rows = np.arange(0, M, max(1, M // 61))
     cols = np.arange(0, N, max(1, N // 61))
     for got in outs:
