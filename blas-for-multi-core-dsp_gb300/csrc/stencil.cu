@@ -112,90 +112,92 @@ __global__ void __launch_bounds__(NT) stencil_tb_kernel(const T *__restrict__ sr
     }
 }
 
-// FP32 form: a warp owns whole 128-float rows of the tile, a lane four
-// consecutive columns.  Per output row a thread does one 16-byte shared load
-// (the row below), two shuffles (left / right neighbours of its middle row)
-// and one 16-byte shared store for four points; (top, middle) stay in
-// registers down the warp's row band.  The tile is 128 columns wide including
-// the halo of t cells on each side, so a CTA writes TW = 128 - 2t columns.
-// Columns 0 and 127 of the tile are never inside a sweep's valid region, so
-// the shuffle values the edge lanes receive there are never used.
-constexpr int V4_P = 128, V4_TH = 64;
+// FP32 form, no shared memory: register-streamed temporal blocking.  A warp
+// owns a strip of 128 columns (lane l: columns 4l .. 4l+3) and walks a
+// segment of rows top to bottom, one input row per step.  Sweep level
+// l = 1..T keeps the last two rows of level l-1 in registers; when level l-1
+// produces row rho+1, level l computes row rho from (rho-1, rho, rho+1)
+// with the left / right neighbours of the middle row from the adjacent
+// lanes (two shuffles per four points).  The level-T rows are written out.
+// Each level loses one column at each strip edge and one row at each
+// segment end, so a strip writes 128 - 2T columns and a segment reads T
+// rows of halo above and below.  Every point gets the same neighbours in the
+// same add order as one sweep at a time, so results are bit-identical.
+constexpr int RS_W = 128, RS_SEG = 256, RS_NT = 256;
 
-template <int ORDER>
-__global__ void __launch_bounds__(NT) stencil_v4_kernel(const float *__restrict__ src, float *__restrict__ dst,
-                                                        int64_t M, int64_t N, int tsweeps) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int H = V4_TH + 2 * tsweeps, TW = V4_P - 2 * tsweeps;
-    float *cur = reinterpret_cast<float *>(smem_raw);
-    float *nxt = cur + H * V4_P;
+template <int T, int ORDER>
+__global__ void __launch_bounds__(RS_NT) stencil_rs_kernel(const float *__restrict__ src, float *__restrict__ dst,
+                                                           int64_t M, int64_t N, int strips, int segs) {
+    const int lane = threadIdx.x % 32;
+    const int64_t wid = (int64_t)blockIdx.x * (RS_NT / 32) + threadIdx.x / 32;
+    if (wid >= (int64_t)strips * segs) return;   // whole warp
+    const int sx = (int)(wid % strips), sy = (int)(wid / strips);
     const int64_t ld = N + 2;
-    const int64_t R0 = 1 + (int64_t)blockIdx.y * V4_TH - tsweeps;   // padded coords of local (0,0)
-    const int64_t C0 = 1 + (int64_t)blockIdx.x * TW - tsweeps;
-    const int lane = threadIdx.x % 32, band = threadIdx.x / 32;
+    const int64_t c0 = 1 + (int64_t)sx * (RS_W - 2 * T) - T;   // padded column of lane 0, q = 0
+    const int64_t out_r0 = 1 + (int64_t)sy * RS_SEG;            // padded rows written: [out_r0, out_r1)
+    const int64_t out_r1 = out_r0 + RS_SEG < M + 1 ? out_r0 + RS_SEG : M + 1;
+    const int64_t cl = c0 + 4 * lane;                            // this lane's first column
 
-    for (int lr = band; lr < H; lr += NT / 32) {
-        const int64_t r = R0 + lr;
-        if (r < 0 || r > M + 1) continue;
-        const float *srow = src + r * ld;
-        for (int lc = lane; lc < V4_P; lc += 32) {
-            const int64_t c = C0 + lc;
-            if (c >= 0 && c <= N + 1) cur[lr * V4_P + lc] = srow[c];
-        }
-    }
-    __syncthreads();
-
-    // this lane's four columns: fixed when on (or beyond) the grid boundary
-    bool cfix[4];
+    bool cfix[4], cload[4], cstore[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        const int64_t gc = C0 + 4 * lane + q;
+        const int64_t gc = cl + q;
+        const int lc = 4 * lane + q;
         cfix[q] = gc <= 0 || gc >= N + 1;
+        cload[q] = gc >= 0 && gc <= N + 1;
+        cstore[q] = lc >= T && lc < RS_W - T && gc >= 1 && gc <= N;
     }
-    using O = SOps<float>;
-    for (int s = 1; s <= tsweeps; s++) {
-        const int h = H - 2 * s;
-        const int per = (h + NT / 32 - 1) / (NT / 32);
-        const int rbeg = s + band * per;
-        const int rend = min(rbeg + per, H - s);
-        if (rbeg < rend) {   // warp-uniform
-            const float4 *cp = reinterpret_cast<const float4 *>(cur + rbeg * V4_P) + lane;
-            float4 *np = reinterpret_cast<float4 *>(nxt + rbeg * V4_P) + lane;
-            float4 top = cp[-V4_P / 4], mid = cp[0];
-            int64_t gr = R0 + rbeg;
-            for (int lr = rbeg; lr < rend; lr++, cp += V4_P / 4, np += V4_P / 4, gr++) {
-                const float4 down = cp[V4_P / 4];
-                const float left0 = __shfl_up_sync(0xffffffffu, mid.w, 1);
-                const float right3 = __shfl_down_sync(0xffffffffu, mid.x, 1);
-                const bool rfix = gr <= 0 || gr >= M + 1;
-                float4 v;
-                v.x = update<float, ORDER>(top.x, left0, mid.y, down.x, mid.x, gr - 1);
-                v.y = update<float, ORDER>(top.y, mid.x, mid.z, down.y, mid.y, gr - 1);
-                v.z = update<float, ORDER>(top.z, mid.y, mid.w, down.z, mid.z, gr - 1);
-                v.w = update<float, ORDER>(top.w, mid.z, right3, down.w, mid.w, gr - 1);
-                if (rfix || cfix[0]) v.x = mid.x;
-                if (rfix || cfix[1]) v.y = mid.y;
-                if (rfix || cfix[2]) v.z = mid.z;
-                if (rfix || cfix[3]) v.w = mid.w;
-                *np = v;
-                top = mid;
-                mid = down;
-            }
-        }
-        __syncthreads();
-        float *tmp = cur; cur = nxt; nxt = tmp;
-    }
-    (void)O::fifth;
 
-    for (int lr = tsweeps + band; lr < tsweeps + V4_TH; lr += NT / 32) {
-        const int64_t r = R0 + lr;
-        if (r < 1 || r > M) continue;
-        float *drow = dst + r * ld;
-        for (int lc = tsweeps + lane; lc < tsweeps + TW; lc += 32) {
-            const int64_t c = C0 + lc;
-            if (c >= 1 && c <= N) drow[c] = cur[lr * V4_P + lc];
+    float4 p2[T], p1[T];   // level l-1 rows rho-1 and rho of level l's window
+#pragma unroll
+    for (int l = 0; l < T; l++) p2[l] = p1[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+
+    for (int64_t i = out_r0 - T - 1; i < out_r1 + T; i++) {   // input row i (level 0)
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i >= 0 && i <= M + 1) {
+            const float *row = src + i * ld + cl;
+            if (cload[0]) x.x = __ldg(row);
+            if (cload[1]) x.y = __ldg(row + 1);
+            if (cload[2]) x.z = __ldg(row + 2);
+            if (cload[3]) x.w = __ldg(row + 3);
+        }
+#pragma unroll
+        for (int l = 0; l < T; l++) {
+            // level l+1, row rho = i - l - 1: top p2[l], middle p1[l], down x
+            const int64_t gr = i - l - 1;
+            const float4 top = p2[l], mid = p1[l];
+            const float left0 = __shfl_up_sync(0xffffffffu, mid.w, 1);
+            const float right3 = __shfl_down_sync(0xffffffffu, mid.x, 1);
+            const bool rfix = gr <= 0 || gr >= M + 1;
+            float4 v;
+            v.x = (rfix || cfix[0]) ? mid.x : update<float, ORDER>(top.x, left0, mid.y, x.x, mid.x, gr - 1);
+            v.y = (rfix || cfix[1]) ? mid.y : update<float, ORDER>(top.y, mid.x, mid.z, x.y, mid.y, gr - 1);
+            v.z = (rfix || cfix[2]) ? mid.z : update<float, ORDER>(top.z, mid.y, mid.w, x.z, mid.z, gr - 1);
+            v.w = (rfix || cfix[3]) ? mid.w : update<float, ORDER>(top.w, mid.z, right3, x.w, mid.w, gr - 1);
+            p2[l] = mid;
+            p1[l] = x;
+            x = v;
+        }
+        // x: level T, row i - T
+        const int64_t ro = i - T;
+        if (ro >= out_r0 && ro < out_r1) {
+            float *row = dst + ro * ld + cl;
+            if (cstore[0]) row[0] = x.x;
+            if (cstore[1]) row[1] = x.y;
+            if (cstore[2]) row[2] = x.z;
+            if (cstore[3]) row[3] = x.w;
         }
     }
+}
+
+template <int T>
+void launch_rs(const float *src, float *dst, int64_t M, int64_t N, int order, cudaStream_t st) {
+    const int strips = (int)ceil_div(N, RS_W - 2 * T);
+    const int segs = (int)ceil_div(M, RS_SEG);
+    const unsigned blocks = (unsigned)ceil_div((int64_t)strips * segs, RS_NT / 32);
+    if (order == 0) stencil_rs_kernel<T, 0><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
+    else if (order == 1) stencil_rs_kernel<T, 1><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
+    else stencil_rs_kernel<T, 2><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
 }
 
 template <typename T>
@@ -207,8 +209,8 @@ gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *
     GB_CHECK_ARG(A && B && A != B, "stencil2d: A and B must be distinct device buffers");
     // tile and temporal depth: FP32 is HBM-bound (block 8 sweeps); FP64 is
     // bound by the FP64 pipe, where recomputing halos only costs, so t = 1.
-    const char *v4env = getenv("GB_STENCIL_V4");
-    const bool v4 = sizeof(T) == 4 && !(v4env && v4env[0] == '0');
+    const char *rsenv = getenv("GB_STENCIL_RS");   // "0": the shared-memory kernel (measurement)
+    const bool rs = sizeof(T) == 4 && !(rsenv && rsenv[0] == '0');
     const int tmax = sizeof(T) == 4 ? 8 : 1;
     const int TH = sizeof(T) == 4 ? 64 : 32, TW = sizeof(T) == 4 ? 128 : 64;
     // launches L with L == iters (mod 2) so the result lands in B for odd
@@ -225,27 +227,20 @@ gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *
         if (rem) t += 1;
         const T *src = (l % 2 == 0) ? A : B;
         T *dst = (l % 2 == 0) ? B : A;
-        if (v4) {
-            const size_t sm4 = 2 * (size_t)(V4_TH + 2 * t) * V4_P * sizeof(float);
-            dim3 g4((unsigned)ceil_div(N, V4_P - 2 * t), (unsigned)ceil_div(M, V4_TH));
-            GB_CHECK_ARG(g4.y <= 65535u, "stencil2d: M too large");
+        if (rs) {
             const float *s4 = (const float *)src;
             float *d4 = (float *)dst;
-            switch (order) {
-                case 0:
-                    cudaFuncSetAttribute(stencil_v4_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
-                    stencil_v4_kernel<0><<<g4, NT, sm4, st>>>(s4, d4, M, N, t);
-                    break;
-                case 1:
-                    cudaFuncSetAttribute(stencil_v4_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
-                    stencil_v4_kernel<1><<<g4, NT, sm4, st>>>(s4, d4, M, N, t);
-                    break;
-                default:
-                    cudaFuncSetAttribute(stencil_v4_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm4);
-                    stencil_v4_kernel<2><<<g4, NT, sm4, st>>>(s4, d4, M, N, t);
-                    break;
+            switch (t) {
+                case 1: launch_rs<1>(s4, d4, M, N, order, st); break;
+                case 2: launch_rs<2>(s4, d4, M, N, order, st); break;
+                case 3: launch_rs<3>(s4, d4, M, N, order, st); break;
+                case 4: launch_rs<4>(s4, d4, M, N, order, st); break;
+                case 5: launch_rs<5>(s4, d4, M, N, order, st); break;
+                case 6: launch_rs<6>(s4, d4, M, N, order, st); break;
+                case 7: launch_rs<7>(s4, d4, M, N, order, st); break;
+                default: launch_rs<8>(s4, d4, M, N, order, st); break;
             }
-            GB_LAUNCH_CHECK("stencil_v4_kernel");
+            GB_LAUNCH_CHECK("stencil_rs_kernel");
             done += t;
             continue;
         }
