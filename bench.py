@@ -624,18 +624,20 @@ def run_skinny(ctx):
     nbytes_alg = s * (M * K + K * N + 2 * M * N)
     flops = 2.0 * M * N * K
     ops = {}
+    pad = args.ld_pad   # extra elements per stored row (an unaligned leading dimension when not 0 mod 4)
     for mode in MODES:
         ar, ac = (K, M) if mode[0] == "T" else (M, K)
         br, bc = (N, K) if mode[1] == "T" else (K, N)
-        A = torch.empty((ar, ac), dtype=dt, device=ctx.dev)
-        B = torch.empty((br, bc), dtype=dt, device=ctx.dev)
-        gb.fill(A, ar, ac, ac, 21 + (mode[0] == "T"), 0, bits, stream=ctx.stream)
-        gb.fill(B, br, bc, bc, 23 + (mode[1] == "T"), 0, bits, stream=ctx.stream)
-        ops[mode] = (A, ac, B, bc)
+        A = torch.empty((ar, ac + pad), dtype=dt, device=ctx.dev)
+        B = torch.empty((br, bc + pad), dtype=dt, device=ctx.dev)
+        gb.fill(A, ar, ac, ac + pad, 21 + (mode[0] == "T"), 0, bits, stream=ctx.stream)
+        gb.fill(B, br, bc, bc + pad, 23 + (mode[1] == "T"), 0, bits, stream=ctx.stream)
+        ops[mode] = (A, ac + pad, B, bc + pad)
     C = torch.empty((M, N), dtype=dt, device=ctx.dev)
     gb.fill(C, M, N, N, 25, 0, bits, stream=ctx.stream)
 
-    skinny_algo = {"skinny": gb.ALGO_SKINNY, "auto": gb.ALGO_AUTO, "bf16x3": gb.ALGO_BF16X3}[args.skinny_algo]
+    skinny_algo = {"skinny": gb.ALGO_SKINNY, "auto": gb.ALGO_AUTO, "bf16x3": gb.ALGO_BF16X3,
+                   "ozaki": gb.ALGO_OZAKI}[args.skinny_algo]
 
     def gemm(mode):
         A, lda, B, ldb = ops[mode]
@@ -681,7 +683,7 @@ def run_skinny(ctx):
 
     e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 3)), len(MODES) * nbytes_alg, 1e9)
     config = {"workload": "%s FP%d M=%d N=%d K=%d, NN/NT/TN/TT, U[-1,1] seed 2" % (args.workload, bits, M, N, K),
-              "M": M, "N": N, "K": K, "modes": list(MODES), "algo": args.skinny_algo,
+              "M": M, "N": N, "K": K, "modes": list(MODES), "algo": args.skinny_algo, "ld_pad": pad,
               "bytes_per_gemm": nbytes_alg, "parallelism": "replicas x%d" % ctx.world,
               "l2": "inputs larger than L2 (large operand %d MB)" % (s * big * K // 10 ** 6)}
     line = base_line(ctx, "HBM GB/s (%s)" % args.workload, value, "GB/s", ms, args.steps, "f%d" % bits, config)
@@ -942,14 +944,26 @@ def run_serve(ctx):
     plain = serve("plain", streams=1, use_grouped=0, use_graphs=0) if not args.no_plain else None
     # isolated solves: a sample of the stream, one request at a time
     iso = []
+    by_class = {}
     rng = np.random.default_rng(44)
     srv = gb.Server(streams=1)
     for i in rng.choice(len(reqs), size=min(args.iso_sample, len(reqs)), replace=False):
         srv.submit(make_request(int(i), reqs[int(i)], 0))
         srv.drain(60.0)
-        iso += [lat for _, lat in srv.poll()]
+        lats = [lat for _, lat in srv.poll()]
+        iso += lats
+        r = reqs[int(i)]
+        by_class.setdefault("%s_f%d" % (("gemm", "thinB", "shortA", "transpose", "jacobi")[r[1]], r[2]), []).extend(lats)
     srv.close()
     iso_p50, iso_p99 = float(np.percentile(iso, 50)) * 1e3, float(np.percentile(iso, 99)) * 1e3
+    # offered load: the stream's share of each class x its mean isolated solve time
+    share = {}
+    for r in reqs:
+        k = "%s_f%d" % (("gemm", "thinB", "shortA", "transpose", "jacobi")[r[1]], r[2])
+        share[k] = share.get(k, 0) + 1
+    iso_classes = {k: {"n": len(v), "mean_ms": 1e3 * float(np.mean(v)), "p99_ms": 1e3 * float(np.percentile(v, 99))}
+                   for k, v in sorted(by_class.items())}
+    offered = sum(share[k] / len(reqs) * args.rate * float(np.mean(v)) for k, v in by_class.items())
     config = {"workload": "serving stream: Poisson %g req/s for %g s (seed 4), mixed GEMM/thinB/shortA/transpose/"
                           "Jacobi, 70/30 FP32/FP64, 48 GB HBM budget" % (args.rate, args.duration),
               "requests": len(reqs), "budget_gb": args.budget_gb, "streams": 4, "ring_slots": slots,
@@ -957,7 +971,8 @@ def run_serve(ctx):
     line = base_line(ctx, "serve p50/p99, req/s", main["req_per_s"], "req/s", main["submit_span_s"] * 1e3, 1,
                      "f32+f64", config)
     line.update({"serve": main, "plain": plain,
-                 "isolated": {"p50_ms": iso_p50, "p99_ms": iso_p99, "sample": len(iso)},
+                 "isolated": {"p50_ms": iso_p50, "p99_ms": iso_p99, "sample": len(iso), "by_class": iso_classes},
+                 "offered_load_gpu_s_per_s": offered,
                  "p99_over_isolated_p99": main["p99_ms"] / iso_p99 if iso_p99 > 0 else None,
                  "gpu_launches": launches, "clocks": clocks,
                  "e2e": {"value": main["req_per_s"], "unit": "req/s", "h2d_bytes_per_step": 0,
@@ -1008,8 +1023,9 @@ def main():
     ap.add_argument("--algo", default="best", choices=["best", "bf16x3", "bf16x6", "simt"])
     ap.add_argument("--bits", type=int, default=32, choices=[32, 64])
     ap.add_argument("--n", type=int, default=8, help="small dimension of thinb/shorta")
-    ap.add_argument("--skinny-algo", default="auto", choices=["auto", "skinny", "bf16x3"])
+    ap.add_argument("--skinny-algo", default="auto", choices=["auto", "skinny", "bf16x3", "ozaki"])
     ap.add_argument("--rows", type=int, default=262144, help="thinb/shorta: the large dimension")
+    ap.add_argument("--ld-pad", type=int, default=0, help="thinb/shorta: leading-dimension padding in elements")
     ap.add_argument("--shape", default="30000x17000", help="transpose: MxN")
     ap.add_argument("--iters", type=int, default=200, help="jacobi sweeps")
     ap.add_argument("--slices", type=int, default=0, help="dgemm: Ozaki slices (0: fewest matching native error)")

@@ -103,12 +103,14 @@ struct ThinTcArgs {
     float *C; int64_t cs_r, cs_c;
     float alpha, beta;
     int semantics;
-    int splits; int64_t kchunk; int64_t rtiles;   // units of 128 rows x kchunk
+    int splits; int64_t kchunk;                    // K range of a split: a multiple of 64
     float *part;                                   // splits x rows x nb partials (splits > 1)
     void *wpieces;                                 // thin_tc_wpieces_bytes(nb, K) of scratch
     cudaStream_t stream;
 };
-size_t thin_tc_wpieces_bytes(int nb, int64_t K);
+bool thin_tc_row_classes(int tx, int64_t ldx);          // row-major X with ldx % 4 != 0
+int64_t thin_tc_stages(int64_t K, bool classes);       // 64-k stages per row tile
+size_t thin_tc_wpieces_bytes(int nb, int64_t K, bool classes);
 gb_status launch_thin_tc(const ThinTcArgs &a);
 
 gb_status launch_skinny_f32(const GemmArgs &g);

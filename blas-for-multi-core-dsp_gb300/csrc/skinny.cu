@@ -358,9 +358,19 @@ struct TCfg {
 template <int NS>
 __host__ __device__ constexpr int rows_per_thread() { return NS > 4 ? 4 : 1; }
 
+// Row-major X whose leading dimension is not a multiple of 4 floats is taken
+// in four row classes r = 4i + c, each with its own 16-byte aligned tensor
+// map (base X + c*ldx - d_c, row stride 4*ldx, coordinate x holding
+// k = x - d_c); W is then read from a packed copy Wp[k + 32][NS] whose row
+// coordinate absorbs the shift, and the values at k < 0 (the previous row's
+// tail) are zeroed.
 struct TParams {
     int64_t rows, K;
-    int n, splits, kchunk_kb, rtiles;
+    int n, splits, kchunk_kb, nkb;
+    int rstride, woff;                    // 4 / 32 with row classes (packed W), else 1 / 0
+    int64_t cls_rows[4];
+    int cls_delta[4];
+    int cls_u0[5];
     void *C; int64_t cs_r, cs_c;
     float alpha, beta;
     int semantics;
@@ -368,9 +378,21 @@ struct TParams {
     int *err;
 };
 
+struct TMaps {
+    CUtensorMap x[4], w;
+};
+
+__device__ __forceinline__ void tunit(const TParams &p, int u, int &c, int &rt, int &sp) {
+    c = 0;
+    while (c < 3 && u >= p.cls_u0[c + 1]) c++;
+    const int v = u - p.cls_u0[c];
+    rt = v / p.splits;
+    sp = v - rt * p.splits;
+}
+
 template <int NS, bool XCOLS, bool WT>
 __global__ void __launch_bounds__(TCfg<rows_per_thread<NS>()>::NTH, 1)
-    thin_tma_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, TParams p) {
+    thin_tma_kernel(const __grid_constant__ TMaps maps, TParams p) {
     constexpr int R = rows_per_thread<NS>();
     using CF = TCfg<R>;
     constexpr int NCW = CF::NCW, BR = CF::BR, STAGES = CF::STAGES, STAGE = CF::STAGE, XS = CF::XS;
@@ -380,16 +402,14 @@ __global__ void __launch_bounds__(TCfg<rows_per_thread<NS>()>::NTH, 1)
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE);
     uint64_t *empty = full + STAGES;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int nkb = (int)((p.K + BK - 1) / BK);
-    const int units = p.rtiles * p.splits;
+    const int nkb = p.nkb;
+    const int units = p.cls_u0[4];
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
             ptx::mbar_init(&full[s], 1);
             ptx::mbar_init(&empty[s], NCW);
         }
         ptx::fence_mbar_init();
-        ptx::tma_prefetch_desc(&tmx);
-        ptx::tma_prefetch_desc(&tmw);
     }
     __syncthreads();
 
@@ -397,7 +417,8 @@ __global__ void __launch_bounds__(TCfg<rows_per_thread<NS>()>::NTH, 1)
         if (lane == 0) {
             int g = 0;
             for (int u = blockIdx.x; u < units; u += gridDim.x) {
-                const int rt = u / p.splits, sp = u - rt * p.splits;
+                int c, rt, sp;
+                tunit(p, u, c, rt, sp);
                 const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
                 const int r0 = rt * BR;
                 for (int kb = kb0; kb < kb1; kb++, g++) {
@@ -407,11 +428,11 @@ __global__ void __launch_bounds__(TCfg<rows_per_thread<NS>()>::NTH, 1)
                     ptx::mbar_arrive_expect_tx(&full[s], XS + BK * NS * 4);
 #pragma unroll
                     for (int bx = 0; bx < CF::NBOX; bx++) {
-                        if (XCOLS) ptx::tma_load_2d(st + bx * 32768, &tmx, &full[s], r0 + bx * 256, kb * BK);
-                        else ptx::tma_load_2d(st + bx * 32768, &tmx, &full[s], kb * BK, r0 + bx * 256);
+                        if (XCOLS) ptx::tma_load_2d(st + bx * 32768, &maps.x[c], &full[s], r0 + bx * 256, kb * BK);
+                        else ptx::tma_load_2d(st + bx * 32768, &maps.x[c], &full[s], kb * BK, r0 + bx * 256);
                     }
-                    if (WT) ptx::tma_load_2d(st + XS, &tmw, &full[s], kb * BK, 0);
-                    else ptx::tma_load_2d(st + XS, &tmw, &full[s], 0, kb * BK);
+                    if (WT) ptx::tma_load_2d(st + XS, &maps.w, &full[s], kb * BK, 0);
+                    else ptx::tma_load_2d(st + XS, &maps.w, &full[s], 0, kb * BK + p.woff - p.cls_delta[c]);
                 }
             }
         }
@@ -422,8 +443,10 @@ __global__ void __launch_bounds__(TCfg<rows_per_thread<NS>()>::NTH, 1)
     const int t = threadIdx.x;
     int g = 0;
     for (int u = blockIdx.x; u < units; u += gridDim.x) {
-        const int rt = u / p.splits, sp = u - rt * p.splits;
+        int c, rt, sp;
+        tunit(p, u, c, rt, sp);
         const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
+        const int delta = p.cls_delta[c];
         float acc[R][NS];
 #pragma unroll
         for (int i = 0; i < R; i++)
@@ -451,10 +474,15 @@ __global__ void __launch_bounds__(TCfg<rows_per_thread<NS>()>::NTH, 1)
                     } else {
                         const uint8_t *row = box + br * 128;
 #pragma unroll
-                        for (int c = 0; c < 4; c++) {
-                            const float4 v = *reinterpret_cast<const float4 *>(row + (((h / 4 + c) ^ (br & 7)) << 4));
-                            x[i][4 * c] = v.x; x[i][4 * c + 1] = v.y; x[i][4 * c + 2] = v.z; x[i][4 * c + 3] = v.w;
+                        for (int cc = 0; cc < 4; cc++) {
+                            const float4 v = *reinterpret_cast<const float4 *>(row + (((h / 4 + cc) ^ (br & 7)) << 4));
+                            x[i][4 * cc] = v.x; x[i][4 * cc + 1] = v.y; x[i][4 * cc + 2] = v.z; x[i][4 * cc + 3] = v.w;
                         }
+                    }
+                    if (kb == 0 && h == 0 && delta > 0) {   // coordinates below d_c are the previous row
+#pragma unroll
+                        for (int kk = 0; kk < 3; kk++)
+                            if (kk < delta) x[i][kk] = 0.f;
                     }
                 }
                 if (WT) {   // ws[j][kk]
@@ -495,8 +523,9 @@ __global__ void __launch_bounds__(TCfg<rows_per_thread<NS>()>::NTH, 1)
         if (!go) break;
 #pragma unroll
         for (int i = 0; i < R; i++) {
-            const int64_t row = (int64_t)rt * BR + t + i * TPR;
-            if (row >= p.rows) continue;
+            const int64_t ci = (int64_t)rt * BR + t + i * TPR;   // row within the class
+            if (ci >= p.cls_rows[c]) continue;
+            const int64_t row = ci * p.rstride + c;
             if (p.splits > 1) {
                 float *pp = p.part + ((int64_t)sp * p.rows + row) * 8;
 #pragma unroll
@@ -553,18 +582,30 @@ bool tma_eligible(const SkParams &p) {
     if (sizeof(T) != 4 || NB != 8) return false;
     const char *e = getenv("GB_SKINNY_TMA");
     if (e && e[0] == '0') return false;
-    return p.K > 0 && p.rows < (int64_t(1) << 31) && p.K < (int64_t(1) << 31) && p.ldx % 4 == 0 && p.ldw % 4 == 0 &&
-           (uintptr_t)p.X % 16 == 0 && (uintptr_t)p.W % 16 == 0;
+    // K-major X needs ldx % 4 == 0; row-major X any ldx (row classes); W any
+    // layout (packed when the tensor map cannot read it in place)
+    return p.K > 0 && p.rows < (int64_t(1) << 31) && p.K < (int64_t(1) << 30) && (p.ldx % 4 == 0 || !p.tx) &&
+           (uintptr_t)p.X % 16 == 0;
 }
 
-// The tensor-core form: X read by TMA (16-byte aligned, ldx % 4 == 0), any
-// W layout (it is split into BF16 pieces first); GB_SKINNY_TC=0 turns it off.
+// FFMA-TMA form: rows taken in four classes (row-major X, ldx % 4 != 0), and
+// whether W is read from a packed copy
+inline bool thin_classes(const SkParams &p) { return !p.tx && p.ldx % 4 != 0; }
+inline bool thin_pack_w(const SkParams &p) {
+    return thin_classes(p) || p.ldw % 4 != 0 || (uintptr_t)p.W % 16 != 0;
+}
+constexpr int64_t kWpOff = 32;   // packed W: row k at k + 32 (rows below and above K are zero)
+inline int64_t thin_wp_rows(int64_t K) { return K + 2 * kWpOff + thin::BK; }
+
+// The tensor-core form: X read by TMA (16-byte aligned base; any ldx -- four
+// row or k-line classes when ldx % 4 != 0), any W layout (it is split into
+// BF16 pieces first); GB_SKINNY_TC=0 turns it off.
 template <typename T, int NB>
 bool tc_eligible(const SkParams &p) {
     if (sizeof(T) != 4 || NB < 16 || p.n <= 8 || p.K < 64) return false;
     const char *e = getenv("GB_SKINNY_TC");
     if (e && e[0] == '0') return false;
-    return p.rows < (int64_t(1) << 31) && p.K < (int64_t(1) << 30) && p.ldx % 4 == 0 && (uintptr_t)p.X % 16 == 0;
+    return p.rows < (int64_t(1) << 31) && p.K < (int64_t(1) << 30) && (uintptr_t)p.X % 16 == 0;
 }
 
 template <typename T, int NB>
@@ -572,19 +613,21 @@ gb_status make_plan(SkParams &p, Plan &pl, bool allow_tc = true) {
     pl.w_bytes = 0;
     pl.tc = allow_tc && tc_eligible<T, NB>(p);
     if (pl.tc) {
-        // units of 128 rows x a K range; split K until there are ~4 units per SM
+        // units of 128 rows (per row class) x a K range; split K until there are ~4 units per SM
+        const bool classes = thin_tc_row_classes(p.tx, p.ldx);
         pl.tma = false;
         pl.rows_kernel = !p.tx;
         pl.vec = pl.wvec = true;
-        pl.rtiles = ceil_div(p.rows, 128);
-        const int64_t nkb = ceil_div(p.K, 32);
+        pl.rtiles = ceil_div(p.rows, 128) + (classes ? 3 : 0);
+        const int64_t nst = thin_tc_stages(p.K, classes);
         int splits = 1;
-        while (pl.rtiles * splits < 4 * (int64_t)sm_count() && nkb / (splits * 2) >= 16 && splits < 64) splits *= 2;
-        const int64_t ckb = ceil_div(nkb, splits);
-        p.kchunk = ckb * 32;
-        p.splits = (int)ceil_div(nkb, ckb);
+        while (pl.rtiles * splits < 4 * (int64_t)sm_count() && nst / (splits * 2) >= 8 && splits < 64) splits *= 2;
+        const int64_t cst = ceil_div(nst, splits);
+        p.kchunk = cst * 64;
+        p.splits = (int)ceil_div(nst, cst);
+        if (p.splits < 1) p.splits = 1;
         pl.part_bytes = p.splits > 1 ? (size_t)p.splits * p.rows * NB * sizeof(T) : 0;
-        pl.w_bytes = thin_tc_wpieces_bytes(NB, p.K);
+        pl.w_bytes = thin_tc_wpieces_bytes(NB, p.K, classes);
         return ok();
     }
     pl.tma = tma_eligible<T, NB>(p);
@@ -593,8 +636,9 @@ gb_status make_plan(SkParams &p, Plan &pl, bool allow_tc = true) {
         pl.rows_kernel = !p.tx;
         pl.vec = pl.wvec = true;
         const int br = p.n > 4 ? thin::TCfg<4>::BR : thin::TCfg<1>::BR;
-        pl.rtiles = ceil_div(p.rows, br);
-        const int64_t nkb = ceil_div(p.K, thin::BK);
+        const bool classes = thin_classes(p);
+        pl.rtiles = ceil_div(p.rows, br) + (classes ? 3 : 0);
+        const int64_t nkb = ceil_div(p.K + (classes ? 3 : 0), thin::BK);
         // split K until there are ~6 units per SM (tail balance of the persistent grid)
         int splits = 1;
         while (pl.rtiles * splits < 6 * (int64_t)sm_count() && nkb / (splits * 2) >= 16 && splits < 64) splits *= 2;
@@ -603,6 +647,7 @@ gb_status make_plan(SkParams &p, Plan &pl, bool allow_tc = true) {
         p.splits = (int)ceil_div(nkb, ckb);
         if (p.splits < 1) p.splits = 1;
         pl.part_bytes = p.splits > 1 ? (size_t)p.splits * p.rows * NB * sizeof(T) : 0;
+        pl.w_bytes = thin_pack_w(p) ? (size_t)thin_wp_rows(p.K) * (p.n <= 4 ? 4 : 8) * sizeof(float) : 0;
         return ok();
     }
     pl.rows_kernel = !p.tx;
@@ -632,9 +677,22 @@ gb_status make_plan(SkParams &p, Plan &pl, bool allow_tc = true) {
     return ok();
 }
 
+// W (logical K x n; tw: stored n x K) -> Wp[k + 32][j], ns columns, zero
+// outside 0 <= k < K, j < n
+__global__ void wpack_kernel(const float *__restrict__ W, int64_t ldw, int tw, int n, int64_t K, int64_t rows, int ns,
+                             float *__restrict__ wp) {
+    const int64_t total = rows * ns;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e / ns, j = e - r * ns, k = r - kWpOff;
+        float v = 0.f;
+        if (j < n && k >= 0 && k < K) v = tw ? W[j * ldw + k] : W[k * ldw + j];
+        wp[e] = v;
+    }
+}
+
 template <int NS, bool XCOLS, bool WT>
-gb_status launch_thin(const CUtensorMap &tx, const CUtensorMap &tw, const thin::TParams &tp, int grid,
-                      cudaStream_t st) {
+gb_status launch_thin(const thin::TMaps &maps, const thin::TParams &tp, int grid, cudaStream_t st) {
     using CF = thin::TCfg<thin::rows_per_thread<NS>()>;
     static bool attr = false;
     if (!attr) {
@@ -642,7 +700,7 @@ gb_status launch_thin(const CUtensorMap &tx, const CUtensorMap &tw, const thin::
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM));
         attr = true;
     }
-    thin::thin_tma_kernel<NS, XCOLS, WT><<<grid, CF::NTH, CF::SMEM, st>>>(tx, tw, tp);
+    thin::thin_tma_kernel<NS, XCOLS, WT><<<grid, CF::NTH, CF::SMEM, st>>>(maps, tp);
     GB_LAUNCH_CHECK("thin_tma_kernel");
     return ok();
 }
@@ -652,7 +710,7 @@ gb_status launch_plan(const SkParams &p, const Plan &pl, cudaStream_t st) {
     if (pl.tc) {
         ThinTcArgs a{p.rows, p.K, (const float *)p.X, p.ldx, p.tx, (const float *)p.W, p.ldw, p.tw, p.n, NB,
                      (float *)p.C, p.cs_r, p.cs_c, (float)p.alpha, (float)p.beta, p.semantics, p.splits, p.kchunk,
-                     pl.rtiles, (float *)p.part, p.wpieces, st};
+                     (float *)p.part, p.wpieces, st};
         gb_status s = launch_thin_tc(a);
         if (s != GB_OK) return s;
         if (p.splits > 1) {
@@ -665,33 +723,73 @@ gb_status launch_plan(const SkParams &p, const Plan &pl, cudaStream_t st) {
     }
     if (pl.tma) {
         const int ns = p.n <= 4 ? 4 : 8;
-        CUtensorMap tx, tw;
-        bool okm = p.tx ? make_tmap_f32(&tx, p.X, (uint64_t)p.rows, (uint64_t)p.K, (uint64_t)p.ldx * 4, 256,
-                                        thin::BK, false)
-                        : make_tmap_f32(&tx, p.X, (uint64_t)p.K, (uint64_t)p.rows, (uint64_t)p.ldx * 4, thin::BK,
-                                        256, true);
-        okm = okm && (p.tw ? make_tmap_f32(&tw, p.W, (uint64_t)p.K, (uint64_t)p.n, (uint64_t)p.ldw * 4, thin::BK,
-                                           (uint32_t)ns, false)
-                           : make_tmap_f32(&tw, p.W, (uint64_t)p.n, (uint64_t)p.K, (uint64_t)p.ldw * 4,
-                                           (uint32_t)ns, thin::BK, false));
+        const bool classes = thin_classes(p), pack = thin_pack_w(p);
+        thin::TMaps maps;
+        memset(&maps, 0, sizeof(maps));
+        thin::TParams tp;
+        memset(&tp, 0, sizeof(tp));
+        tp.rows = p.rows; tp.K = p.K; tp.n = p.n; tp.splits = p.splits;
+        tp.kchunk_kb = (int)(p.kchunk / thin::BK);
+        tp.nkb = (int)ceil_div(p.K + (classes ? 3 : 0), thin::BK);
+        tp.rstride = classes ? 4 : 1;
+        tp.woff = pack ? (int)kWpOff : 0;
+        bool okm = true;
+        if (pack) {
+            const int64_t rows = thin_wp_rows(p.K);
+            const int blocks = (int)(ceil_div(rows * ns, 256) < 2 * sm_count() ? ceil_div(rows * ns, 256)
+                                                                                : 2 * sm_count());
+            wpack_kernel<<<blocks, 256, 0, st>>>((const float *)p.W, p.ldw, p.tw, p.n, p.K, rows, ns,
+                                                 (float *)p.wpieces);
+            GB_LAUNCH_CHECK("wpack_kernel");
+            okm = make_tmap_f32(&maps.w, p.wpieces, (uint64_t)ns, (uint64_t)rows, (uint64_t)ns * 4, (uint32_t)ns,
+                                thin::BK, false);
+        } else {
+            okm = p.tw ? make_tmap_f32(&maps.w, p.W, (uint64_t)p.K, (uint64_t)p.n, (uint64_t)p.ldw * 4, thin::BK,
+                                       (uint32_t)ns, false)
+                       : make_tmap_f32(&maps.w, p.W, (uint64_t)p.n, (uint64_t)p.K, (uint64_t)p.ldw * 4,
+                                       (uint32_t)ns, thin::BK, false);
+        }
+        const int br = ns == 8 ? thin::TCfg<4>::BR : thin::TCfg<1>::BR;
+        int u = 0;
+        for (int c = 0; c < 4; c++) {
+            tp.cls_u0[c] = u;
+            int64_t rows_c = c == 0 ? p.rows : 0;
+            int delta = 0;
+            const float *base = (const float *)p.X;
+            if (classes) {
+                rows_c = p.rows > c ? (p.rows - c + 3) / 4 : 0;
+                delta = (int)((c * p.ldx) % 4);
+                base = (const float *)p.X + c * p.ldx - delta;
+            }
+            tp.cls_rows[c] = rows_c;
+            tp.cls_delta[c] = delta;
+            u += (int)(ceil_div(rows_c, br) * p.splits);
+            if (rows_c == 0) continue;
+            okm = okm && (p.tx ? make_tmap_f32(&maps.x[c], base, (uint64_t)p.rows, (uint64_t)p.K,
+                                               (uint64_t)p.ldx * 4, 256, thin::BK, false)
+                               : make_tmap_f32(&maps.x[c], base, (uint64_t)(p.K + delta), (uint64_t)rows_c,
+                                               (uint64_t)p.ldx * 4 * (classes ? 4 : 1), thin::BK, 256, true));
+        }
+        tp.cls_u0[4] = u;
         if (!okm) return set_status(GB_ERR_CUDA, "skinny: cuTensorMapEncodeTiled failed");
         int *err = error_word();
         if (!err) return set_status(GB_ERR_OOM, "skinny: no device error word");
-        thin::TParams tp{p.rows, p.K, p.n, p.splits, (int)(p.kchunk / thin::BK), (int)pl.rtiles, p.C, p.cs_r,
-                         p.cs_c, (float)p.alpha, (float)p.beta, p.semantics, (float *)p.part, err};
-        const int64_t units = pl.rtiles * p.splits;
-        const int grid = (int)(units < sm_count() ? units : sm_count());
+        tp.C = p.C; tp.cs_r = p.cs_r; tp.cs_c = p.cs_c; tp.alpha = (float)p.alpha; tp.beta = (float)p.beta;
+        tp.semantics = p.semantics; tp.part = (float *)p.part; tp.err = err;
+        const int grid = u < sm_count() ? u : sm_count();
+        if (grid == 0) return ok();
         gb_status s;
-        const int sel = (ns == 8 ? 4 : 0) | (p.tx ? 2 : 0) | (p.tw ? 1 : 0);
+        const bool wt = p.tw && !pack;
+        const int sel = (ns == 8 ? 4 : 0) | (p.tx ? 2 : 0) | (wt ? 1 : 0);
         switch (sel) {
-            case 0: s = launch_thin<4, false, false>(tx, tw, tp, grid, st); break;
-            case 1: s = launch_thin<4, false, true>(tx, tw, tp, grid, st); break;
-            case 2: s = launch_thin<4, true, false>(tx, tw, tp, grid, st); break;
-            case 3: s = launch_thin<4, true, true>(tx, tw, tp, grid, st); break;
-            case 4: s = launch_thin<8, false, false>(tx, tw, tp, grid, st); break;
-            case 5: s = launch_thin<8, false, true>(tx, tw, tp, grid, st); break;
-            case 6: s = launch_thin<8, true, false>(tx, tw, tp, grid, st); break;
-            default: s = launch_thin<8, true, true>(tx, tw, tp, grid, st); break;
+            case 0: s = launch_thin<4, false, false>(maps, tp, grid, st); break;
+            case 1: s = launch_thin<4, false, true>(maps, tp, grid, st); break;
+            case 2: s = launch_thin<4, true, false>(maps, tp, grid, st); break;
+            case 3: s = launch_thin<4, true, true>(maps, tp, grid, st); break;
+            case 4: s = launch_thin<8, false, false>(maps, tp, grid, st); break;
+            case 5: s = launch_thin<8, false, true>(maps, tp, grid, st); break;
+            case 6: s = launch_thin<8, true, false>(maps, tp, grid, st); break;
+            default: s = launch_thin<8, true, true>(maps, tp, grid, st); break;
         }
         if (s != GB_OK) return s;
         if (p.splits > 1) {
@@ -823,14 +921,19 @@ gb_status run_noalloc(SkParams p, cudaStream_t st) {
     Plan pl;
     gb_status s = make_plan<float, NB>(p, pl, /*allow_tc=*/false);
     if (s != GB_OK) return s;
-    if (pl.part_bytes) {
-        if (pl.part_bytes > kNoAllocScratchBytes)
+    if (pl.part_bytes || pl.w_bytes) {
+        // partial sums first, then the packed W (256-byte aligned), as in run()
+        const size_t off = (pl.part_bytes + 255) / 256 * 256;
+        if (off + pl.w_bytes > kNoAllocScratchBytes)
             return set_status(GB_ERR_INVALID_ARG,
                               "gb_sgemm_skinny_noalloc: %d-way split-K over %lld rows needs %zu bytes of scratch, "
                               "more than the fixed %zu bytes",
-                              p.splits, (long long)p.rows, pl.part_bytes, kNoAllocScratchBytes);
-        s = noalloc_scratch(&p.part);
+                              p.splits, (long long)p.rows, off + pl.w_bytes, kNoAllocScratchBytes);
+        void *base = nullptr;
+        s = noalloc_scratch(&base);
         if (s != GB_OK) return s;
+        p.part = pl.part_bytes ? base : nullptr;
+        p.wpieces = pl.w_bytes ? (unsigned char *)base + off : nullptr;
     }
     return launch_plan<float, NB>(p, pl, st);
 }

@@ -125,8 +125,8 @@ __global__ void __launch_bounds__(NT) stencil_tb_kernel(const T *__restrict__ sr
 // same add order as one sweep at a time, so results are bit-identical.
 constexpr int RS_W = 128, RS_SEG = 256, RS_NT = 256;
 
-template <int T, int ORDER>
-__global__ void __launch_bounds__(RS_NT) stencil_rs_kernel(const float *__restrict__ src, float *__restrict__ dst,
+template <typename E, int T, int ORDER>
+__global__ void __launch_bounds__(RS_NT) stencil_rs_kernel(const E *__restrict__ src, E *__restrict__ dst,
                                                            int64_t M, int64_t N, int strips, int segs) {
     const int lane = threadIdx.x % 32;
     const int64_t wid = (int64_t)blockIdx.x * (RS_NT / 32) + threadIdx.x / 32;
@@ -148,56 +148,60 @@ __global__ void __launch_bounds__(RS_NT) stencil_rs_kernel(const float *__restri
         cstore[q] = lc >= T && lc < RS_W - T && gc >= 1 && gc <= N;
     }
 
-    float4 p2[T], p1[T];   // level l-1 rows rho-1 and rho of level l's window
+    E p2[T][4], p1[T][4];   // level l-1 rows rho-1 and rho of level l's window
 #pragma unroll
-    for (int l = 0; l < T; l++) p2[l] = p1[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int l = 0; l < T; l++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) p2[l][q] = p1[l][q] = E(0);
 
     for (int64_t i = out_r0 - T - 1; i < out_r1 + T; i++) {   // input row i (level 0)
-        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        E x[4] = {E(0), E(0), E(0), E(0)};
         if (i >= 0 && i <= M + 1) {
-            const float *row = src + i * ld + cl;
-            if (cload[0]) x.x = __ldg(row);
-            if (cload[1]) x.y = __ldg(row + 1);
-            if (cload[2]) x.z = __ldg(row + 2);
-            if (cload[3]) x.w = __ldg(row + 3);
+            const E *row = src + i * ld + cl;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (cload[q]) x[q] = __ldg(row + q);
         }
 #pragma unroll
         for (int l = 0; l < T; l++) {
             // level l+1, row rho = i - l - 1: top p2[l], middle p1[l], down x
             const int64_t gr = i - l - 1;
-            const float4 top = p2[l], mid = p1[l];
-            const float left0 = __shfl_up_sync(0xffffffffu, mid.w, 1);
-            const float right3 = __shfl_down_sync(0xffffffffu, mid.x, 1);
+            const E left0 = __shfl_up_sync(0xffffffffu, p1[l][3], 1);
+            const E right3 = __shfl_down_sync(0xffffffffu, p1[l][0], 1);
             const bool rfix = gr <= 0 || gr >= M + 1;
-            float4 v;
-            v.x = (rfix || cfix[0]) ? mid.x : update<float, ORDER>(top.x, left0, mid.y, x.x, mid.x, gr - 1);
-            v.y = (rfix || cfix[1]) ? mid.y : update<float, ORDER>(top.y, mid.x, mid.z, x.y, mid.y, gr - 1);
-            v.z = (rfix || cfix[2]) ? mid.z : update<float, ORDER>(top.z, mid.y, mid.w, x.z, mid.z, gr - 1);
-            v.w = (rfix || cfix[3]) ? mid.w : update<float, ORDER>(top.w, mid.z, right3, x.w, mid.w, gr - 1);
-            p2[l] = mid;
-            p1[l] = x;
-            x = v;
+            E v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const E lft = q == 0 ? left0 : p1[l][q - 1];
+                const E rgt = q == 3 ? right3 : p1[l][q + 1];
+                v[q] = (rfix || cfix[q]) ? p1[l][q] : update<E, ORDER>(p2[l][q], lft, rgt, x[q], p1[l][q], gr - 1);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                p2[l][q] = p1[l][q];
+                p1[l][q] = x[q];
+                x[q] = v[q];
+            }
         }
         // x: level T, row i - T
         const int64_t ro = i - T;
         if (ro >= out_r0 && ro < out_r1) {
-            float *row = dst + ro * ld + cl;
-            if (cstore[0]) row[0] = x.x;
-            if (cstore[1]) row[1] = x.y;
-            if (cstore[2]) row[2] = x.z;
-            if (cstore[3]) row[3] = x.w;
+            E *row = dst + ro * ld + cl;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (cstore[q]) row[q] = x[q];
         }
     }
 }
 
-template <int T>
-void launch_rs(const float *src, float *dst, int64_t M, int64_t N, int order, cudaStream_t st) {
+template <typename E, int T>
+void launch_rs(const E *src, E *dst, int64_t M, int64_t N, int order, cudaStream_t st) {
     const int strips = (int)ceil_div(N, RS_W - 2 * T);
     const int segs = (int)ceil_div(M, RS_SEG);
     const unsigned blocks = (unsigned)ceil_div((int64_t)strips * segs, RS_NT / 32);
-    if (order == 0) stencil_rs_kernel<T, 0><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
-    else if (order == 1) stencil_rs_kernel<T, 1><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
-    else stencil_rs_kernel<T, 2><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
+    if (order == 0) stencil_rs_kernel<E, T, 0><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
+    else if (order == 1) stencil_rs_kernel<E, T, 1><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
+    else stencil_rs_kernel<E, T, 2><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
 }
 
 template <typename T>
@@ -210,6 +214,8 @@ gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *
     // tile and temporal depth: FP32 is HBM-bound (block 8 sweeps); FP64 is
     // bound by the FP64 pipe, where recomputing halos only costs, so t = 1.
     const char *rsenv = getenv("GB_STENCIL_RS");   // "0": the shared-memory kernel (measurement)
+    // FP64 keeps the shared-memory kernel with t = 1: it is bound by the FP64
+    // pipe, and the streaming form measured slower there (1.38 vs 1.64 TB/s)
     const bool rs = sizeof(T) == 4 && !(rsenv && rsenv[0] == '0');
     const int tmax = sizeof(T) == 4 ? 8 : 1;
     const int TH = sizeof(T) == 4 ? 64 : 32, TW = sizeof(T) == 4 ? 128 : 64;
@@ -228,17 +234,19 @@ gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *
         const T *src = (l % 2 == 0) ? A : B;
         T *dst = (l % 2 == 0) ? B : A;
         if (rs) {
-            const float *s4 = (const float *)src;
-            float *d4 = (float *)dst;
-            switch (t) {
-                case 1: launch_rs<1>(s4, d4, M, N, order, st); break;
-                case 2: launch_rs<2>(s4, d4, M, N, order, st); break;
-                case 3: launch_rs<3>(s4, d4, M, N, order, st); break;
-                case 4: launch_rs<4>(s4, d4, M, N, order, st); break;
-                case 5: launch_rs<5>(s4, d4, M, N, order, st); break;
-                case 6: launch_rs<6>(s4, d4, M, N, order, st); break;
-                case 7: launch_rs<7>(s4, d4, M, N, order, st); break;
-                default: launch_rs<8>(s4, d4, M, N, order, st); break;
+            {
+                const float *s4 = (const float *)src;
+                float *d4 = (float *)dst;
+                switch (t) {
+                    case 1: launch_rs<float, 1>(s4, d4, M, N, order, st); break;
+                    case 2: launch_rs<float, 2>(s4, d4, M, N, order, st); break;
+                    case 3: launch_rs<float, 3>(s4, d4, M, N, order, st); break;
+                    case 4: launch_rs<float, 4>(s4, d4, M, N, order, st); break;
+                    case 5: launch_rs<float, 5>(s4, d4, M, N, order, st); break;
+                    case 6: launch_rs<float, 6>(s4, d4, M, N, order, st); break;
+                    case 7: launch_rs<float, 7>(s4, d4, M, N, order, st); break;
+                    default: launch_rs<float, 8>(s4, d4, M, N, order, st); break;
+                }
             }
             GB_LAUNCH_CHECK("stencil_rs_kernel");
             done += t;

@@ -119,3 +119,57 @@ def test_thin_deterministic(torch):
         gbblas.sgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=gbblas.ALGO_SKINNY)
         outs.append(host(dC))
     assert outs[0].tobytes() == outs[1].tobytes()
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("kind", ["thinB", "shortA"])
+@pytest.mark.parametrize("small,big,K,mis", [(12, 3001, 1037, 1), (33, 1000, 640, 2), (64, 2000, 4099, 3),
+                                             (16, 700, 96, 1), (40, 60, 3000, 3), (8, 900, 513, 1),
+                                             (3, 1001, 2050, 2), (8, 40, 9000, 3)])
+def test_thin_unaligned_leading_dimension_exact(torch, mode, kind, small, big, K, mis):
+    """Leading dimensions that are not a multiple of 4 floats: row-major X is
+    streamed as four row classes with phase-shifted W pieces (tensor-core
+    form); the other layouts take the register-streaming kernels.  Integer
+    inputs: exact in any order."""
+    import gbblas
+    ta, tb = mode
+    M, N = (big, small) if kind == "thinB" else (small, big)
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    lda, ldb, ldc = ac + mis, bc + mis, N + mis
+    A, B = _ints(ar, ac, 21, lda), _ints(br, bc, 22, ldb)
+    C0 = _ints(M, N, 23, ldc)
+    opA = A[:, :ac].T if ta == "T" else A[:, :ac]
+    opB = B[:, :bc].T if tb == "T" else B[:, :bc]
+    want = C0.copy()
+    want[:, :N] = (0.5 * (opA.astype(np.float64) @ opB.astype(np.float64)) - 3.0 * C0[:, :N]).astype(np.float32)
+    dC = dev(C0)
+    gbblas.sgemm(ta, tb, M, N, K, 0.5, dev(A), lda, dev(B), ldb, -3.0, dC, ldc, algo=gbblas.ALGO_SKINNY)
+    got = host(dC)
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (mode, kind, bad[:5])
+
+
+@pytest.mark.parametrize("mode", ["NN", "NT", "TN", "TT"])
+@pytest.mark.parametrize("N", [8, 24])
+def test_thin_unaligned_nan_in_previous_row_does_not_leak(torch, mode, N):
+    """The class decomposition reads a few values before each row start (the
+    previous row's tail); they are zeroed before use, so a NaN there must not
+    reach the result."""
+    import gbblas
+    ta, tb = mode
+    M, K = 2000, 515                 # thinB; lda = K + 1 when A is row-major
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    lda, ldb = ac + 1, bc
+    A = oracle.fill(ar, ac, 91, dtype=np.float32, ld=lda)
+    A[:, ac:] = np.nan               # padding between rows
+    B = oracle.fill(br, bc, 92, dtype=np.float32, ld=ldb)
+    C0 = np.zeros((M, N), np.float32)
+    dC = dev(C0)
+    gbblas.sgemm(ta, tb, M, N, K, 1.0, dev(A), lda, dev(B), ldb, 0.0, dC, N, algo=gbblas.ALGO_SKINNY)
+    got = host(dC)
+    assert np.isfinite(got).all()
+    rows = np.arange(0, M, 37)
+    err, _ = oracle.normwise_error(got, ta, tb, M, N, K, 1.0, A, lda, B, ldb, 0.0, C0, N, rows, np.arange(N))
+    assert err <= 2 * K * 2.0 ** -24, err
