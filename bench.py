@@ -761,9 +761,14 @@ def run_jacobi(ctx):
     A0 = A.clone()
     B = A.clone()
     nbytes = 2.0 * M * N * s * iters
+    nine = args.points == 9
+    w9 = [0.05, 0.1, 0.05, 0.1, 0.4, 0.1, 0.05, 0.1, 0.05]   # a smoothing window
 
     def op():
-        gb.stencil2d(M, N, A, B, iters, gb.STENCIL_HOST, bits, stream=ctx.stream)
+        if nine:
+            gb.stencil9(M, N, A, B, iters, w9, bits, stream=ctx.stream)
+        else:
+            gb.stencil2d(M, N, A, B, iters, gb.STENCIL_HOST, bits, stream=ctx.stream)
 
     for _ in range(max(1, args.warmup)):
         op()
@@ -778,13 +783,14 @@ def run_jacobi(ctx):
 
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
     value = ctx.world * args.steps * nbytes / (ms * 1e-3) / 1e9
-    gflops = 5.0 * M * N * iters / (kms * 1e-3) / 1e12
+    gflops = (17.0 if nine else 5.0) * M * N * iters / (kms * 1e-3) / 1e12
     extra = {"kernel_ms": kms, "points_per_s": M * N * iters / (kms * 1e-3),
              "fp_tflops": gflops, "note": "achieved = algorithmic bytes (2*M*N*s per sweep) / time; temporal "
              "blocking lets it exceed the HBM peak (DRAM bytes in profiles/)"}
     if bits == 64:
         extra.update({"compute_bound": "fp64", "compute_peak_tflops": FP64_PEAK, "compute_frac": gflops / FP64_PEAK})
-    roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "jacobi_f%d_8192" % bits, extra)
+    roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "%s_f%d_8192" % ("stencil9" if nine else "jacobi", bits),
+                   extra)
     hA = A0.cpu().pin_memory()
     hR = torch.empty_like(A, device="cpu").pin_memory()
 
@@ -796,14 +802,17 @@ def run_jacobi(ctx):
         return 2 * A.numel() * s, A.numel() * s
 
     e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 3)), nbytes, 1e9)
-    config = {"workload": "Jacobi 8192^2 FP%d, %d sweeps, boundary 1.0, interior U[0,1] seed 2" % (bits, iters),
-              "M": M, "N": N, "iters": iters, "order": "host", "parallelism": "replicas x%d" % ctx.world,
+    config = {"workload": "%s 8192^2 FP%d, %d sweeps, boundary 1.0, interior U[0,1] seed 2"
+                          % ("9-point stencil (3x3 smoothing window)" if nine else "Jacobi", bits, iters),
+              "M": M, "N": N, "iters": iters, "order": "window, product + 8 fma" if nine else "host",
+              "parallelism": "replicas x%d" % ctx.world,
               "l2": "grid larger than L2"}
-    line = base_line(ctx, "HBM GB/s (jacobi)", value, "GB/s", ms, args.steps, "f%d" % bits, config)
+    line = base_line(ctx, "HBM GB/s (%s)" % ("stencil9" if nine else "jacobi"), value, "GB/s", ms, args.steps,
+                     "f%d" % bits, config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
                                            "d2h_bytes_per_step": d2h},
                  "gpu_launches": launches, "clocks": clocks})
-    if ctx.rank == 0 and not args.no_cpu_baseline:
+    if ctx.rank == 0 and not args.no_cpu_baseline and not nine:
         v, nt, desc = cpu_bw_sample("jacobi", bits)
         line["cpu_baseline"] = {"value": v, "unit": "GB/s", "cores": nt, "kind": "port", "sample": desc}
     ctx.finish(line)
@@ -1028,6 +1037,7 @@ def main():
     ap.add_argument("--ld-pad", type=int, default=0, help="thinb/shorta: leading-dimension padding in elements")
     ap.add_argument("--shape", default="30000x17000", help="transpose: MxN")
     ap.add_argument("--iters", type=int, default=200, help="jacobi sweeps")
+    ap.add_argument("--points", type=int, default=5, choices=[5, 9], help="jacobi: 5-point or 9-point stencil")
     ap.add_argument("--slices", type=int, default=0, help="dgemm: Ozaki slices (0: fewest matching native error)")
     ap.add_argument("--size", type=int, default=0, help="dgemm: M=N=K (default 8192)")
     ap.add_argument("--subgrid", type=int, default=1024, help="dgemm: error subgrid size")

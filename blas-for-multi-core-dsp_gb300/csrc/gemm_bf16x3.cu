@@ -257,7 +257,56 @@ struct EpiParams {
     int tiles_m, tiles_n;
     int *err;
     int chunk_kb;    // k-blocks per accumulator chunk (folding form)
+    // Stream-K tail: tiles [0, dp_tiles) go whole to CTAs in turn; the K
+    // iterations of tiles [dp_tiles, tiles) are split evenly over the grid, so
+    // a tile there may be computed in two parts (by CTAs b and b + 1): each
+    // part's raw accumulator goes to sk_part[2b + half], and the second CTA to
+    // finish (sk_cnt[b]) adds the two in order and writes C.
+    int dp_tiles;
+    float *sk_part;
+    int *sk_cnt;
 };
+
+// Work items of one CTA: (tile, k-blocks [kb0, kb1)).
+struct WorkIt {
+    int i;
+    int64_t pos, end;   // stream-K position / end in (tile - dp_tiles) * num_kb + kb
+};
+
+__device__ __forceinline__ bool next_item(const EpiParams &p, int num_tiles, WorkIt &w, int &tile, int &kb0,
+                                          int &kb1) {
+    if (w.pos < 0) {
+        const int t = blockIdx.x + w.i * gridDim.x;
+        if (t < p.dp_tiles) {
+            tile = t; kb0 = 0; kb1 = p.num_kb; w.i++;
+            return true;
+        }
+        const int64_t W = (int64_t)(num_tiles - p.dp_tiles) * p.num_kb;
+        w.pos = W * blockIdx.x / gridDim.x;
+        w.end = W * (blockIdx.x + 1) / gridDim.x;
+    }
+    if (w.pos >= w.end) return false;
+    if (blockIdx.x & 1) {
+        // odd CTAs walk their range backwards, so both parts of every split
+        // tile are computed at the same time (by the end of two neighbours'
+        // walks or by their start) and share its operand tiles in L2
+        const int st = (int)((w.end - 1) / p.num_kb);
+        const int64_t t0 = (int64_t)st * p.num_kb;
+        const int64_t s0 = w.pos > t0 ? w.pos : t0;
+        kb0 = (int)(s0 - t0);
+        kb1 = (int)(w.end - t0);
+        tile = p.dp_tiles + st;
+        w.end = s0;
+        return true;
+    }
+    const int st = (int)(w.pos / p.num_kb);
+    kb0 = (int)(w.pos - (int64_t)st * p.num_kb);
+    const int64_t left = w.end - w.pos;
+    kb1 = left < p.num_kb - kb0 ? kb0 + (int)left : p.num_kb;
+    tile = p.dp_tiles + st;
+    w.pos += kb1 - kb0;
+    return true;
+}
 
 __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int &tm, int &tn) {
     const int per_group = GROUP_M * tiles_n;
@@ -297,7 +346,6 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int num_tiles = p.tiles_m * p.tiles_n;
     const int chunk_kb = FOLD ? p.chunk_kb : p.num_kb;
-    const int nchunks = (p.num_kb + chunk_kb - 1) / chunk_kb;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
@@ -324,11 +372,13 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
         if (lane == 0) {   // TMA producer
             int kbg = 0;   // running k-block counter across tiles (stage / phase)
             bool go = true;
-            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+            WorkIt wi{0, -1, 0};
+            int t, kbA, kbB;
+            while (go && next_item(p, num_tiles, wi, t, kbA, kbB)) {
                 int tm, tn;
                 tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
                 const int m0 = tm * BM, n0 = tn * BN;
-                for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
+                for (int kb = kbA; kb < kbB; kb++, kbg++) {
                     const int s = kbg % STAGES;
                     if (kbg >= STAGES && !ptx::mbar_wait(&empty[s], ((kbg / STAGES) & 1) ^ 1, p.err, 1)) {
                         go = false;
@@ -350,8 +400,11 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
             int kbg = 0, ch = 0;   // running k-block and accumulator-chunk counters
             (void)B_TILE;
             bool go = true;
-            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
-                for (int c = 0; c < nchunks && go; c++, ch++) {
+            WorkIt wi{0, -1, 0};
+            int t, kbA, kbB;
+            while (go && next_item(p, num_tiles, wi, t, kbA, kbB)) {
+                const int nch = (kbB - kbA + chunk_kb - 1) / chunk_kb;
+                for (int c = 0; c < nch && go; c++, ch++) {
                     const int b = ch & 1;
                     if (ch >= 2 && !ptx::mbar_wait(&acc_empty[b], ((ch >> 1) & 1) ^ 1, p.err, 2)) {
                         go = false;
@@ -360,8 +413,9 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                     ptx::tc_fence_after();
                     const uint32_t acc = tmem + (uint32_t)(b * ACC_COLS);
                     const uint32_t acc_lo = FOLD ? acc + 128u : acc;   // cross products
-                    const int kb1 = (c + 1) * chunk_kb < p.num_kb ? (c + 1) * chunk_kb : p.num_kb;
-                    for (int kb = c * chunk_kb; kb < kb1; kb++, kbg++) {
+                    const int kbc = kbA + c * chunk_kb;
+                    const int kb1 = kbc + chunk_kb < kbB ? kbc + chunk_kb : kbB;
+                    for (int kb = kbc; kb < kb1; kb++, kbg++) {
                         const int s = kbg % STAGES;
                         if (!ptx::mbar_wait(&full[s], (kbg / STAGES) & 1, p.err, 3)) { go = false; break; }
                         ptx::tc_fence_after();
@@ -372,7 +426,7 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                             ad[i] = ptx::sdesc_kmajor_sw64(st + i * A_TILE);
                             bd[i] = ptx::sdesc_kmajor_sw64(st + NP * A_TILE + i * B_TILE);
                         }
-                        const bool first = kb == c * chunk_kb;
+                        const bool first = kb == kbc;
 #pragma unroll
                         for (int k = 0; k < BK / 16; k++) {
                             // advance 16 BF16 = 32 bytes along K inside the 64-byte swizzle atom
@@ -400,16 +454,23 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
         int ch = 0;
         float total[FOLD ? BN : 1];
         bool go = true;
-        for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+        __shared__ int sk_last;
+        WorkIt wi{0, -1, 0};
+        int t, kbA, kbB;
+        while (go && next_item(p, num_tiles, wi, t, kbA, kbB)) {
             int tm, tn;
             tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
             const int64_t row0 = (int64_t)tm * BM + q * 32;
             const int64_t n0 = (int64_t)tn * BN;
+            // a stream-K part: raw accumulator to its slot, C written by the second finisher
+            const bool part = !FOLD && (kbA != 0 || kbB != p.num_kb);
+            const int sk_b = kbA == 0 ? (int)blockIdx.x : (int)blockIdx.x - 1;
+            float *slot = part ? p.sk_part + ((size_t)sk_b * 2 + (kbA == 0 ? 0 : 1)) * (BM * BN) : nullptr;
             uint32_t accb = 0;
             if (FOLD) {
 #pragma unroll
                 for (int j = 0; j < (FOLD ? BN : 1); j++) total[j] = 0.f;
-                for (int c = 0; c < nchunks; c++, ch++) {
+                for (int c = 0; c < (kbB - kbA + chunk_kb - 1) / chunk_kb; c++, ch++) {
                     const int b = ch & 1;
                     if (!ptx::mbar_wait(&acc_full[b], (ch >> 1) & 1, p.err, 4)) { go = false; break; }
                     ptx::tc_fence_after();
@@ -450,6 +511,12 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                     for (int j = 0; j < 32; j++) stage[lane * 33 + j] = __uint_as_float(r[j]);
                 }
                 __syncwarp();
+                if (part) {   // raw values, tile-local layout [row][col]
+#pragma unroll
+                    for (int rr = 0; rr < 32; rr++) slot[(q * 32 + rr) * BN + c + lane] = stage[rr * 33 + lane];
+                    __syncwarp();
+                    continue;
+                }
                 const int64_t col = n0 + c + lane;
                 if (col < p.N) {
                     const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
@@ -479,6 +546,45 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                 __syncwarp();
                 if (lane == 0) ptx::mbar_arrive(&acc_empty[ch & 1]);
                 ch++;
+            }
+            if (part) {
+                __threadfence();                                  // this part is visible GPU-wide ...
+                asm volatile("bar.sync 1, 128;" ::: "memory");   // ... for all four epilogue warps
+                if (warp == 2 && lane == 0) {
+                    const int old = atomicAdd(&p.sk_cnt[sk_b], 1);
+                    if (old == 1) p.sk_cnt[sk_b] = 0;            // both parts done: reset for the next call
+                    sk_last = old == 1;
+                    __threadfence();
+                }
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                if (sk_last) {   // left part + right part, in that order, then the epilogue
+                    const float *p0 = p.sk_part + (size_t)sk_b * 2 * (BM * BN), *p1 = p0 + BM * BN;
+                    const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
+                    const bool read_c = p.semantics == GB_SEM_ACCUM_SCALAR_BETA ||
+                                        (p.semantics == GB_SEM_BLAS && p.beta != 0.f);
+                    for (int c = 0; c < BN; c += 32) {
+                        const int64_t col = n0 + c + lane;
+                        if (col >= p.N) continue;
+                        // all 32 rows' loads in flight before any use
+                        float v[32], cin[32];
+#pragma unroll
+                        for (int rr = 0; rr < 32; rr++) {
+                            const int e = (q * 32 + rr) * BN + c + lane;
+                            v[rr] = rr < rows ? __ldcg(p0 + e) + __ldcg(p1 + e) : 0.f;
+                            cin[rr] = (read_c && rr < rows) ? p.C[(row0 + rr) * p.ldc + col] : 0.f;
+                        }
+#pragma unroll
+                        for (int rr = 0; rr < 32; rr++) {
+                            if (rr >= rows) break;
+                            float x = p.alpha * v[rr];
+                            if (p.semantics == GB_SEM_BLAS) x = p.beta != 0.f ? fmaf(p.beta, cin[rr], x) : x;
+                            else if (p.semantics == GB_SEM_SCALAR_BETA) x = x + p.beta;
+                            else x = cin[rr] + (x + p.beta);
+                            p.C[(row0 + rr) * p.ldc + col] = x;
+                        }
+                    }
+                }
+                asm volatile("bar.sync 1, 128;" ::: "memory");   // sk_last is reused by the next part
             }
         }
     }
@@ -845,8 +951,25 @@ gb_status launch_sgemm_bf16x6(const GemmArgs &g) {
     return two_pass(g, 3, env_chunk("GB_BF16X6_CHUNK", 8));
 }
 
+// Stream-K split of the last waves (tiles that do not fill the grid), or
+// none: dp_tiles = tiles.  Only when every CTA's share of the split range is
+// at least one whole tile, so a split tile has exactly two parts.
+// Off unless GB_BF16X3_SK=1: on this GPU the split measured slower than
+// whole tiles even where whole tiles waste most of a wave (4096^3, 512
+// tiles on 152 SMs: 0.344 vs 0.306 ms per call; 1152 x 4352 x 4096, 153
+// tiles: 0.187 vs 0.163 ms), the two parts of a tile fetching its operand
+// panels separately (L2 traffic +32 %, DRAM reads +60 %).
+static int stream_k_dp_tiles(int tiles, int grid, bool fold) {
+    const char *e = getenv("GB_BF16X3_SK");
+    if (fold || !(e && e[0] == '1') || grid <= 1) return tiles;
+    const int full = tiles / grid, rem = tiles % grid;
+    if (rem == 0 || full < 1) return tiles;
+    return (full - 1) * grid;
+}
+
 template <int NP, int BN, bool FOLD>
-static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64_t kp, int *err, int fold_kb) {
+static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64_t kp, int *err, int fold_kb,
+                                 float *sk_part, int *sk_cnt) {
     using CF = TwoPass<NP, BN>;
     static bool attr_set = false;
     if (!attr_set) {
@@ -855,10 +978,12 @@ static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64
         attr_set = true;
     }
     const int tiles_m = (int)ceil_div(g.M, BM), tiles_n = (int)ceil_div(g.N, BN);
-    EpiParams p{(float *)g.C, g.M, g.N, g.ldc, (float)g.alpha, (float)g.beta, g.semantics, (int)(kp / BK),
-                tiles_m, tiles_n, err, FOLD ? fold_kb : 1};
     const int tiles = tiles_m * tiles_n;
     const int grid = tiles < sm_count() ? tiles : sm_count();
+    const int dp = sk_part ? stream_k_dp_tiles(tiles, grid, FOLD) : tiles;
+    if (dp < tiles) GB_CUDA_TRY(cudaMemsetAsync(sk_cnt, 0, (size_t)grid * sizeof(int), g.stream));
+    EpiParams p{(float *)g.C, g.M, g.N, g.ldc, (float)g.alpha, (float)g.beta, g.semantics, (int)(kp / BK),
+                tiles_m, tiles_n, err, FOLD ? fold_kb : 1, dp, sk_part, sk_cnt};
     bf16x3_gemm_kernel<NP, BN, FOLD><<<grid, NT, CF::SMEM_BYTES, g.stream>>>(maps, p);
     GB_LAUNCH_CHECK("bf16x3_gemm_kernel");
     return ok();
@@ -869,8 +994,14 @@ static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64
 static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
     const int64_t kp = ceil_div(g.K, 64) * 64;   // multiple of BK, zero-padded
     const size_t a_bytes = (size_t)g.M * kp * 2, b_bytes = (size_t)g.N * kp * 2;
-    uint8_t *ws = (uint8_t *)workspace(np * (a_bytes + b_bytes) + 4096, g.stream);
+    // pieces, then the stream-K part slots (2 per CTA of 128 x 256 FP32) and counters
+    const size_t pieces = (np * (a_bytes + b_bytes) + 255) / 256 * 256;
+    const bool sk = np == 2 && fold_kb == 0;
+    const size_t sk_bytes = sk ? (size_t)sm_count() * 2 * BM * 256 * 4 + (size_t)sm_count() * 4 : 0;
+    uint8_t *ws = (uint8_t *)workspace(pieces + sk_bytes + 4096, g.stream);
     if (!ws) return (gb_status)gb_get_last_status();
+    float *sk_part = sk ? (float *)(ws + pieces) : nullptr;
+    int *sk_cnt = sk ? (int *)(ws + pieces + (size_t)sm_count() * 2 * BM * 256 * 4) : nullptr;
     __nv_bfloat16 *ap[3], *bp[3];
     for (int i = 0; i < np; i++) {
         ap[i] = (__nv_bfloat16 *)(ws + i * a_bytes);
@@ -916,10 +1047,10 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
     }
     if (!okm) return set_status(GB_ERR_CUDA, "bf16x3: cuTensorMapEncodeTiled failed");
     if (np == 3)
-        return fold_kb > 0 ? two_pass_launch<3, 128, true>(g, maps, kp, err, fold_kb)
-                           : two_pass_launch<3, 128, false>(g, maps, kp, err, 0);
-    return fold_kb > 0 ? two_pass_launch<2, 128, true>(g, maps, kp, err, fold_kb)
-                       : two_pass_launch<2, 256, false>(g, maps, kp, err, 0);
+        return fold_kb > 0 ? two_pass_launch<3, 128, true>(g, maps, kp, err, fold_kb, nullptr, nullptr)
+                           : two_pass_launch<3, 128, false>(g, maps, kp, err, 0, nullptr, nullptr);
+    return fold_kb > 0 ? two_pass_launch<2, 128, true>(g, maps, kp, err, fold_kb, nullptr, nullptr)
+                       : two_pass_launch<2, 256, false>(g, maps, kp, err, 0, sk_part, sk_cnt);
 }
 
 }  // namespace gb

@@ -276,3 +276,38 @@ extern "C" gb_status gb_gemm_batch(const gb_gemm_desc *descs, int n, void *strea
     if (!g_batch_runner) g_batch_runner = group_runner_create(4, 4096);
     return group_runner_run(g_batch_runner, descs, n, stream, 0);
 }
+
+// Strided batch: GEMM i uses A + i*strideA, B + i*strideB, C + i*strideC
+// (strides in elements), all with the same shape, modes and scalars; run as
+// grouped launches of up to 4096 GEMMs.
+extern "C" gb_status gb_gemm_strided_batched(int dtype_bits, char transA, char transB, int64_t M, int64_t N,
+                                             int64_t K, double alpha, const void *A, int64_t lda, int64_t strideA,
+                                             const void *B, int64_t ldb, int64_t strideB, double beta, void *C,
+                                             int64_t ldc, int64_t strideC, int64_t batch, int semantics,
+                                             void *stream) {
+    using namespace gb;
+    GB_CHECK_ARG(dtype_bits == 32 || dtype_bits == 64, "gb_gemm_strided_batched: dtype_bits must be 32 or 64");
+    GB_CHECK_ARG(batch >= 0, "gb_gemm_strided_batched: negative batch count");
+    GB_CHECK_ARG(strideA >= 0 && strideB >= 0 && strideC >= 0, "gb_gemm_strided_batched: negative stride");
+    if (batch == 0) return ok();
+    // distinct C matrices must not overlap: strideC covers one C (rows x ldc)
+    GB_CHECK_ARG(batch == 1 || strideC >= (M > 0 ? (M - 1) * ldc + N : 0),
+                 "gb_gemm_strided_batched: strideC %lld smaller than one C", (long long)strideC);
+    const size_t es = dtype_bits / 8;
+    std::vector<gb_gemm_desc> d((size_t)(batch < 4096 ? batch : 4096));
+    for (int64_t b0 = 0; b0 < batch; b0 += 4096) {
+        const int n = (int)(batch - b0 < 4096 ? batch - b0 : 4096);
+        for (int i = 0; i < n; i++) {
+            gb_gemm_desc &q = d[i];
+            memset(&q, 0, sizeof(q));
+            q.dtype_bits = dtype_bits; q.transA = transA; q.transB = transB; q.semantics = semantics;
+            q.M = M; q.N = N; q.K = K; q.alpha = alpha; q.beta = beta;
+            q.A = (const char *)A + (size_t)(b0 + i) * strideA * es; q.lda = lda;
+            q.B = (const char *)B + (size_t)(b0 + i) * strideB * es; q.ldb = ldb;
+            q.C = (char *)C + (size_t)(b0 + i) * strideC * es; q.ldc = ldc;
+        }
+        gb_status st = gb_gemm_batch(d.data(), n, stream);
+        if (st != GB_OK) return st;
+    }
+    return ok();
+}

@@ -204,6 +204,157 @@ void launch_rs(const E *src, E *dst, int64_t M, int64_t N, int order, cudaStream
     else stencil_rs_kernel<E, T, 2><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs);
 }
 
+// 9-point stencil with a 3x3 weight window (w[0..2] the row above, w[3..5]
+// the row, w[6..8] the row below): r = w0*a_tl, then eight fused
+// multiply-adds in window order.  Same register-streaming scheme as the
+// 5-point kernel; every row that enters a level's window brings the left /
+// right neighbours of its edge columns (two shuffles per row and level).
+template <typename E>
+struct W9 {
+    E w[9];
+};
+
+template <typename E>
+struct Row4 {
+    E v[4];
+    E lft, rgt;   // column 4*lane - 1 and 4*lane + 4
+};
+
+template <typename E>
+__device__ __forceinline__ E fma_rn(E a, E b, E c);
+template <>
+__device__ __forceinline__ float fma_rn<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+template <>
+__device__ __forceinline__ double fma_rn<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <typename E>
+__device__ __forceinline__ E mul_rn(E a, E b);
+template <>
+__device__ __forceinline__ float mul_rn<float>(float a, float b) { return __fmul_rn(a, b); }
+template <>
+__device__ __forceinline__ double mul_rn<double>(double a, double b) { return __dmul_rn(a, b); }
+
+template <typename E, int T>
+__global__ void __launch_bounds__(RS_NT) stencil9_rs_kernel(const E *__restrict__ src, E *__restrict__ dst,
+                                                            int64_t M, int64_t N, int strips, int segs, W9<E> w) {
+    const int lane = threadIdx.x % 32;
+    const int64_t wid = (int64_t)blockIdx.x * (RS_NT / 32) + threadIdx.x / 32;
+    if (wid >= (int64_t)strips * segs) return;   // whole warp
+    const int sx = (int)(wid % strips), sy = (int)(wid / strips);
+    const int64_t ld = N + 2;
+    const int64_t c0 = 1 + (int64_t)sx * (RS_W - 2 * T) - T;
+    const int64_t out_r0 = 1 + (int64_t)sy * RS_SEG;
+    const int64_t out_r1 = out_r0 + RS_SEG < M + 1 ? out_r0 + RS_SEG : M + 1;
+    const int64_t cl = c0 + 4 * lane;
+
+    bool cfix[4], cload[4], cstore[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int64_t gc = cl + q;
+        const int lc = 4 * lane + q;
+        cfix[q] = gc <= 0 || gc >= N + 1;
+        cload[q] = gc >= 0 && gc <= N + 1;
+        cstore[q] = lc >= T && lc < RS_W - T && gc >= 1 && gc <= N;
+    }
+
+    Row4<E> p2[T], p1[T];
+#pragma unroll
+    for (int l = 0; l < T; l++) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) p2[l].v[q] = p1[l].v[q] = E(0);
+        p2[l].lft = p2[l].rgt = p1[l].lft = p1[l].rgt = E(0);
+    }
+
+    for (int64_t i = out_r0 - T - 1; i < out_r1 + T; i++) {
+        Row4<E> x;
+#pragma unroll
+        for (int q = 0; q < 4; q++) x.v[q] = E(0);
+        if (i >= 0 && i <= M + 1) {
+            const E *row = src + i * ld + cl;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (cload[q]) x.v[q] = __ldg(row + q);
+        }
+#pragma unroll
+        for (int l = 0; l < T; l++) {
+            x.lft = __shfl_up_sync(0xffffffffu, x.v[3], 1);
+            x.rgt = __shfl_down_sync(0xffffffffu, x.v[0], 1);
+            const int64_t gr = i - l - 1;
+            const bool rfix = gr <= 0 || gr >= M + 1;
+            const Row4<E> &t = p2[l], &m = p1[l];
+            Row4<E> v;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const E tl = q == 0 ? t.lft : t.v[q - 1], tr = q == 3 ? t.rgt : t.v[q + 1];
+                const E ml = q == 0 ? m.lft : m.v[q - 1], mr = q == 3 ? m.rgt : m.v[q + 1];
+                const E dl = q == 0 ? x.lft : x.v[q - 1], dr = q == 3 ? x.rgt : x.v[q + 1];
+                E r = mul_rn(w.w[0], tl);
+                r = fma_rn(w.w[1], t.v[q], r);
+                r = fma_rn(w.w[2], tr, r);
+                r = fma_rn(w.w[3], ml, r);
+                r = fma_rn(w.w[4], m.v[q], r);
+                r = fma_rn(w.w[5], mr, r);
+                r = fma_rn(w.w[6], dl, r);
+                r = fma_rn(w.w[7], x.v[q], r);
+                r = fma_rn(w.w[8], dr, r);
+                v.v[q] = (rfix || cfix[q]) ? m.v[q] : r;
+            }
+            p2[l] = p1[l];
+            p1[l] = x;
+            x = v;
+        }
+        const int64_t ro = i - T;
+        if (ro >= out_r0 && ro < out_r1) {
+            E *row = dst + ro * ld + cl;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (cstore[q]) row[q] = x.v[q];
+        }
+    }
+}
+
+template <typename E, int T>
+void launch_rs9(const E *src, E *dst, int64_t M, int64_t N, const W9<E> &w, cudaStream_t st) {
+    const int strips = (int)ceil_div(N, RS_W - 2 * T);
+    const int segs = (int)ceil_div(M, RS_SEG);
+    const unsigned blocks = (unsigned)ceil_div((int64_t)strips * segs, RS_NT / 32);
+    stencil9_rs_kernel<E, T><<<blocks, RS_NT, 0, st>>>(src, dst, M, N, strips, segs, w);
+}
+
+template <typename E>
+gb_status stencil9(int64_t M, int64_t N, E *A, E *B, int iters, const E *w_host, void *stream) {
+    GB_CHECK_ARG(M >= 0 && N >= 0, "stencil9: negative size");
+    GB_CHECK_ARG(iters >= 0, "stencil9: negative iteration count");
+    if (M == 0 || N == 0 || iters == 0) return ok();
+    GB_CHECK_ARG(A && B && A != B, "stencil9: A and B must be distinct device buffers");
+    GB_CHECK_ARG(w_host != nullptr, "stencil9: null weight window");
+    GB_CHECK_ARG((M + RS_SEG - 1) / RS_SEG < (1 << 30), "stencil9: M too large");
+    W9<E> w;
+    for (int i = 0; i < 9; i++) w.w[i] = w_host[i];
+    // FP32: 4 sweeps per pass (the window rows of 4 levels fill the register
+    // budget); FP64 is bound by the FP64 pipe: one sweep per pass
+    const int tmax = sizeof(E) == 4 ? 4 : 1;
+    int L = (int)ceil_div(iters, tmax);
+    if ((L & 1) != (iters & 1)) L += 1;   // result in B for odd iters, in A for even
+    cudaStream_t st = as_stream(stream);
+    int done = 0;
+    for (int l = 0; l < L; l++) {
+        int t = (iters - done) / (L - l);
+        if ((iters - done) % (L - l)) t += 1;
+        const E *src = (l % 2 == 0) ? A : B;
+        E *dst = (l % 2 == 0) ? B : A;
+        switch (t) {
+            case 1: launch_rs9<E, 1>(src, dst, M, N, w, st); break;
+            case 2: launch_rs9<E, (sizeof(E) == 4 ? 2 : 1)>(src, dst, M, N, w, st); break;
+            case 3: launch_rs9<E, (sizeof(E) == 4 ? 3 : 1)>(src, dst, M, N, w, st); break;
+            default: launch_rs9<E, (sizeof(E) == 4 ? 4 : 1)>(src, dst, M, N, w, st); break;
+        }
+        GB_LAUNCH_CHECK("stencil9_rs_kernel");
+        done += t;
+    }
+    return ok();
+}
+
 template <typename T>
 gb_status stencil(int64_t M, int64_t N, T *A, T *B, int iters, int order, void *stream) {
     GB_CHECK_ARG(M >= 0 && N >= 0, "stencil2d: negative size");
@@ -284,6 +435,14 @@ gb_status gb_stencil2d_f64(int64_t M, int64_t N, double *A, double *B, int iters
 
 gb_status gb_stencil2d_f32(int64_t M, int64_t N, float *A, float *B, int iters, int order, void *stream) {
     return gb::stencil<float>(M, N, A, B, iters, order, stream);
+}
+
+gb_status gb_stencil9_f32(int64_t M, int64_t N, float *A, float *B, int iters, const float *w, void *stream) {
+    return gb::stencil9<float>(M, N, A, B, iters, w, stream);
+}
+
+gb_status gb_stencil9_f64(int64_t M, int64_t N, double *A, double *B, int iters, const double *w, void *stream) {
+    return gb::stencil9<double>(M, N, A, B, iters, w, stream);
 }
 
 }  // extern "C"

@@ -82,6 +82,43 @@ __global__ void __launch_bounds__(256) transpose2x2_kernel(const float *__restri
     }
 }
 
+// B += A^T (transpose-accumulate): the 64 x 64 tile of A goes through padded
+// shared memory as above; each B element gets one IEEE add.  HBM-bound:
+// 3 M N sizeof(T) bytes (A read, B read and written).
+template <typename T>
+__global__ void __launch_bounds__(TILE * ROWS) transpose_add_kernel(const T *__restrict__ A, int64_t lda, T *B,
+                                                                    int64_t ldb, int64_t M, int64_t N) {
+    __shared__ T tile[TILE][TILE + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int64_t r0 = (int64_t)blockIdx.y * TILE, c0 = (int64_t)blockIdx.x * TILE;
+#pragma unroll
+    for (int i = 0; i < TILE; i += ROWS) {
+        int64_t r = r0 + ty + i, c = c0 + tx;
+        if (r < M && c < N) tile[ty + i][tx] = A[r * lda + c];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < TILE; i += ROWS) {
+        int64_t br = c0 + ty + i, bc = r0 + tx;
+        if (br < N && bc < M) B[br * ldb + bc] = B[br * ldb + bc] + tile[tx][ty + i];
+    }
+}
+
+template <typename T>
+gb_status transpose_add(int64_t M, int64_t N, const T *A, int64_t lda, T *B, int64_t ldb, void *stream) {
+    GB_CHECK_ARG(M >= 0 && N >= 0, "transpose_add: negative size");
+    GB_CHECK_ARG(lda >= N || M == 0, "transpose_add: lda (%lld) < N (%lld)", (long long)lda, (long long)N);
+    GB_CHECK_ARG(ldb >= M || N == 0, "transpose_add: ldb (%lld) < M (%lld)", (long long)ldb, (long long)M);
+    if (M == 0 || N == 0) return ok();
+    GB_CHECK_ARG(A && B, "transpose_add: null pointer");
+    GB_CHECK_ARG((const void *)A != (const void *)B, "transpose_add: A and B must not be the same buffer");
+    dim3 grid((unsigned)ceil_div(N, TILE), (unsigned)ceil_div(M, TILE));
+    GB_CHECK_ARG(grid.y <= 65535u, "transpose_add: M too large");
+    transpose_add_kernel<T><<<grid, dim3(TILE, ROWS), 0, as_stream(stream)>>>(A, lda, B, ldb, M, N);
+    GB_LAUNCH_CHECK("transpose_add_kernel");
+    return ok();
+}
+
 template <typename T>
 gb_status transpose(int64_t M, int64_t N, const T *A, int64_t lda, T *B, int64_t ldb, void *stream) {
     GB_CHECK_ARG(M >= 0 && N >= 0, "transpose: negative size");
@@ -114,6 +151,16 @@ gb_status gb_transpose_f32(int64_t M, int64_t N, const float *A, int64_t lda, fl
 gb_status gb_transpose_f64(int64_t M, int64_t N, const double *A, int64_t lda, double *B, int64_t ldb,
                            void *stream) {
     return gb::transpose<double>(M, N, A, lda, B, ldb, stream);
+}
+
+gb_status gb_transpose_add_f32(int64_t M, int64_t N, const float *A, int64_t lda, float *B, int64_t ldb,
+                               void *stream) {
+    return gb::transpose_add<float>(M, N, A, lda, B, ldb, stream);
+}
+
+gb_status gb_transpose_add_f64(int64_t M, int64_t N, const double *A, int64_t lda, double *B, int64_t ldb,
+                               void *stream) {
+    return gb::transpose_add<double>(M, N, A, lda, B, ldb, stream);
 }
 
 }  // extern "C"

@@ -110,6 +110,12 @@ _SIGS = {
                   ctypes.POINTER(GemmOpts)], _int),
     "gb_gemm_pick_algo": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64], _int),
     "gb_transpose_f32": ([_i64, _i64, _vp, _i64, _vp, _i64, _vp], _int),
+    "gb_transpose_add_f32": ([_i64, _i64, _vp, _i64, _vp, _i64, _vp], _int),
+    "gb_stencil9_f32": ([_i64, _i64, _vp, _vp, _int, _vp, _vp], _int),
+    "gb_stencil9_f64": ([_i64, _i64, _vp, _vp, _int, _vp, _vp], _int),
+    "gb_transpose_add_f64": ([_i64, _i64, _vp, _i64, _vp, _i64, _vp], _int),
+    "gb_gemm_strided_batched": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, ctypes.c_double, _vp, _i64,
+                                 _i64, _vp, _i64, _i64, ctypes.c_double, _vp, _i64, _i64, _i64, _int, _vp], _int),
     "gb_transpose_f64": ([_i64, _i64, _vp, _i64, _vp, _i64, _vp], _int),
     "gb_stencil2d_f64": ([_i64, _i64, _vp, _vp, _int, _int, _vp], _int),
     "gb_stencil2d_f32": ([_i64, _i64, _vp, _vp, _int, _int, _vp], _int),
@@ -244,6 +250,27 @@ def pick_algo(bits, ta, tb, M, N, K):
 def transpose(M, N, A, lda, B, ldb, bits, stream=None):
     f = lib().gb_transpose_f64 if bits == 64 else lib().gb_transpose_f32
     _check(f(M, N, _ptr(A), lda, _ptr(B), ldb, _stream(stream)), "transpose")
+
+
+def transpose_add(M, N, A, lda, B, ldb, bits, stream=None):
+    """B += A^T (bit-exact transpose-accumulate)."""
+    f = lib().gb_transpose_add_f64 if bits == 64 else lib().gb_transpose_add_f32
+    _check(f(M, N, _ptr(A), lda, _ptr(B), ldb, _stream(stream)), "transpose_add")
+
+
+def gemm_strided_batched(bits, ta, tb, M, N, K, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc, strideC,
+                         batch, semantics=SEM_BLAS, stream=None):
+    _check(lib().gb_gemm_strided_batched(bits, ta.encode(), tb.encode(), M, N, K, alpha, _ptr(A), lda, strideA,
+                                         _ptr(B), ldb, strideB, beta, _ptr(C), ldc, strideC, batch, semantics,
+                                         _stream(stream)), "gb_gemm_strided_batched")
+
+
+def stencil9(M, N, A, B, iters, w, bits=64, stream=None):
+    """9-point stencil with the 3x3 weight window w (host sequence of 9)."""
+    import numpy as _np
+    wv = _np.ascontiguousarray(_np.asarray(w, dtype=_np.float64 if bits == 64 else _np.float32).reshape(9))
+    f = lib().gb_stencil9_f64 if bits == 64 else lib().gb_stencil9_f32
+    _check(f(M, N, _ptr(A), _ptr(B), iters, wv.ctypes.data, _stream(stream)), "stencil9")
 
 
 def stencil2d(M, N, A, B, iters, order=STENCIL_HOST, bits=64, stream=None):

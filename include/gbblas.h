@@ -139,7 +139,9 @@ gb_status gb_dgemm(char transA, char transB, int64_t M, int64_t N, int64_t K,
  * computes (same kernels, same split-K plan; thinB when N <= M, else
  * shortA); for 8 < min(M, N) <= 64, where GB_ALGO_SKINNY runs 3xBF16 on the
  * tensor cores, it runs the FP32 FFMA streaming kernels (FP32 rounding, the
- * same 2*K*u normwise bound).  K >= 1.  It keeps the split-K partial sums in a fixed
+ * same 2*K*u normwise bound).  K >= 1.  It keeps the split-K partial sums
+ * (and, when an operand's layout cannot be read by TMA in place, a packed copy
+ * of the small operand) in a fixed
  * 16 MiB array of device memory that every GPU loading the library reserves
  * until the process exits.  A call whose split-K plan needs more than 16 MiB
  * (splits x max(M, N) x padded min(M, N) x 4 bytes) is rejected with
@@ -180,12 +182,33 @@ typedef struct gb_gemm_desc {
  * on `stream`; the descriptors are copied before the call returns. */
 gb_status gb_gemm_batch(const gb_gemm_desc *descs, int n, void *stream);
 
+/* Strided batch of equal-shape GEMMs: GEMM i reads A + i*strideA and
+ * B + i*strideB and writes C + i*strideC (strides in elements; 0 shares an
+ * operand), each as in gb_sgemm / gb_dgemm (dtype_bits 32 or 64), through
+ * the grouped kernel in launches of up to 4096.  No reference counterpart
+ * (ld-aware batched variants of the irregular path). */
+gb_status gb_gemm_strided_batched(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
+                                  double alpha, const void *A, int64_t lda, int64_t strideA,
+                                  const void *B, int64_t ldb, int64_t strideB, double beta,
+                                  void *C, int64_t ldc, int64_t strideC, int64_t batch, int semantics,
+                                  void *stream);
+
 /* ------------------------------------------------------ transpose */
 /* B (N x M, ldb >= M) = A^T, A is M x N (lda >= N).  Bit-exact copy.
  * Replaces transpose/device_code/kernel.c:2002 transpose_float_32x32_dbuf
  * and :1167 transpose_16x16_dbuf, and dgemm_kernel.c:974 transpose_A2B. */
 gb_status gb_transpose_f32(int64_t M, int64_t N, const float *A, int64_t lda, float *B, int64_t ldb, void *stream);
 gb_status gb_transpose_f64(int64_t M, int64_t N, const double *A, int64_t lda, double *B, int64_t ldb, void *stream);
+
+/* B (N x M, ldb >= M) += A^T, A is M x N (lda >= N): one IEEE add per
+ * element, bit-exact.  The transpose-accumulate of the reference's
+ * micro_kernel_16x16_add / micro_kernel_16x16x2_add (dgemm_release_V1.1/
+ * device_code/dgemm_kernel.c:174, :635) and micro_kernel_float_32x32_add
+ * (sgemm_release_V1.3.1/device_code/sgemm_kernel.c:482) as an entry point. */
+gb_status gb_transpose_add_f32(int64_t M, int64_t N, const float *A, int64_t lda, float *B, int64_t ldb,
+                               void *stream);
+gb_status gb_transpose_add_f64(int64_t M, int64_t N, const double *A, int64_t lda, double *B, int64_t ldb,
+                               void *stream);
 
 /* -------------------------------------------------------- stencil */
 typedef enum gb_stencil_order {
@@ -205,6 +228,18 @@ typedef enum gb_stencil_order {
  * chosen order. */
 gb_status gb_stencil2d_f64(int64_t M, int64_t N, double *A, double *B, int iters, int order, void *stream);
 gb_status gb_stencil2d_f32(int64_t M, int64_t N, float *A, float *B, int iters, int order, void *stream);
+
+/* `iters` sweeps of a 9-point stencil with the 3x3 weight window w (a HOST
+ * array of 9: w[0..2] weigh the row above (columns -1, 0, +1), w[3..5] the
+ * row itself, w[6..8] the row below), on the same padded grids, ping-pong
+ * and fixed halo as gb_stencil2d:
+ *     r = w0*a(-1,-1); r = fma(w1, a(-1,0), r); ... r = fma(w8, a(+1,+1), r)
+ * in window order, so results are bit-identical to that recurrence.  No
+ * reference counterpart: the generalisation of stencil_2d
+ * (stencil_2d_V1.2/device_code/kernel_stencil.c) on the same temporal-
+ * blocking engine. */
+gb_status gb_stencil9_f32(int64_t M, int64_t N, float *A, float *B, int iters, const float *w, void *stream);
+gb_status gb_stencil9_f64(int64_t M, int64_t N, double *A, double *B, int iters, const double *w, void *stream);
 
 /* ---------------------------------------------------------- serving */
 /* A request loop over the kernels above, for streams of independent

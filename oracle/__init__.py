@@ -46,6 +46,10 @@ def lib():
                                     ctypes.c_float, _dp, _i64, _i64, _i64, ctypes.c_int],
             "gbo_transpose_f32": [_i64, _i64, _dp, _i64, _dp, _i64],
             "gbo_transpose_f64": [_i64, _i64, _dp, _i64, _dp, _i64],
+            "gbo_transpose_add_f32": [_i64, _i64, _dp, _i64, _dp, _i64],
+            "gbo_stencil9_f32": [_i64, _i64, _dp, _dp, ctypes.c_int, _dp],
+            "gbo_stencil9_f64": [_i64, _i64, _dp, _dp, ctypes.c_int, _dp],
+            "gbo_transpose_add_f64": [_i64, _i64, _dp, _i64, _dp, _i64],
             "gbo_stencil_f64": [_i64, _i64, _dp, _dp, ctypes.c_int, ctypes.c_int],
             "gbo_stencil_f32": [_i64, _i64, _dp, _dp, ctypes.c_int, ctypes.c_int],
             "gbo_gemm_dot2_f64": [ctypes.c_int, ctypes.c_int, _i64, _i64, _i64, ctypes.c_double, _dp, _i64, _dp, _i64,
@@ -119,6 +123,20 @@ def thinB_sgemm_ref(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, kg=307
 def transpose_into(M, N, A, lda, B, ldb):
     f = lib().gbo_transpose_f64 if A.dtype == np.float64 else lib().gbo_transpose_f32
     f(M, N, _p(A), lda, _p(B), ldb)
+
+
+def transpose_add_into(M, N, A, lda, B, ldb):
+    """B += A^T in place (transpose-accumulate)."""
+    f = lib().gbo_transpose_add_f64 if A.dtype == np.float64 else lib().gbo_transpose_add_f32
+    f(M, N, _p(A), lda, _p(B), ldb)
+
+
+def stencil9(M, N, A, B, iters, w):
+    """iters 9-point sweeps with the 3x3 weight window w, ping-ponging A and B."""
+    dt = A.dtype
+    wv = np.ascontiguousarray(np.asarray(w, dtype=dt).reshape(9))
+    f = lib().gbo_stencil9_f64 if dt == np.float64 else lib().gbo_stencil9_f32
+    f(M, N, _p(A), _p(B), iters, _p(wv))
 
 
 def stencil(M, N, A, B, iters, order=0):

@@ -215,6 +215,30 @@ void gbo_transpose_f64(int64_t M, int64_t N, const double *A, int64_t lda, doubl
             memcpy(&B[OFFSET(j, i, ldb)], &A[OFFSET(i, j, lda)], sizeof(double));
 }
 
+/* Transpose-accumulate B += A^T: the semantics of the reference's
+ * micro_kernel_16x16_add / micro_kernel_16x16x2_add
+ * (dgemm_release_V1.1/device_code/dgemm_kernel.c:174, :635) and
+ * micro_kernel_float_32x32_add (sgemm_release_V1.3.1/device_code/
+ * sgemm_kernel.c:482), which add a transposed tile into C; one IEEE add per
+ * element. */
+void gbo_transpose_add_f32(int64_t M, int64_t N, const float *A, int64_t lda, float *B, int64_t ldb)
+{
+    int nt = gbo_get_threads();
+    #pragma omp parallel for num_threads(nt) collapse(2) schedule(static)
+    for (int64_t i = 0; i < M; i++)
+        for (int64_t j = 0; j < N; j++)
+            B[OFFSET(j, i, ldb)] = B[OFFSET(j, i, ldb)] + A[OFFSET(i, j, lda)];
+}
+
+void gbo_transpose_add_f64(int64_t M, int64_t N, const double *A, int64_t lda, double *B, int64_t ldb)
+{
+    int nt = gbo_get_threads();
+    #pragma omp parallel for num_threads(nt) collapse(2) schedule(static)
+    for (int64_t i = 0; i < M; i++)
+        for (int64_t j = 0; j < N; j++)
+            B[OFFSET(j, i, ldb)] = B[OFFSET(j, i, ldb)] + A[OFFSET(i, j, lda)];
+}
+
 /* ---------------------------------------------------------------- stencil */
 /* stencil_2d_V1.2/host_code/matrix_stencil.c:35-48 with a working pointer
  * swap (the reference's switch_pointer at :28-33 swaps copies) and the
@@ -256,6 +280,45 @@ void gbo_stencil_f64(int64_t M, int64_t N, double *A, double *B, int iters, int 
 void gbo_stencil_f32(int64_t M, int64_t N, float *A, float *B, int iters, int order)
 {
     STENCIL_BODY(float, 0.2f)
+}
+
+/* 9-point stencil with a 3x3 weight window w (row-major: w[0..2] the row
+ * above, w[3..5] the row itself, w[6..8] the row below), the generalisation
+ * of stencil_2d named as the next step of the hot path.  Order: the first
+ * product rounded, then eight fused multiply-adds in window order.  Same
+ * padded layout and ping-pong as gbo_stencil; the halo is never written. */
+#define STENCIL9_BODY(T, FMA)                                                   \
+    int nt = gbo_get_threads();                                                 \
+    const int64_t ld = N + 2;                                                   \
+    for (int it = 0; it < iters; it++) {                                        \
+        const T *src = (it % 2 == 0) ? A : B;                                   \
+        T *dst = (it % 2 == 0) ? B : A;                                         \
+        _Pragma("omp parallel for num_threads(nt) schedule(static)")            \
+        for (int64_t row = 0; row < M; row++) {                                 \
+            for (int64_t col = 0; col < N; col++) {                             \
+                const T *p = src + row * ld + col;   /* window top-left */      \
+                T r = w[0] * p[0];                                              \
+                r = FMA(w[1], p[1], r);                                         \
+                r = FMA(w[2], p[2], r);                                         \
+                r = FMA(w[3], p[ld], r);                                        \
+                r = FMA(w[4], p[ld + 1], r);                                    \
+                r = FMA(w[5], p[ld + 2], r);                                    \
+                r = FMA(w[6], p[2 * ld], r);                                    \
+                r = FMA(w[7], p[2 * ld + 1], r);                                \
+                r = FMA(w[8], p[2 * ld + 2], r);                                \
+                dst[(row + 1) * ld + col + 1] = r;                              \
+            }                                                                   \
+        }                                                                       \
+    }
+
+void gbo_stencil9_f64(int64_t M, int64_t N, double *A, double *B, int iters, const double *w)
+{
+    STENCIL9_BODY(double, fma)
+}
+
+void gbo_stencil9_f32(int64_t M, int64_t N, float *A, float *B, int iters, const float *w)
+{
+    STENCIL9_BODY(float, fmaf)
 }
 
 /* -------------------------------------------------------- accuracy oracle */

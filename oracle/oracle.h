@@ -85,6 +85,12 @@ void gbo_thinB_sgemm_ref(int ta, int tb, int64_t M, int64_t N, int64_t K, float 
  * copies bits. */
 void gbo_transpose_f32(int64_t M, int64_t N, const float *A, int64_t lda, float *B, int64_t ldb);
 void gbo_transpose_f64(int64_t M, int64_t N, const double *A, int64_t lda, double *B, int64_t ldb);
+/* 9-point stencil, 3x3 weight window, first product then 8 fmas */
+void gbo_stencil9_f64(int64_t M, int64_t N, double *A, double *B, int iters, const double *w);
+void gbo_stencil9_f32(int64_t M, int64_t N, float *A, float *B, int iters, const float *w);
+/* B += A^T (transpose-accumulate of the reference's *_add micro-kernels) */
+void gbo_transpose_add_f32(int64_t M, int64_t N, const float *A, int64_t lda, float *B, int64_t ldb);
+void gbo_transpose_add_f64(int64_t M, int64_t N, const double *A, int64_t lda, double *B, int64_t ldb);
 
 /* --------------------------------------------------------------- stencil */
 /* One 5-point Jacobi sweep per iteration on an (M+2)x(N+2) padded grid,

@@ -104,3 +104,41 @@ def test_fill_matches_oracle(torch):
             gbblas.fill(d, 123, 77, 80, 99, kind, bits)
             got = host(d)
             assert got[:, :77].tobytes() == np.ascontiguousarray(want[:, :77]).tobytes()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("M,N,pad", [(1, 1, 0), (63, 65, 3), (300, 129, 0), (1000, 777, 5)])
+def test_transpose_add_bit_exact(torch, dtype, M, N, pad):
+    """B += A^T, the reference's *_add transpose-accumulate, one IEEE add per element."""
+    import gbblas
+    bits = 64 if dtype == np.float64 else 32
+    A = oracle.fill(M, N, 61, dtype=dtype, ld=N + pad)
+    B = oracle.fill(N, M, 62, kind=2, dtype=dtype, ld=M + pad)
+    want = B.copy()
+    oracle.transpose_add_into(M, N, A, N + pad, want, M + pad)
+    dB = dev(B)
+    gbblas.transpose_add(M, N, dev(A), N + pad, dB, M + pad, bits)
+    assert host(dB).tobytes() == want.tobytes()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("M,N,iters", [(1, 1, 1), (33, 47, 2), (200, 333, 9), (300, 500, 13), (257, 1000, 4),
+                                      (130, 113, 7)])
+def test_stencil9_bit_exact(torch, dtype, M, N, iters):
+    """9-point stencil, arbitrary 3x3 weights: bit-identical to the
+    product-then-eight-fmas recurrence, several sweeps per pass."""
+    import gbblas
+    rng = np.random.default_rng(M * 7 + N)
+    w = rng.uniform(-0.3, 0.4, size=9).astype(dtype)
+    A = np.ones((M + 2, N + 2), dtype=dtype)
+    A[1:M + 1, 1:N + 1] = oracle.fill(M, N, 19, kind=1, dtype=dtype)
+    B = A.copy()
+    a, b = A.copy(), B.copy()
+    oracle.stencil9(M, N, a, b, iters, w)
+    dA, dB = dev(A), dev(B)
+    gbblas.stencil9(M, N, dA, dB, iters, w, 64 if dtype == np.float64 else 32)
+    res, want = (host(dB), b) if iters % 2 else (host(dA), a)
+    assert res.tobytes() == want.tobytes()
+    other = host(dA) if iters % 2 else host(dB)
+    for edge in (np.s_[0, :], np.s_[-1, :], np.s_[:, 0], np.s_[:, -1]):
+        assert other[edge].tobytes() == A[edge].tobytes()

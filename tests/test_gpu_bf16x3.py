@@ -229,3 +229,32 @@ def test_bf16x6_error_tracks_simt(torch):
         errs[name], _ = oracle.normwise_error(host(dC), "N", "N", M, N, K, 1.0, A, K, B, N, 0.0, C0, N, rows, cols)
     assert errs["x6"] <= 2 * errs["simt"], errs
     assert errs["x6"] * 4 <= errs["x3"], errs
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("M,N,K", [(4096, 4096, 320), (2048, 4096, 96), (4000, 3900, 1000)])
+def test_bf16x3_stream_k_tail_exact(torch, mode, M, N, K):
+    """Tile counts that leave a partial last wave, with the stream-K tail
+    switched on (GB_BF16X3_SK=1): the tail tiles are split in K over two CTAs
+    and summed by the second finisher.  Small integers keep every partial sum
+    exact, so the result must equal the exact product."""
+    import os
+    import gbblas
+    os.environ["GB_BF16X3_SK"] = "1"
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A, B = _ints(ar, ac, 31), _ints(br, bc, 32)
+    C0 = _ints(M, N, 33)
+    opA = A.T if ta == "T" else A
+    opB = B.T if tb == "T" else B
+    want = (opA.astype(np.float64) @ opB.astype(np.float64) - 2.0 * C0).astype(np.float32)
+    try:
+        for _ in range(2):   # twice: the part counters must be back at zero
+            dC = dev(C0)
+            gbblas.sgemm(ta, tb, M, N, K, 1.0, dev(A), ac, dev(B), bc, -2.0, dC, N, algo=gbblas.ALGO_BF16X3)
+            got = host(dC)
+            bad = np.argwhere(got != want)
+            assert bad.size == 0, (mode, bad[:5])
+    finally:
+        os.environ.pop("GB_BF16X3_SK", None)

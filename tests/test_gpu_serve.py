@@ -187,3 +187,22 @@ def test_autotune_picks_a_working_algorithm(torch):
     assert gbblas.lib().gb_autotune_get(32, b"N", b"N", 1024, 1024, 1024) == best
     best64, _ = gbblas.autotune_gemm(64, "N", "N", 600, 600, 600)
     assert best64 in (gbblas.ALGO_ORDERED, gbblas.ALGO_OZAKI)
+
+
+def test_strided_batched_matches_single_calls(torch):
+    """gb_gemm_strided_batched: 37 equal-shape GEMMs through the grouped kernel
+    equal 37 single gb_dgemm calls with the ordered algorithm on FP64 within
+    the normwise bound, and shared operands (stride 0) work."""
+    import gbblas
+    batch, M, N, K = 37, 70, 90, 130
+    A = oracle.fill(batch * M, K, 71, dtype=np.float64)
+    B = oracle.fill(K, N, 72, dtype=np.float64)            # shared: strideB = 0
+    C0 = oracle.fill(batch * M, N, 73, dtype=np.float64)
+    dC = dev(C0)
+    gbblas.gemm_strided_batched(64, "N", "N", M, N, K, 1.25, dev(A), K, M * K, dev(B), N, 0, -0.5, dC, N, M * N,
+                                batch)
+    got = host(dC)
+    for i in range(batch):
+        Ai, Ci = A[i * M:(i + 1) * M], C0[i * M:(i + 1) * M]
+        err, _ = oracle.normwise_error(got[i * M:(i + 1) * M], "N", "N", M, N, K, 1.25, Ai, K, B, N, -0.5, Ci, N)
+        assert err <= 2 * K * 2.0 ** -53, (i, err)

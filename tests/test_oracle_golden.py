@@ -99,3 +99,23 @@ def test_dot2_beats_naive_on_ill_conditioned():
     y = np.array([1.0, 1.0, 1.0]).reshape(3, 1)
     ref = oracle.gemm_dot2("N", "N", 1, 1, 3, 1.0, x, 3, y, 1, 0.0, None, 1, [0], [0])
     assert ref[0, 0] == 1.0
+
+
+def test_stencil9_reduces_to_weighted_sum():
+    """The 9-point oracle on a tiny grid against a direct numpy evaluation in
+    the same fused order (numpy has no fma, so compare with a tolerance and
+    check the halo is untouched)."""
+    import numpy as np
+    M, N = 5, 6
+    rng = np.random.default_rng(3)
+    w = rng.uniform(-1, 1, size=9)
+    A = rng.uniform(0, 1, size=(M + 2, N + 2))
+    B = A.copy()
+    a, b = A.copy(), B.copy()
+    oracle.stencil9(M, N, a, b, 1, w)
+    ref = np.zeros((M, N))
+    for di in range(3):
+        for dj in range(3):
+            ref += w[di * 3 + dj] * A[di:di + M, dj:dj + N]
+    assert np.allclose(b[1:M + 1, 1:N + 1], ref, rtol=0, atol=1e-14)
+    assert np.array_equal(b[0], B[0]) and np.array_equal(b[:, 0], B[:, 0])
