@@ -246,6 +246,7 @@ struct TwoPass {
 // tensor maps of the A and B pieces (hi, lo[, lo2])
 struct PieceMaps {
     CUtensorMap a[3], b[3];
+    CUtensorMap bh[3];   // B pieces with 128-row boxes (half tiles of the tail wave)
 };
 
 struct EpiParams {
@@ -265,16 +266,33 @@ struct EpiParams {
     int dp_tiles;
     float *sk_part;
     int *sk_cnt;
+    // Half-tile tail: tiles [half_start, tiles) (a last wave at most half
+    // full) run as two 128-column halves on different CTAs, so the wave takes
+    // half a tile time.
+    int half_start;
 };
 
-// Work items of one CTA: (tile, k-blocks [kb0, kb1)).
+// Work items of one CTA: (tile, k-blocks [kb0, kb1), half: -1 whole tile,
+// 0 / 1 the left / right 128 columns).
 struct WorkIt {
     int i;
     int64_t pos, end;   // stream-K position / end in (tile - dp_tiles) * num_kb + kb
 };
 
 __device__ __forceinline__ bool next_item(const EpiParams &p, int num_tiles, WorkIt &w, int &tile, int &kb0,
-                                          int &kb1) {
+                                          int &kb1, int &half) {
+    half = -1;
+    if (p.half_start < num_tiles) {   // whole tiles, then the tail in halves
+        const int t = blockIdx.x + w.i * gridDim.x;
+        w.i++;
+        kb0 = 0; kb1 = p.num_kb;
+        if (t < p.half_start) { tile = t; return true; }
+        const int h = t - p.half_start;
+        if (h >= 2 * (num_tiles - p.half_start)) return false;
+        tile = p.half_start + h / 2;
+        half = h & 1;
+        return true;
+    }
     if (w.pos < 0) {
         const int t = blockIdx.x + w.i * gridDim.x;
         if (t < p.dp_tiles) {
@@ -373,11 +391,12 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
             int kbg = 0;   // running k-block counter across tiles (stage / phase)
             bool go = true;
             WorkIt wi{0, -1, 0};
-            int t, kbA, kbB;
-            while (go && next_item(p, num_tiles, wi, t, kbA, kbB)) {
+            int t, kbA, kbB, half;
+            while (go && next_item(p, num_tiles, wi, t, kbA, kbB, half)) {
                 int tm, tn;
                 tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-                const int m0 = tm * BM, n0 = tn * BN;
+                const int m0 = tm * BM, n0 = tn * BN + (half > 0 ? BN / 2 : 0);
+                const uint32_t bytes = half < 0 ? STAGE_BYTES : NP * A_TILE + NP * (B_TILE / 2);
                 for (int kb = kbA; kb < kbB; kb++, kbg++) {
                     const int s = kbg % STAGES;
                     if (kbg >= STAGES && !ptx::mbar_wait(&empty[s], ((kbg / STAGES) & 1) ^ 1, p.err, 1)) {
@@ -385,11 +404,12 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                         break;
                     }
                     uint8_t *st = smem + s * STAGE_BYTES;
-                    ptx::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+                    ptx::mbar_arrive_expect_tx(&full[s], bytes);
 #pragma unroll
                     for (int i = 0; i < NP; i++) {
                         ptx::tma_load_2d(st + i * A_TILE, &maps.a[i], &full[s], kb * BK, m0);
-                        ptx::tma_load_2d(st + NP * A_TILE + i * B_TILE, &maps.b[i], &full[s], kb * BK, n0);
+                        ptx::tma_load_2d(st + NP * A_TILE + i * B_TILE, half < 0 ? &maps.b[i] : &maps.bh[i],
+                                         &full[s], kb * BK, n0);
                     }
                 }
             }
@@ -400,9 +420,11 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
             int kbg = 0, ch = 0;   // running k-block and accumulator-chunk counters
             (void)B_TILE;
             bool go = true;
+            constexpr uint32_t idesc_half = ptx::idesc_bf16_f32(BM, BN / 2);
             WorkIt wi{0, -1, 0};
-            int t, kbA, kbB;
-            while (go && next_item(p, num_tiles, wi, t, kbA, kbB)) {
+            int t, kbA, kbB, half;
+            while (go && next_item(p, num_tiles, wi, t, kbA, kbB, half)) {
+                const uint32_t id = half < 0 ? idesc : idesc_half;
                 const int nch = (kbB - kbA + chunk_kb - 1) / chunk_kb;
                 for (int c = 0; c < nch && go; c++, ch++) {
                     const int b = ch & 1;
@@ -437,7 +459,7 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
 #pragma unroll
                                 for (int i = d; i >= 0; i--) {
                                     const bool lead = FOLD ? (d == NP - 1 && i == d) || d == 0 : d == NP - 1 && i == d;
-                                    ptx::umma_f16(d == 0 ? acc : acc_lo, ad[i] + dk, bd[d - i] + dk, idesc,
+                                    ptx::umma_f16(d == 0 ? acc : acc_lo, ad[i] + dk, bd[d - i] + dk, id,
                                                   !(first && k == 0 && lead));
                                 }
                         }
@@ -456,12 +478,13 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
         bool go = true;
         __shared__ int sk_last;
         WorkIt wi{0, -1, 0};
-        int t, kbA, kbB;
-        while (go && next_item(p, num_tiles, wi, t, kbA, kbB)) {
+        int t, kbA, kbB, half;
+        while (go && next_item(p, num_tiles, wi, t, kbA, kbB, half)) {
             int tm, tn;
             tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
             const int64_t row0 = (int64_t)tm * BM + q * 32;
-            const int64_t n0 = (int64_t)tn * BN;
+            const int64_t n0 = (int64_t)tn * BN + (half > 0 ? BN / 2 : 0);
+            const int ncols = half < 0 ? BN : BN / 2;
             // a stream-K part: raw accumulator to its slot, C written by the second finisher
             const bool part = !FOLD && (kbA != 0 || kbB != p.num_kb);
             const int sk_b = kbA == 0 ? (int)blockIdx.x : (int)blockIdx.x - 1;
@@ -498,6 +521,7 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
             }
 #pragma unroll
             for (int c = 0; c < BN; c += 32) {
+                if (c >= ncols) break;
                 // thread `lane` holds row row0+lane, columns c..c+31: transpose through
                 // shared memory so each store instruction writes one row contiguously
                 if (FOLD) {
@@ -982,8 +1006,17 @@ static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64
     const int grid = tiles < sm_count() ? tiles : sm_count();
     const int dp = sk_part ? stream_k_dp_tiles(tiles, grid, FOLD) : tiles;
     if (dp < tiles) GB_CUDA_TRY(cudaMemsetAsync(sk_cnt, 0, (size_t)grid * sizeof(int), g.stream));
+    // half-tile tail when the last wave is at most half full (whole tiles
+    // would leave most of the GPU idle for a tile time); GB_BF16X3_HALF=0 off
+    int half_start = tiles;
+    {
+        const char *e = getenv("GB_BF16X3_HALF");
+        const int rem = tiles % grid;
+        if (!FOLD && BN == 256 && dp == tiles && !(e && e[0] == '0') && rem > 0 && 2 * rem <= grid)
+            half_start = tiles - rem;
+    }
     EpiParams p{(float *)g.C, g.M, g.N, g.ldc, (float)g.alpha, (float)g.beta, g.semantics, (int)(kp / BK),
-                tiles_m, tiles_n, err, FOLD ? fold_kb : 1, dp, sk_part, sk_cnt};
+                tiles_m, tiles_n, err, FOLD ? fold_kb : 1, dp, sk_part, sk_cnt, half_start};
     bf16x3_gemm_kernel<NP, BN, FOLD><<<grid, NT, CF::SMEM_BYTES, g.stream>>>(maps, p);
     GB_LAUNCH_CHECK("bf16x3_gemm_kernel");
     return ok();
@@ -1044,6 +1077,7 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
     for (int i = 0; i < np; i++) {
         okm = okm && make_tmap_bf16(&maps.a[i], ap[i], kp, g.M, kp * 2, BK, BM, 64);
         okm = okm && make_tmap_bf16(&maps.b[i], bp[i], kp, g.N, kp * 2, BK, bn, 64);
+        okm = okm && make_tmap_bf16(&maps.bh[i], bp[i], kp, g.N, kp * 2, BK, bn / 2, 64);
     }
     if (!okm) return set_status(GB_ERR_CUDA, "bf16x3: cuTensorMapEncodeTiled failed");
     if (np == 3)

@@ -258,3 +258,24 @@ def test_bf16x3_stream_k_tail_exact(torch, mode, M, N, K):
             assert bad.size == 0, (mode, bad[:5])
     finally:
         os.environ.pop("GB_BF16X3_SK", None)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("M,N,K", [(4096, 4096, 96), (1152, 4352, 64), (300, 700, 128)])
+def test_bf16x3_half_tile_tail_exact(torch, mode, M, N, K):
+    """A last wave at most half full runs as 128-column half tiles (N = 128
+    MMAs on the first half of the B stage); small integers: exact."""
+    import gbblas
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A, B = _ints(ar, ac, 41), _ints(br, bc, 42)
+    C0 = _ints(M, N, 43)
+    opA = A.T if ta == "T" else A
+    opB = B.T if tb == "T" else B
+    want = (3.0 * (opA.astype(np.float64) @ opB.astype(np.float64)) + 1.0 * C0).astype(np.float32)
+    dC = dev(C0)
+    gbblas.sgemm(ta, tb, M, N, K, 3.0, dev(A), ac, dev(B), bc, 1.0, dC, N, algo=gbblas.ALGO_BF16X3)
+    got = host(dC)
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (mode, bad[:5])
