@@ -125,60 +125,6 @@ __global__ void __launch_bounds__(NT) stencil_tb_kernel(const T *__restrict__ sr
 // same add order as one sweep at a time, so results are bit-identical.
 constexpr int RS_W = 128, RS_SEG = 256, RS_NT = 256;
 
-// The row walk of one warp of stencil_rs_kernel: input row i enters level 0,
-// level l+1 computes row i - l - 1 from the last two rows of level l and the
-// new one, and level T's row i - T is stored.
-template <typename E, int T, int ORDER, bool INTERIOR>
-__device__ __forceinline__ void rs_walk(const E *__restrict__ src, E *__restrict__ dst, int64_t M, int64_t ld,
-                                        int64_t cl, int64_t out_r0, int64_t out_r1, const bool (&cfix)[4],
-                                        const bool (&cload)[4], const bool (&cstore)[4]) {
-    E p2[T][4], p1[T][4];   // level l-1 rows rho-1 and rho of level l's window
-#pragma unroll
-    for (int l = 0; l < T; l++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) p2[l][q] = p1[l][q] = E(0);
-
-    for (int64_t i = out_r0 - T - 1; i < out_r1 + T; i++) {   // input row i (level 0)
-        E x[4] = {E(0), E(0), E(0), E(0)};
-        if (INTERIOR || (i >= 0 && i <= M + 1)) {
-            const E *row = src + i * ld + cl;
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (INTERIOR || cload[q]) x[q] = __ldg(row + q);
-        }
-#pragma unroll
-        for (int l = 0; l < T; l++) {
-            // level l+1, row rho = i - l - 1: top p2[l], middle p1[l], down x
-            const int64_t gr = i - l - 1;
-            const E left0 = __shfl_up_sync(0xffffffffu, p1[l][3], 1);
-            const E right3 = __shfl_down_sync(0xffffffffu, p1[l][0], 1);
-            const bool rfix = !INTERIOR && (gr <= 0 || gr >= M + 1);
-            E v[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const E lft = q == 0 ? left0 : p1[l][q - 1];
-                const E rgt = q == 3 ? right3 : p1[l][q + 1];
-                const E u = update<E, ORDER>(p2[l][q], lft, rgt, x[q], p1[l][q], gr - 1);
-                v[q] = INTERIOR ? u : ((rfix || cfix[q]) ? p1[l][q] : u);
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                p2[l][q] = p1[l][q];
-                p1[l][q] = x[q];
-                x[q] = v[q];
-            }
-        }
-        // x: level T, row i - T
-        const int64_t ro = i - T;
-        if (ro >= out_r0 && ro < out_r1) {
-            E *row = dst + ro * ld + cl;
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (cstore[q]) row[q] = x[q];
-        }
-    }
-}
-
 template <typename E, int T, int ORDER>
 __global__ void __launch_bounds__(RS_NT) stencil_rs_kernel(const E *__restrict__ src, E *__restrict__ dst,
                                                            int64_t M, int64_t N, int strips, int segs) {
@@ -202,11 +148,50 @@ __global__ void __launch_bounds__(RS_NT) stencil_rs_kernel(const E *__restrict__
         cstore[q] = lc >= T && lc < RS_W - T && gc >= 1 && gc <= N;
     }
 
-    // warps whose whole domain (input rows and strip columns) lies inside the
-    // grid interior need no boundary selects and no load guards
-    const bool interior = c0 >= 1 && c0 + RS_W - 1 <= N && out_r0 - T - 1 >= 1 && out_r1 + T - 1 <= M;
-    if (interior) rs_walk<E, T, ORDER, true>(src, dst, M, ld, cl, out_r0, out_r1, cfix, cload, cstore);
-    else rs_walk<E, T, ORDER, false>(src, dst, M, ld, cl, out_r0, out_r1, cfix, cload, cstore);
+    E p2[T][4], p1[T][4];   // level l-1 rows rho-1 and rho of level l's window
+#pragma unroll
+    for (int l = 0; l < T; l++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) p2[l][q] = p1[l][q] = E(0);
+
+    for (int64_t i = out_r0 - T - 1; i < out_r1 + T; i++) {   // input row i (level 0)
+        E x[4] = {E(0), E(0), E(0), E(0)};
+        if (i >= 0 && i <= M + 1) {
+            const E *row = src + i * ld + cl;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (cload[q]) x[q] = __ldg(row + q);
+        }
+#pragma unroll
+        for (int l = 0; l < T; l++) {
+            // level l+1, row rho = i - l - 1: top p2[l], middle p1[l], down x
+            const int64_t gr = i - l - 1;
+            const E left0 = __shfl_up_sync(0xffffffffu, p1[l][3], 1);
+            const E right3 = __shfl_down_sync(0xffffffffu, p1[l][0], 1);
+            const bool rfix = gr <= 0 || gr >= M + 1;
+            E v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const E lft = q == 0 ? left0 : p1[l][q - 1];
+                const E rgt = q == 3 ? right3 : p1[l][q + 1];
+                v[q] = (rfix || cfix[q]) ? p1[l][q] : update<E, ORDER>(p2[l][q], lft, rgt, x[q], p1[l][q], gr - 1);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                p2[l][q] = p1[l][q];
+                p1[l][q] = x[q];
+                x[q] = v[q];
+            }
+        }
+        // x: level T, row i - T
+        const int64_t ro = i - T;
+        if (ro >= out_r0 && ro < out_r1) {
+            E *row = dst + ro * ld + cl;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (cstore[q]) row[q] = x[q];
+        }
+    }
 }
 
 template <typename E, int T>
