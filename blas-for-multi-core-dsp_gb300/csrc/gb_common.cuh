@@ -113,6 +113,13 @@ int64_t thin_tc_stages(int64_t K, bool classes);       // 64-k stages per row ti
 size_t thin_tc_wpieces_bytes(int nb, int64_t K, bool classes);
 gb_status launch_thin_tc(const ThinTcArgs &a);
 
+// FP64 skinny product from integer digits on the tensor cores (skinny_oz.cu).
+bool thin_oz_eligible(int tx, int64_t ldx, const void *X, int64_t rows, int64_t K);
+size_t thin_oz_workspace_bytes(int64_t rows, int64_t K, int n, int splits);
+gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, int tx, const double *W, int64_t ldw,
+                         int tw, int n, double *C, int64_t cs_r, int64_t cs_c, double alpha, double beta,
+                         int semantics, int splits, int64_t kchunk, void *ws, cudaStream_t st);
+
 gb_status launch_skinny_f32(const GemmArgs &g);
 gb_status launch_skinny_f64(const GemmArgs &g);
 // C = beta*C (beta==0: C = 0) or C = C + beta (scalar) epilogue-only path (K == 0)

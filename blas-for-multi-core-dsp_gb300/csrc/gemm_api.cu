@@ -53,12 +53,12 @@ int pick(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
     const int64_t large = M < N ? N : M;
     const double work = (double)M * (double)N * (double)K;
     if (bits == 64) {
-        // Ozaki pads the small side of a skinny product to 128: below 32 the
-        // native FP64 streaming kernel is faster
+        // FP64 skinny: the skinny path streams X once, cutting it into digits
+        // for the tensor cores (the general Ozaki form would pad the small
+        // side to 128 and re-read its slices for every slice pair)
         const bool skinny = small <= 64 && large >= 4 * small && large >= 1024;
-        if (skinny && small < 32) return GB_ALGO_SKINNY;
-        if (work > 134217728.0) return GB_ALGO_OZAKI;   // 2^27 = 512^3
         if (skinny) return GB_ALGO_SKINNY;
+        if (work > 134217728.0) return GB_ALGO_OZAKI;   // 2^27 = 512^3
         return GB_ALGO_ORDERED;
     }
     // FP32 skinny: the skinny path streams X once (FFMA up to n = 8, 3xBF16

@@ -85,6 +85,22 @@ bool make_tmap_f32(CUtensorMap *map, const void *base, uint64_t inner, uint64_t 
     return r == CUDA_SUCCESS;
 }
 
+// 2-D FP64 tensor [outer][inner], box box_inner x box_outer, no swizzle or
+// 128-byte swizzle (box_inner * 8 must then be 128).
+bool make_tmap_f64(CUtensorMap *map, const void *base, uint64_t inner, uint64_t outer, uint64_t row_bytes,
+                   uint32_t box_inner, uint32_t box_outer, bool sw128) {
+    PFN_encodeTiled enc = encode_fn();
+    if (!enc) return false;
+    cuuint64_t dims[2] = {inner, outer};
+    cuuint64_t strides[1] = {row_bytes};
+    cuuint32_t box[2] = {box_inner, box_outer};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void *>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, sw128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 namespace {
 
 // ------------------------------------------------------------------ split

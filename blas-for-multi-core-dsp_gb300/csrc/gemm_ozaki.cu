@@ -393,6 +393,18 @@ __global__ void __launch_bounds__(NT, 1)
 
 static gb_status ozaki_one(const GemmArgs &g, int s);
 
+// Exponents e of `lines` lines of `len` FP64 values (max |x| < 2^e, 0 for an
+// all-zero line): line i at X + i*ld (contiguous) or, strided, element k of
+// line i at X[k*ld + i].
+gb_status ozaki_line_exponents(const double *X, int64_t ld, bool strided, int64_t lines, int64_t len, int *e,
+                               cudaStream_t st) {
+    if (lines <= 0) return ok();
+    if (!strided) maxexp_contig_kernel<<<(unsigned)ceil_div(lines, 8), 256, 0, st>>>(X, ld, lines, len, e);
+    else maxexp_strided_kernel<<<(unsigned)ceil_div(lines, 256), 256, 0, st>>>(X, ld, lines, len, e);
+    GB_LAUNCH_CHECK("ozaki exponents");
+    return ok();
+}
+
 // Slices of both operands take s * (Mp + Np) * Kp * 2 bytes of workspace.
 // Past kWorkspaceCap the K range is cut into chunks, each sliced and
 // multiplied on its own and accumulated into C (beta applied by the first

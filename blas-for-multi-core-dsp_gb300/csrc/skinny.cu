@@ -856,6 +856,20 @@ gb_status dispatch(const GemmArgs &g) {
     p.K = g.K; p.C = g.C; p.alpha = g.alpha; p.beta = g.beta; p.semantics = g.semantics;
     if (p.n > 64) return set_status(GB_ERR_UNSUPPORTED, "skinny: small dimension %lld > 64",
                                     (long long)(g.M < g.N ? g.M : g.N));
+    if (sizeof(T) == 8 && thin_oz_eligible(p.tx, p.ldx, p.X, p.rows, p.K)) {
+        // FP64: digits on the tensor cores; units of 128 rows x K chunks of
+        // 512, split K until there are ~4 units per SM
+        const int64_t rtiles = ceil_div(p.rows, 128), nchunks = ceil_div(p.K, 512);
+        int splits = 1;
+        while (rtiles * splits < 4 * (int64_t)sm_count() && nchunks / (splits * 2) >= 2 && splits < 64) splits *= 2;
+        const int64_t cpc = ceil_div(nchunks, splits);
+        splits = (int)ceil_div(nchunks, cpc);
+        void *ws = workspace(thin_oz_workspace_bytes(p.rows, p.K, p.n, splits), g.stream);
+        if (!ws) return (gb_status)gb_get_last_status();
+        return launch_thin_oz(p.rows, p.K, (const double *)p.X, p.ldx, p.tx, (const double *)p.W, p.ldw, p.tw, p.n,
+                              (double *)p.C, p.cs_r, p.cs_c, p.alpha, p.beta, p.semantics, splits, cpc * 512, ws,
+                              g.stream);
+    }
     if (p.n <= 8) return run<T, 8>(p, g.stream);
     if (p.n <= 16) return run<T, 16>(p, g.stream);
     if (p.n <= 32) return run<T, 32>(p, g.stream);

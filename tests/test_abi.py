@@ -103,7 +103,7 @@ def test_auto_algorithm_choice(L):
     assert gbblas.pick_algo(32, "N", "N", 262144, 8, 4096) == gbblas.ALGO_SKINNY
     assert gbblas.pick_algo(32, "N", "N", 262144, 64, 4096) == gbblas.ALGO_SKINNY
     assert gbblas.pick_algo(64, "T", "T", 16, 262144, 4096) == gbblas.ALGO_SKINNY
-    assert gbblas.pick_algo(64, "T", "T", 48, 262144, 4096) == gbblas.ALGO_OZAKI
+    assert gbblas.pick_algo(64, "T", "T", 48, 262144, 4096) == gbblas.ALGO_SKINNY
     assert gbblas.pick_algo(64, "T", "T", 16, 2000, 1000) == gbblas.ALGO_SKINNY
     assert gbblas.pick_algo(64, "N", "N", 512, 512, 512) == gbblas.ALGO_ORDERED
     assert gbblas.pick_algo(64, "N", "N", 1024, 1024, 1024) == gbblas.ALGO_OZAKI

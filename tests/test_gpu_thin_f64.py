@@ -1,0 +1,111 @@
+"""FP64 skinny products (thinB / shortA, n <= 64) through integer digits on
+the tensor cores, against the oracle.
+
+* Small-integer inputs: every digit product and every level sum is an exact
+  integer, so the result must equal the exact product bit for bit -- this
+  pins the FP64 tensor-map boxes, the digit slices in tensor memory, the 36
+  digit pairs into 8 level accumulators, the column passes of 16 and the
+  split-K parts.
+* U[-1,1] and wide-exponent (u * 2^e, e in [-20, 20]) inputs: normwise error
+  against the Dot2 oracle within 2*K*u64, and against the native FP64
+  kernels (GB_SKINNY_OZ=0) within the same bound.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from gpu_util import dev, host, op_shape, torch_cuda
+
+pytestmark = pytest.mark.gpu
+MODES = ["NN", "NT", "TN", "TT"]
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return torch_cuda()
+
+
+def _ints(rows, cols, seed, ld):
+    rng = np.random.default_rng(seed)
+    X = np.zeros((rows, ld), dtype=np.float64)
+    X[:, :cols] = rng.integers(-40, 41, size=(rows, cols)).astype(np.float64)
+    return X
+
+
+def _ld(c):
+    return max(2, (c + 1) // 2 * 2)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("kind", ["thinB", "shortA"])
+@pytest.mark.parametrize("small,big,K", [(8, 3001, 1037), (16, 700, 96), (5, 1000, 640), (33, 257, 4099),
+                                         (64, 2000, 600), (12, 60, 9000)])
+@pytest.mark.parametrize("sem", [0, 2])
+def test_thin_f64_exact_on_integers(torch, mode, kind, small, big, K, sem):
+    import gbblas
+    ta, tb = mode
+    M, N = (big, small) if kind == "thinB" else (small, big)
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    lda, ldb, ldc = _ld(ac), _ld(bc), N + 1
+    A, B = _ints(ar, ac, 1, lda), _ints(br, bc, 2, ldb)
+    C0 = _ints(M, N, 3, ldc)
+    opA = A[:, :ac].T if ta == "T" else A[:, :ac]
+    opB = B[:, :bc].T if tb == "T" else B[:, :bc]
+    prod = opA @ opB        # integers below 2^53: exact in FP64
+    want = C0.copy()
+    if sem == 0:
+        want[:, :N] = -1.0 * prod + 2.0 * C0[:, :N]
+    else:
+        want[:, :N] = C0[:, :N] + (-1.0 * prod + 2.0)
+    dC = dev(C0)
+    gbblas.dgemm(ta, tb, M, N, K, -1.0, dev(A), lda, dev(B), ldb, 2.0, dC, ldc, algo=gbblas.ALGO_SKINNY,
+                 semantics=sem)
+    got = host(dC)
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (mode, kind, bad[:5])
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("kind", ["thinB", "shortA"])
+@pytest.mark.parametrize("small,fill", [(8, 0), (24, 2), (64, 0)])
+def test_thin_f64_normwise_and_matches_native(torch, mode, kind, small, fill):
+    import gbblas
+    ta, tb = mode
+    big, K = 4000, 2049
+    M, N = (big, small) if kind == "thinB" else (small, big)
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    lda, ldb, ldc = _ld(ac), _ld(bc), N
+    A = oracle.fill(ar, ac, 81, kind=fill, dtype=np.float64, ld=lda)
+    B = oracle.fill(br, bc, 82, kind=fill, dtype=np.float64, ld=ldb)
+    C0 = oracle.fill(M, N, 83, kind=fill, dtype=np.float64, ld=ldc)
+    outs = []
+    for oz in ("1", "0"):
+        os.environ["GB_SKINNY_OZ"] = oz
+        try:
+            dC = dev(C0)
+            gbblas.dgemm(ta, tb, M, N, K, 0.75, dev(A), lda, dev(B), ldb, -0.5, dC, ldc, algo=gbblas.ALGO_SKINNY)
+            outs.append(host(dC))
+        finally:
+            os.environ.pop("GB_SKINNY_OZ", None)
+    rows = np.arange(0, M, max(1, M // 53))
+    cols = np.arange(0, N, max(1, N // 53))
+    for got in outs:
+        err, _ = oracle.normwise_error(got, ta, tb, M, N, K, 0.75, A, lda, B, ldb, -0.5, C0, ldc, rows, cols)
+        assert err <= 2 * K * 2.0 ** -53, err
+
+
+def test_thin_f64_deterministic(torch):
+    import gbblas
+    M, N, K = 3000, 20, 20000
+    A = oracle.fill(M, K, 91, dtype=np.float64)
+    B = oracle.fill(K, N, 92, dtype=np.float64)
+    outs = []
+    for _ in range(2):
+        dC = dev(np.zeros((M, N), np.float64))
+        gbblas.dgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=gbblas.ALGO_SKINNY)
+        outs.append(host(dC))
+    assert outs[0].tobytes() == outs[1].tobytes()
