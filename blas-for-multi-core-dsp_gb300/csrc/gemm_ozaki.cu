@@ -29,6 +29,7 @@
 // (alternating per chunk), warps 2-5 drain them into int32 registers and the
 // FP64 sum in TMEM, and write C.
 #include <cuda.h>
+#include <limits.h>
 #include <cuda_bf16.h>
 
 #include "gb_common.cuh"
@@ -95,18 +96,55 @@ __global__ void maxexp_contig_kernel(const double *__restrict__ X, int64_t ld, i
     if (lane == 0) e[line] = exp_of_maxbits(mb);
 }
 
-// one thread per column j of a len x cols storage (rows strided by ld)
-__global__ void maxexp_strided_kernel(const double *__restrict__ X, int64_t ld, int64_t cols, int64_t len,
-                                      int *__restrict__ e) {
-    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= cols) return;
+// Column exponents of a len x cols storage (rows strided by ld), in three
+// small kernels: e[] = INT_MIN; each block reduces 32 consecutive columns
+// (lane = column, coalesced) over kpb rows and raises e[col] to the
+// exponent of its maximum (exponents are monotone in |x|, so the maximum of
+// the partial exponents is the exponent of the maximum; an all-zero part
+// contributes INT_MIN); INT_MIN (an all-zero column) -> 0.
+__global__ void exp_init_kernel(int *__restrict__ e, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        e[i] = INT_MIN;
+}
+
+__global__ void __launch_bounds__(256) maxexp_strided_kernel(const double *__restrict__ X, int64_t ld, int64_t cols,
+                                                             int64_t len, int64_t kpb, int *__restrict__ e) {
+    __shared__ unsigned long long part[8][32];
+    const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+    const int64_t j = (int64_t)blockIdx.x * 32 + lane;
+    const int64_t k0 = (int64_t)blockIdx.y * kpb;
     unsigned long long mb = 0;
-    const unsigned long long *p = reinterpret_cast<const unsigned long long *>(X);
-    for (int64_t k = 0; k < len; k++) {
-        unsigned long long b = __ldg(p + k * ld + j) & 0x7FFFFFFFFFFFFFFFull;
-        mb = b > mb ? b : mb;
+    if (j < cols) {
+        const unsigned long long *p = reinterpret_cast<const unsigned long long *>(X);
+        const int64_t k1 = k0 + kpb < len ? k0 + kpb : len;
+#pragma unroll 8
+        for (int64_t k = k0 + w; k < k1; k += 8) {
+            const unsigned long long b = __ldg(p + k * ld + j) & 0x7FFFFFFFFFFFFFFFull;
+            mb = b > mb ? b : mb;
+        }
     }
-    e[j] = exp_of_maxbits(mb);
+    part[w][lane] = mb;
+    __syncthreads();
+    if (w == 0 && j < cols) {
+#pragma unroll
+        for (int i = 1; i < 8; i++) mb = part[i][lane] > mb ? part[i][lane] : mb;
+        if (mb != 0) atomicMax(e + j, exp_of_maxbits(mb));
+    }
+}
+
+__global__ void exp_finish_kernel(int *__restrict__ e, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (e[i] == INT_MIN) e[i] = 0;
+}
+
+static void launch_maxexp_strided(const double *X, int64_t ld, int64_t cols, int64_t len, int *e, cudaStream_t st) {
+    const unsigned nb = (unsigned)(ceil_div(cols, 256) < 4096 ? ceil_div(cols, 256) : 4096);
+    exp_init_kernel<<<nb, 256, 0, st>>>(e, cols);
+    int64_t kpb = 256;   // rows per block; more when len would need over 65535 blocks in y
+    while (ceil_div(len, kpb) > 65535) kpb *= 2;
+    dim3 grid((unsigned)ceil_div(cols, 32), (unsigned)ceil_div(len, kpb));
+    maxexp_strided_kernel<<<grid, 256, 0, st>>>(X, ld, cols, len, kpb, e);
+    exp_finish_kernel<<<nb, 256, 0, st>>>(e, cols);
 }
 
 // ---------------------------------------------------------------- digits
@@ -400,7 +438,7 @@ gb_status ozaki_line_exponents(const double *X, int64_t ld, bool strided, int64_
                                cudaStream_t st) {
     if (lines <= 0) return ok();
     if (!strided) maxexp_contig_kernel<<<(unsigned)ceil_div(lines, 8), 256, 0, st>>>(X, ld, lines, len, e);
-    else maxexp_strided_kernel<<<(unsigned)ceil_div(lines, 256), 256, 0, st>>>(X, ld, lines, len, e);
+    else launch_maxexp_strided(X, ld, lines, len, e, st);
     GB_LAUNCH_CHECK("ozaki exponents");
     return ok();
 }
@@ -456,13 +494,13 @@ static gb_status ozaki_one(const GemmArgs &g, int s) {
     if (!g.ta) {
         maxexp_contig_kernel<<<(unsigned)ceil_div(g.M, 8), 256, 0, g.stream>>>(A, g.lda, g.M, g.K, erow);
     } else {
-        maxexp_strided_kernel<<<(unsigned)ceil_div(g.M, 256), 256, 0, g.stream>>>(A, g.lda, g.M, g.K, erow);
+        launch_maxexp_strided(A, g.lda, g.M, g.K, erow, g.stream);
     }
     GB_LAUNCH_CHECK("ozaki exponents A");
     if (g.tb) {
         maxexp_contig_kernel<<<(unsigned)ceil_div(g.N, 8), 256, 0, g.stream>>>(B, g.ldb, g.N, g.K, fcol);
     } else {
-        maxexp_strided_kernel<<<(unsigned)ceil_div(g.N, 256), 256, 0, g.stream>>>(B, g.ldb, g.N, g.K, fcol);
+        launch_maxexp_strided(B, g.ldb, g.N, g.K, fcol, g.stream);
     }
     GB_LAUNCH_CHECK("ozaki exponents B");
 

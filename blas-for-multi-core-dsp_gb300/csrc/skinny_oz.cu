@@ -17,12 +17,13 @@
 //           digit slices of W (small);
 //   pass 2 (thin_oz_kernel, per 16 columns of W):
 //     warp 0     TMA: 128 rows x 32 k of X (FP64) + the 8 digit tiles of W;
-//     warps 2-5  converters, one per TMEM lane quarter, thread = row: the
-//                row's 32 values -> 8 digit slices written into tensor memory
-//                (the A operand of the MMA, never in shared memory);
+//     warps 2-9  converters, two per TMEM lane quarter (one per 16-k box),
+//                thread = row: the row's values -> 8 digit slices written
+//                into tensor memory (the A operand of the MMA, never in
+//                shared memory);
 //     warp 1     MMA: the 36 digit pairs t + u <= 9 into 8 level accumulators
 //                of 16 columns (two sets, alternating per chunk);
-//     warps 6-9  drain: level sums -> FP64, and the epilogue.
+//     warps 10-13 drain: level sums -> FP64, and the epilogue.
 // Truncation: digits beyond 2^-48 of the row (or column) maximum and pairs
 // below 2^-54 are dropped -- well inside the 2*K*u64 normwise bound.
 #include <cuda.h>
@@ -43,7 +44,9 @@ gb_status ozaki_line_exponents(const double *X, int64_t ld, bool strided, int64_
 namespace {
 namespace thin_oz {
 
-constexpr int BM = 128, KB = 32, S = 8, NB = 16, STAGES = 4, CHUNK_KB = 16, NT = 320;
+// warps: 0 TMA, 1 MMA, 2-9 converters (two per TMEM lane quarter, one per
+// 16-k box), 10-13 drain / epilogue
+constexpr int BM = 128, KB = 32, S = 8, NB = 16, STAGES = 4, CHUNK_KB = 16, NCONV = 8, NT = 448;
 constexpr uint32_t LV_COLS = S * NB;        // 128: one set of level accumulators (level L at (L-2)*NB)
 constexpr uint32_t SLOT0 = 2 * LV_COLS;     // 256: digit slots (digit t at +16(t-1)), two of them
 constexpr uint32_t SLOT_COLS = S * 16;      // 128
@@ -92,6 +95,23 @@ __device__ __forceinline__ float small_int_to_float(uint32_t d) {
     return __int_as_float(0x4B000000 | d) - 8388608.0f;
 }
 
+// The 8 digits of F (< 2^48) as floats, most significant first.  The integer
+// pipe (half the FP32 lanes of an SM) only cuts F into four 12-bit pieces;
+// each piece becomes a float and splits into its two digits with exact FP32
+// arithmetic: hi = floor(p / 64) by a round-toward-zero add of 2^23, lo =
+// p - 64 hi.
+__device__ __forceinline__ void digits_f32(uint64_t F, float (&d)[8]) {
+    const uint32_t hi = (uint32_t)(F >> 32), lo = (uint32_t)F;
+    const uint32_t p[4] = {hi >> 4, __funnelshift_r(lo, hi, 24) & 0xFFFu, (lo >> 12) & 0xFFFu, lo & 0xFFFu};
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float f = small_int_to_float(p[i]);
+        const float h = __fadd_rz(f * 0.015625f, 8388608.0f) - 8388608.0f;   // floor(f / 64)
+        d[2 * i] = h;
+        d[2 * i + 1] = __fmaf_rn(-64.0f, h, f);                               // f - 64 h, exact
+    }
+}
+
 template <bool XCOLS>
 __global__ void __launch_bounds__(NT, 1)
     thin_oz_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, OzThinParams p) {
@@ -112,10 +132,10 @@ __global__ void __launch_bounds__(NT, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
             ptx::mbar_init(&full[s], 1);
-            ptx::mbar_init(&empty[s], 1 + 4);   // the MMA commit + four converter warps
+            ptx::mbar_init(&empty[s], 1 + NCONV);   // the MMA commit + the converter warps
         }
         for (int a = 0; a < 2; a++) {
-            ptx::mbar_init(&aready[a], 4);
+            ptx::mbar_init(&aready[a], NCONV);
             ptx::mbar_init(&aempty[a], 1);
             ptx::mbar_init(&lfull[a], 1);
             ptx::mbar_init(&lempty[a], 4);
@@ -204,8 +224,8 @@ __global__ void __launch_bounds__(NT, 1)
                 }
             }
         }
-    } else if (warp < 6) {   // converters: thread = row q*32 + lane of the tile
-        const int q = warp % 4, r = q * 32 + lane;
+    } else if (warp < 2 + NCONV) {   // converters: thread = row q*32 + lane, one 16-k box each
+        const int q = warp % 4, r = q * 32 + lane, b = (warp - 2) / 4;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         int g = 0;
         bool go = true;
@@ -222,46 +242,39 @@ __global__ void __launch_bounds__(NT, 1)
                     break;
                 }
                 ptx::tc_fence_after();
-                const uint8_t *st = smem + s * STAGE;
+                const uint8_t *box = smem + s * STAGE + b * (XS / 2);
                 const uint32_t slot = tmem + lane_off + SLOT0 + (uint32_t)(a * SLOT_COLS);
+                double x[16];
+                if (XCOLS) {   // [16 k][128 rows]
+                    const double *xs = reinterpret_cast<const double *>(box);
 #pragma unroll
-                for (int b = 0; b < 2; b++) {   // 16 k per box -> 8 columns of each digit slice
-                    double x[16];
-                    const uint8_t *box = st + b * (XS / 2);
-                    if (XCOLS) {   // [16 k][128 rows]
-                        const double *xs = reinterpret_cast<const double *>(box);
+                    for (int k = 0; k < 16; k++) x[k] = xs[k * BM + r];
+                } else {       // 128 rows of 128 bytes, 16-byte chunks swizzled by row % 8
+                    const uint8_t *rowp = box + r * 128;
 #pragma unroll
-                        for (int k = 0; k < 16; k++) x[k] = xs[k * BM + r];
-                    } else {       // 128 rows of 128 bytes, 16-byte chunks swizzled by row % 8
-                        const uint8_t *rowp = box + r * 128;
-#pragma unroll
-                        for (int c = 0; c < 8; c++) {
-                            const double2 v = *reinterpret_cast<const double2 *>(rowp + ((c ^ (r & 7)) << 4));
-                            x[2 * c] = v.x;
-                            x[2 * c + 1] = v.y;
-                        }
+                    for (int c = 0; c < 8; c++) {
+                        const double2 v = *reinterpret_cast<const double2 *>(rowp + ((c ^ (r & 7)) << 4));
+                        x[2 * c] = v.x;
+                        x[2 * c + 1] = v.y;
                     }
-                    uint32_t w[S][8];   // digit t, k pair i -> bf16x2
+                }
+                uint32_t w[S][8];   // digit t, k pair i -> bf16x2
 #pragma unroll
-                    for (int i = 0; i < 8; i++) {
-                        uint32_t s0, s1;
-                        const uint64_t F0 = scaled_mantissa(x[2 * i], e, s0);
-                        const uint64_t F1 = scaled_mantissa(x[2 * i + 1], e, s1);
-                        const uint32_t sm = (s0 << 15) | (s1 << 31);
+                for (int i = 0; i < 8; i++) {
+                    uint32_t s0, s1;
+                    float d0[8], d1[8];
+                    digits_f32(scaled_mantissa(x[2 * i], e, s0), d0);
+                    digits_f32(scaled_mantissa(x[2 * i + 1], e, s1), d1);
+                    const uint32_t sm = (s0 << 15) | (s1 << 31);
 #pragma unroll
-                        for (int t = 1; t <= S; t++) {
-                            const float f0 = small_int_to_float(digit_of(F0, t));
-                            const float f1 = small_int_to_float(digit_of(F1, t));
-                            w[t - 1][i] = bf16x2_bits(__floats2bfloat162_rn(f0, f1)) ^ sm;
-                        }
-                    }
+                    for (int t = 0; t < S; t++) w[t][i] = bf16x2_bits(__floats2bfloat162_rn(d0[t], d1[t])) ^ sm;
+                }
 #pragma unroll
-                    for (int t = 0; t < S; t++) {
-                        uint32_t regs[8];
+                for (int t = 0; t < S; t++) {
+                    uint32_t regs[8];
 #pragma unroll
-                        for (int i = 0; i < 8; i++) regs[i] = w[t][i];
-                        ptx::tmem_st_32x32b_x8(slot + (uint32_t)(t * 16 + b * 8), regs);
-                    }
+                    for (int i = 0; i < 8; i++) regs[i] = w[t][i];
+                    ptx::tmem_st_32x32b_x8(slot + (uint32_t)(t * 16 + b * 8), regs);
                 }
                 ptx::tmem_st_wait();
                 ptx::tc_fence_before();
