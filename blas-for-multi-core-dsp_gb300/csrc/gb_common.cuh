@@ -57,6 +57,40 @@ int *error_word();
 inline bool is_trans(char t) { return t == 'T' || t == 't'; }
 inline bool is_mode(char t) { return t == 'N' || t == 'n' || t == 'T' || t == 't'; }
 
+#ifdef __CUDACC__
+// Exponent of a line (row of X, column of W) that holds an Inf or a NaN:
+// the digit paths (Ozaki DGEMM, FP64 skinny) take the line maximum's
+// exponent, E - 1022 for biased exponent E, and E = 2047 only for Inf / NaN.
+constexpr int kNonFiniteLineExp = 1025;
+
+// e = smallest integer with max |x| < 2^e (0 for an all-zero line), from
+// the maximum of the |x| bit patterns (monotone for non-negative doubles).
+__device__ __forceinline__ int exp_of_maxbits(unsigned long long mb) {
+    if (mb == 0) return 0;
+    int E = (int)((mb >> 52) & 0x7FF);
+    if (E == 0) {   // subnormal: value = m * 2^-1074, m < 2^52
+        int lz = __clzll((long long)mb);      // m has 64 - lz significant bits
+        return (64 - lz) - 1074;
+    }
+    return E - 1022;   // value in [2^(E-1023), 2^(E-1022))
+}
+
+// Plain FP64 dot product of row `row` of X (rows x K; tx: stored K x rows)
+// and column `col` of W (K x cols; tw: stored cols x K), in k order.  The
+// digit paths use it for the outputs whose row or column holds an Inf or a
+// NaN, so that those propagate as IEEE arithmetic has them.
+__device__ inline double native_dot(const double *X, int64_t ldx, int tx, int64_t row, const double *W, int64_t ldw,
+                                    int tw, int64_t col, int64_t K) {
+    double s = 0.0;
+    for (int64_t k = 0; k < K; k++) {
+        const double x = tx ? X[k * ldx + row] : X[row * ldx + k];
+        const double w = tw ? W[col * ldw + k] : W[k * ldw + col];
+        s = fma(x, w, s);
+    }
+    return s;
+}
+#endif
+
 // Counter-based generator (identical to the oracle's gbo_* functions).
 __host__ __device__ inline uint64_t mix64(uint64_t z) {
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;

@@ -65,17 +65,7 @@ constexpr int NT = 192;
 constexpr uint32_t TMEM_COLS = 512;            // [0,256): two FP32 accumulators, [256,512): FP64 sum
 
 // ------------------------------------------------------------- exponents
-// e = smallest integer with max |x| < 2^e (0 for an all-zero line), from
-// the maximum of the |x| bit patterns (monotone for non-negative doubles).
-__device__ __forceinline__ int exp_of_maxbits(unsigned long long mb) {
-    if (mb == 0) return 0;
-    int E = (int)((mb >> 52) & 0x7FF);
-    if (E == 0) {   // subnormal: value = m * 2^-1074, m < 2^52
-        int lz = __clzll((long long)mb);      // m has 64 - lz significant bits
-        return (64 - lz) - 1074;
-    }
-    return E - 1022;   // value in [2^(E-1023), 2^(E-1022))
-}
+// (exp_of_maxbits: the line exponent from the maximum |x| bit pattern)
 
 // one warp per line of `len` contiguous elements
 __global__ void maxexp_contig_kernel(const double *__restrict__ X, int64_t ld, int64_t lines, int64_t len,
@@ -216,6 +206,10 @@ struct OzParams {
     signed char pt[MAXPAIRS], pu[MAXPAIRS];   // 1-based digit indices per pair
     const int *erow, *fcol;
     int *err;
+    // operands, for the outputs that a non-finite row or column reaches
+    const double *A, *B;
+    int64_t lda, ldb, K;
+    int ta, tb;
 };
 
 __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int &tm, int &tn) {
@@ -402,7 +396,11 @@ __global__ void __launch_bounds__(NT, 1)
                     const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
                     for (int rr = 0; rr < rows; rr++) {
                         double *cp = p.C + (row0 + rr) * p.ldc + col;
-                        double v = p.alpha * scalbn(stage[rr * 33 + lane], fc);
+                        double v;
+                        if (fc == kNonFiniteLineExp || __ldg(p.erow + row0 + rr) == kNonFiniteLineExp)
+                            v = p.alpha * native_dot(p.A, p.lda, p.ta, row0 + rr, p.B, p.ldb, p.tb, col, p.K);
+                        else
+                            v = p.alpha * scalbn(stage[rr * 33 + lane], fc);
                         if (p.semantics == GB_SEM_BLAS) {
                             if (p.beta != 0.0) v = fma(p.beta, *cp, v);
                         } else if (p.semantics == GB_SEM_SCALAR_BETA) {
@@ -525,6 +523,7 @@ static gb_status ozaki_one(const GemmArgs &g, int s) {
     p.tiles_m = (int)(mp / BM); p.tiles_n = (int)(np / BN);
     p.mp = mp; p.np = np;
     p.erow = erow; p.fcol = fcol; p.err = err;
+    p.A = A; p.B = B; p.lda = g.lda; p.ldb = g.ldb; p.K = g.K; p.ta = g.ta ? 1 : 0; p.tb = g.tb ? 1 : 0;
     // slice pairs t + u <= s + 1, least significant diagonals first (the FP64
     // sum then adds terms in increasing magnitude)
     int n = 0;

@@ -10,22 +10,38 @@
 // digit products run on tcgen05.mma (kind::f16, FP32 accumulate):
 //     x_rk = 2^e_r sum_t d_t 2^-6t,   w_kj = 2^f_j sum_u v_u 2^-6u,
 //     C_rj ~= 2^(e_r+f_j) sum_{L=2..9} 2^-6L S_L,  S_L = sum_{t+u=L} sum_k d_t v_u.
-// Every S_L over a K chunk of 512 is an integer below 8*512*63^2 < 2^24, so
-// the FP32 tensor-memory accumulators hold it exactly; at each chunk's end
-// the drain warps add the eight level sums into FP64 registers.
-//   pass 1: row exponents of X (one read of X), column exponents and the
-//           digit slices of W (small);
+// Row exponents are taken per K chunk of 256 (e_rc: max |x| < 2^e_rc over
+// row r's 256 values), so X is read once from HBM: a scan of the chunk
+// through a second TMA ring finds them, and the conversion re-reads the same
+// chunk from L2 one chunk later.  Every S_L over a chunk is an integer below
+// 8*256*63^2 < 2^24, so the FP32 tensor-memory accumulators hold it exactly;
+// at each chunk's end the drain warps combine the eight level sums into one
+// exact 64-bit integer per output and add it, scaled by 2^(e_rc - 54), into
+// FP64 registers (relative to the row's running maximum exponent): one
+// FP64 conversion and one FMA per output and chunk, as GB300's FP64 pipe is
+// narrow.
+//   pass 1: column exponents and the digit slices of W (small);
 //   pass 2 (thin_oz_kernel, per 16 columns of W):
 //     warp 0     TMA: 128 rows x 32 k of X (FP64) + the 8 digit tiles of W;
+//     warp 14    TMA: the same X boxes, one chunk ahead, for the scan;
+//     warps 10-13 scan chunk c+1 (thread = row: the maximum |x| bit
+//                pattern -> e_rc in shared memory), then drain chunk c:
+//                level sums -> FP64, and the epilogue;
 //     warps 2-9  converters, two per TMEM lane quarter (one per 16-k box),
 //                thread = row: the row's values -> 8 digit slices written
 //                into tensor memory (the A operand of the MMA, never in
 //                shared memory);
-//     warp 1     MMA: the 36 digit pairs t + u <= 9 into 8 level accumulators
-//                of 16 columns (two sets, alternating per chunk);
-//     warps 10-13 drain: level sums -> FP64, and the epilogue.
-// Truncation: digits beyond 2^-48 of the row (or column) maximum and pairs
-// below 2^-54 are dropped -- well inside the 2*K*u64 normwise bound.
+//     warp 1     MMA: one MMA per digit t of X against W's digits
+//                u = 1 .. 9-t at once (N = 16(9-t)): W's digit tiles lie in
+//                shared memory in the order u = 8 .. 1, so the pair (t, u)
+//                lands in accumulator column block 9 - t - u for every t,
+//                i.e. level L = t + u at columns 16(9-L) .. 16(9-L)+15;
+//                two level sets alternate per chunk.
+// Truncation: digits beyond 2^-48 of the chunk's row maximum (or the column
+// maximum) and pairs below 2^-54 are dropped -- well inside the 2*K*u64
+// normwise bound.  An output whose row of X or column of W holds an Inf or a
+// NaN is recomputed as a plain FP64 dot product, so non-finite values
+// propagate.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -44,17 +60,20 @@ gb_status ozaki_line_exponents(const double *X, int64_t ld, bool strided, int64_
 namespace {
 namespace thin_oz {
 
-// warps: 0 TMA, 1 MMA, 2-9 converters (two per TMEM lane quarter, one per
-// 16-k box), 10-13 drain / epilogue
-constexpr int BM = 128, KB = 32, S = 8, NB = 16, STAGES = 4, CHUNK_KB = 16, NCONV = 8, NT = 448;
-constexpr uint32_t LV_COLS = S * NB;        // 128: one set of level accumulators (level L at (L-2)*NB)
+// warps: 0 TMA (converter stages), 1 MMA, 2-9 converters (two per TMEM lane
+// quarter, one per 16-k box), 10-13 scan + drain / epilogue, 14 TMA (scan)
+constexpr int BM = 128, KB = 32, S = 8, NB = 16, STAGES = 4, SSTAGES = 2, CHUNK_KB = 8, NCONV = 8, NT = 480;
+constexpr uint32_t LV_COLS = S * NB;        // 128: one set of level accumulators (level L at (S+1-L)*NB)
 constexpr uint32_t SLOT0 = 2 * LV_COLS;     // 256: digit slots (digit t at +16(t-1)), two of them
 constexpr uint32_t SLOT_COLS = S * 16;      // 128
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int XS = BM * KB * 8;             // 32 KB: two 16-k boxes of FP64
-constexpr int WS = S * NB * KB * 2;         // 8 KB: the 8 digit tiles of W (16 rows of 64 bytes each)
+constexpr int WS = S * NB * KB * 2;         // 8 KB: the 8 digit tiles of W (16 rows of 64 bytes each), u = 8 .. 1
 constexpr int STAGE = XS + WS;
-constexpr int SMEM = STAGES * STAGE + 1024 /*align*/ + 512 /*barriers*/;
+constexpr int BAR_BYTES = 512, EXP_BYTES = 2 * BM * 4;
+constexpr int SMEM = STAGES * STAGE + SSTAGES * XS + 1024 /*align*/ + BAR_BYTES + EXP_BYTES;
+constexpr int NO_EXP = -100000;             // chunk exponent of an all-zero row chunk
+static_assert(SMEM <= 232448, "shared memory");
 
 struct OzThinParams {
     int64_t rows, K;
@@ -62,9 +81,37 @@ struct OzThinParams {
     double *C; int64_t cs_r, cs_c;
     double alpha, beta;
     int semantics;
-    double *part;                           // splits x rows x NB raw sums (split-K)
-    const int *erow, *fcol;
+    double *part;                           // splits x rows x NB sums (split-K)
+    int *nfrow;                             // split-K: rows that hold an Inf / NaN
+    const int *fcol;
     int *err;
+    // operands, for the outputs that a non-finite row or column reaches
+    const double *X, *W;
+    int64_t ldx, ldw;
+    int tx, tw, j0;
+};
+
+// The (unit, chunk) pairs of this CTA in order: unit u = (row tile, split),
+// chunks of CHUNK_KB k blocks from the split's first.
+struct Walk {
+    int u, c0, kb1;
+    __device__ __forceinline__ void set(const OzThinParams &p, int nkb) {
+        c0 = (u % p.splits) * p.kchunk_kb;
+        kb1 = min(nkb, c0 + p.kchunk_kb);
+    }
+    __device__ __forceinline__ void first(const OzThinParams &p, int nkb) {
+        u = blockIdx.x;
+        set(p, nkb);
+    }
+    __device__ __forceinline__ int c1() const { return min(kb1, c0 + CHUNK_KB); }
+    __device__ __forceinline__ bool last() const { return c0 + CHUNK_KB >= kb1; }
+    __device__ __forceinline__ void next(const OzThinParams &p, int nkb) {
+        c0 += CHUNK_KB;
+        if (c0 >= kb1) {
+            u += gridDim.x;
+            set(p, nkb);
+        }
+    }
 };
 
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t *>(&v); }
@@ -95,21 +142,120 @@ __device__ __forceinline__ float small_int_to_float(uint32_t d) {
     return __int_as_float(0x4B000000 | d) - 8388608.0f;
 }
 
-// The 8 digits of F (< 2^48) as floats, most significant first.  The integer
-// pipe (half the FP32 lanes of an SM) only cuts F into four 12-bit pieces;
-// each piece becomes a float and splits into its two digits with exact FP32
-// arithmetic: hi = floor(p / 64) by a round-toward-zero add of 2^23, lo =
-// p - 64 hi.
-__device__ __forceinline__ void digits_f32(uint64_t F, float (&d)[8]) {
-    const uint32_t hi = (uint32_t)(F >> 32), lo = (uint32_t)F;
-    const uint32_t p[4] = {hi >> 4, __funnelshift_r(lo, hi, 24) & 0xFFFu, (lo >> 12) & 0xFFFu, lo & 0xFFFu};
+// 64-bit right shift whose amounts of 64 and more give zero (PTX clamps them).
+__device__ __forceinline__ uint64_t shr64(uint64_t v, uint32_t s) {
+    uint64_t r;
+    asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(v), "r"(s));
+    return r;
+}
+
+// scaled_mantissa() for rows with e >= -974, from the high and low words of
+// x: every finite x of the row has a right shift rs = 1027 + e - E >= 5 (its
+// biased exponent E <= e + 1022).  Zeros and subnormals (E = 0) get the
+// implicit bit set wrongly, but with rs >= 53 it shifts out with the rest.
+__device__ __forceinline__ uint64_t scaled_mantissa_fast(uint32_t hi, uint32_t lo, int e1027) {
+    const uint32_t rs = (uint32_t)(e1027 - (int)((hi >> 20) & 0x7FFu));
+    return shr64(((uint64_t)((hi & 0xFFFFFu) | 0x100000u) << 32) | lo, rs);
+}
+
+// The 8 digits of F (< 2^48), most significant first, as floats carrying the
+// sign of x (the sign bit of `hi`).  The integer pipe only cuts F into three
+// pieces of 18, 18 and 12 bits and writes each into the low bits of
+// C = +-2^23 (a float +-(2^23 + p)); FP32 arithmetic, exact throughout, does
+// the rest: f = +-p, then repeatedly hi = trunc(f / 2^s) by a round-toward-
+// zero fma onto +-2^23 and f - 2^s hi.
+__device__ __forceinline__ void digits_signed(uint64_t F, uint32_t hi, float (&d)[8]) {
+    const uint32_t C = (hi & 0x80000000u) | 0x4B000000u;
+    const float M = __uint_as_float(C);
+    const uint32_t fh = (uint32_t)(F >> 32), fl = (uint32_t)F;
+    const float f0 = __uint_as_float(__funnelshift_r(fl, fh, 30) | C) - M;   // bits 30..47 (fh < 2^16)
+    const float f1 = __uint_as_float(((fl >> 12) & 0x3FFFFu) | C) - M;       // bits 12..29
+    const float f2 = __uint_as_float((fl & 0xFFFu) | C) - M;                  // bits 0..11
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const float f = small_int_to_float(p[i]);
-        const float h = __fadd_rz(f * 0.015625f, 8388608.0f) - 8388608.0f;   // floor(f / 64)
-        d[2 * i] = h;
-        d[2 * i + 1] = __fmaf_rn(-64.0f, h, f);                               // f - 64 h, exact
+    for (int i = 0; i < 2; i++) {
+        const float f = i ? f1 : f0;
+        const float h = __fmaf_rz(f, 1.0f / 4096.0f, M) - M;
+        const float r = __fmaf_rn(-4096.0f, h, f);
+        const float h2 = __fmaf_rz(r, 0.015625f, M) - M;
+        d[3 * i] = h;
+        d[3 * i + 1] = h2;
+        d[3 * i + 2] = __fmaf_rn(-64.0f, h2, r);
     }
+    const float h = __fmaf_rz(f2, 0.015625f, M) - M;
+    d[6] = h;
+    d[7] = __fmaf_rn(-64.0f, h, f2);
+}
+
+// The 16 values of one box row -> 8 digit slices of 8 bf16x2 words.
+template <bool FAST>
+__device__ __forceinline__ void convert16(const double (&x)[16], int e, uint32_t (&w)[S][8]) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        float d0[8], d1[8];
+        const uint64_t b0 = (uint64_t)__double_as_longlong(x[2 * i]), b1 = (uint64_t)__double_as_longlong(x[2 * i + 1]);
+        const uint32_t h0 = (uint32_t)(b0 >> 32), h1 = (uint32_t)(b1 >> 32);
+        uint64_t F0, F1;
+        if (FAST) {
+            F0 = scaled_mantissa_fast(h0, (uint32_t)b0, 1027 + e);
+            F1 = scaled_mantissa_fast(h1, (uint32_t)b1, 1027 + e);
+        } else {
+            uint32_t sg;
+            F0 = scaled_mantissa(x[2 * i], e, sg);
+            F1 = scaled_mantissa(x[2 * i + 1], e, sg);
+        }
+        digits_signed(F0, h0, d0);
+        digits_signed(F1, h1, d1);
+#pragma unroll
+        for (int t = 0; t < S; t++) w[t][i] = bf16x2_bits(__floats2bfloat162_rn(d0[t], d1[t]));
+    }
+}
+
+// C(r, j) = alpha * value (+ beta / C semantics)
+__device__ __forceinline__ void store_out(const OzThinParams &p, double *cp, double v) {
+    v *= p.alpha;
+    if (p.semantics == GB_SEM_BLAS) {
+        if (p.beta != 0.0) v = fma(p.beta, *cp, v);
+    } else if (p.semantics == GB_SEM_SCALAR_BETA) {
+        v = v + p.beta;
+    } else {
+        v = *cp + (v + p.beta);
+    }
+    *cp = v;
+}
+
+// The 16 values of row r in one 16-k box of X: [16 k][128 rows] (XCOLS) or
+// 128 rows of 128 bytes with 16-byte chunks swizzled by row % 8.
+template <bool XCOLS>
+__device__ __forceinline__ void load_row16(const uint8_t *box, int r, double (&x)[16]) {
+    if (XCOLS) {
+        const double *xs = reinterpret_cast<const double *>(box);
+#pragma unroll
+        for (int k = 0; k < 16; k++) x[k] = xs[k * BM + r];
+    } else {
+        const uint8_t *rowp = box + r * 128;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const double2 v = *reinterpret_cast<const double2 *>(rowp + ((c ^ (r & 7)) << 4));
+            x[2 * c] = v.x;
+            x[2 * c + 1] = v.y;
+        }
+    }
+}
+
+// 2^k as a double for k >= -1022, 0 below
+__device__ __forceinline__ double pow2_or_zero(int k) {
+    return k >= -1022 ? __longlong_as_double((long long)(1023 + k) << 52) : 0.0;
+}
+
+// x * 2^k for |k| up to 3069 without a library call: up to three factors in
+// the normal range, the largest first, so that only a result outside the
+// normal range rounds.
+__device__ __forceinline__ double mul_pow2(double x, int k) {
+    const int a = max(-1022, min(1023, k));
+    k -= a;
+    const int b = max(-1022, min(1023, k));
+    const int c = max(-1022, min(1023, k - b));
+    return x * pow2_or_zero(a) * pow2_or_zero(b) * pow2_or_zero(c);
 }
 
 template <bool XCOLS>
@@ -117,13 +263,18 @@ __global__ void __launch_bounds__(NT, 1)
     thin_oz_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, OzThinParams p) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE);
+    uint8_t *sring = smem + STAGES * STAGE;
+    uint64_t *full = reinterpret_cast<uint64_t *>(sring + SSTAGES * XS);
     uint64_t *empty = full + STAGES;
     uint64_t *aready = empty + STAGES;     // [2] digit slots
     uint64_t *aempty = aready + 2;
     uint64_t *lfull = aempty + 2;          // [2] level sets
     uint64_t *lempty = lfull + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(lempty + 2);
+    uint64_t *sfull = lempty + 2;          // [SSTAGES] scan ring
+    uint64_t *sempty = sfull + SSTAGES;
+    uint64_t *xready = sempty + SSTAGES;   // [2] chunk exponents
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(xready + 2);
+    int *exps = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(full) + BAR_BYTES);   // [2][BM]
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int nkb = (int)((p.K + KB - 1) / KB);
@@ -134,11 +285,16 @@ __global__ void __launch_bounds__(NT, 1)
             ptx::mbar_init(&full[s], 1);
             ptx::mbar_init(&empty[s], 1 + NCONV);   // the MMA commit + the converter warps
         }
+        for (int s = 0; s < SSTAGES; s++) {
+            ptx::mbar_init(&sfull[s], 1);
+            ptx::mbar_init(&sempty[s], 4);
+        }
         for (int a = 0; a < 2; a++) {
             ptx::mbar_init(&aready[a], NCONV);
             ptx::mbar_init(&aempty[a], 1);
             ptx::mbar_init(&lfull[a], 1);
             ptx::mbar_init(&lempty[a], 4);
+            ptx::mbar_init(&xready[a], 4);
         }
         ptx::fence_mbar_init();
         ptx::tma_prefetch_desc(&tmx);
@@ -150,33 +306,35 @@ __global__ void __launch_bounds__(NT, 1)
     ptx::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 0) {
-        if (lane == 0) {   // TMA producer
+    if (warp == 0 || warp == 14) {
+        if (lane == 0) {   // TMA producers: warp 0 the converter stages (X + W digits), warp 14 the scan ring
+            const bool scan = warp == 14;
+            const int nst = scan ? SSTAGES : STAGES;
+            uint64_t *fb = scan ? sfull : full, *eb = scan ? sempty : empty;
             int g = 0;
             bool go = true;
             for (int u = blockIdx.x; u < units && go; u += gridDim.x) {
                 const int rt = u / p.splits, sp = u - rt * p.splits;
                 const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
                 for (int kb = kb0; kb < kb1; kb++, g++) {
-                    const int s = g % STAGES;
-                    if (g >= STAGES && !ptx::mbar_wait(&empty[s], ((g / STAGES) & 1) ^ 1, p.err, 61)) {
+                    const int s = g % nst;
+                    if (g >= nst && !ptx::mbar_wait(&eb[s], ((g / nst) & 1) ^ 1, p.err, scan ? 60 : 61)) {
                         go = false;
                         break;
                     }
-                    uint8_t *st = smem + s * STAGE;
-                    ptx::mbar_arrive_expect_tx(&full[s], XS + WS);
+                    uint8_t *st = scan ? sring + s * XS : smem + s * STAGE;
+                    ptx::mbar_arrive_expect_tx(&fb[s], scan ? XS : XS + WS);
 #pragma unroll
                     for (int b = 0; b < 2; b++) {
-                        if (XCOLS) ptx::tma_load_2d(st + b * (XS / 2), &tmx, &full[s], rt * BM, kb * KB + 16 * b);
-                        else ptx::tma_load_2d(st + b * (XS / 2), &tmx, &full[s], kb * KB + 16 * b, rt * BM);
+                        if (XCOLS) ptx::tma_load_2d(st + b * (XS / 2), &tmx, &fb[s], rt * BM, kb * KB + 16 * b);
+                        else ptx::tma_load_2d(st + b * (XS / 2), &tmx, &fb[s], kb * KB + 16 * b, rt * BM);
                     }
-                    ptx::tma_load_2d(st + XS, &tmw, &full[s], kb * KB, 0);
+                    if (!scan) ptx::tma_load_2d(st + XS, &tmw, &fb[s], kb * KB, 0);
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {   // MMA issuer
-            constexpr uint32_t idesc = ptx::idesc_bf16_f32(BM, NB);
             int g = 0, ch = 0;
             bool go = true;
             for (int u = blockIdx.x; u < units && go; u += gridDim.x) {
@@ -205,16 +363,13 @@ __global__ void __launch_bounds__(NT, 1)
                         for (int kk = 0; kk < KB / 16; kk++) {
 #pragma unroll
                             for (int t = 1; t <= S; t++) {
-#pragma unroll
-                                for (int v = 1; v + t <= S + 1; v++) {
-                                    // digit v of W: rows (v-1)*16 .. of the stage's W tile (1 KB each)
-                                    const uint64_t bdesc =
-                                        ptx::sdesc_kmajor_sw64(wst + (uint32_t)((v - 1) * NB * 64)) +
-                                        (uint64_t)((kk * 32) >> 4);
-                                    ptx::umma_f16_ta(lv + (uint32_t)((t + v - 2) * NB),
-                                                     slot + (uint32_t)((t - 1) * 16 + kk * 8), bdesc, idesc,
-                                                     (kb != c0 || kk != 0 || t != 1) ? 1u : 0u);
-                                }
+                                // W digits u = 9-t .. 1: tile rows 16(t-1) .. 127, N = 16(9-t); the first
+                                // MMA of a chunk (t = 1, N = 128) writes every level column
+                                const uint64_t bdesc = ptx::sdesc_kmajor_sw64(wst + (uint32_t)((t - 1) * NB * 64)) +
+                                                       (uint64_t)((kk * 32) >> 4);
+                                ptx::umma_f16_ta(lv, slot + (uint32_t)((t - 1) * 16 + kk * 8), bdesc,
+                                                 ptx::idesc_bf16_f32(BM, NB * (S + 1 - t)),
+                                                 (kb != c0 || kk != 0 || t != 1) ? 1u : 0u);
                             }
                         }
                         ptx::umma_commit(&empty[s]);
@@ -227,14 +382,25 @@ __global__ void __launch_bounds__(NT, 1)
     } else if (warp < 2 + NCONV) {   // converters: thread = row q*32 + lane, one 16-k box each
         const int q = warp % 4, r = q * 32 + lane, b = (warp - 2) / 4;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        int g = 0;
+        int g = 0, ch = 0;
         bool go = true;
         for (int u = blockIdx.x; u < units && go; u += gridDim.x) {
-            const int rt = u / p.splits, sp = u - rt * p.splits;
+            const int sp = u % p.splits;
             const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
-            const int64_t row = (int64_t)rt * BM + r;
-            const int e = row < p.rows ? __ldg(p.erow + row) : 0;
+            int e = 0;
+            bool fast = true;
             for (int kb = kb0; kb < kb1; kb++, g++) {
+                if ((kb - kb0) % CHUNK_KB == 0) {   // a new chunk: the row's exponent over it
+                    const int xs = ch & 1;
+                    if (!ptx::mbar_wait(&xready[xs], (ch >> 1) & 1, p.err, 68)) {
+                        go = false;
+                        break;
+                    }
+                    e = exps[xs * BM + r];
+                    if (e == NO_EXP) e = 0;
+                    fast = __all_sync(0xFFFFFFFFu, e >= -974);
+                    ch++;
+                }
                 const int s = g % STAGES, a = g & 1;
                 if (!ptx::mbar_wait(&full[s], (g / STAGES) & 1, p.err, 65) ||
                     (g >= 2 && !ptx::mbar_wait(&aempty[a], ((g >> 1) & 1) ^ 1, p.err, 66))) {
@@ -242,33 +408,12 @@ __global__ void __launch_bounds__(NT, 1)
                     break;
                 }
                 ptx::tc_fence_after();
-                const uint8_t *box = smem + s * STAGE + b * (XS / 2);
                 const uint32_t slot = tmem + lane_off + SLOT0 + (uint32_t)(a * SLOT_COLS);
                 double x[16];
-                if (XCOLS) {   // [16 k][128 rows]
-                    const double *xs = reinterpret_cast<const double *>(box);
-#pragma unroll
-                    for (int k = 0; k < 16; k++) x[k] = xs[k * BM + r];
-                } else {       // 128 rows of 128 bytes, 16-byte chunks swizzled by row % 8
-                    const uint8_t *rowp = box + r * 128;
-#pragma unroll
-                    for (int c = 0; c < 8; c++) {
-                        const double2 v = *reinterpret_cast<const double2 *>(rowp + ((c ^ (r & 7)) << 4));
-                        x[2 * c] = v.x;
-                        x[2 * c + 1] = v.y;
-                    }
-                }
+                load_row16<XCOLS>(smem + s * STAGE + b * (XS / 2), r, x);
                 uint32_t w[S][8];   // digit t, k pair i -> bf16x2
-#pragma unroll
-                for (int i = 0; i < 8; i++) {
-                    uint32_t s0, s1;
-                    float d0[8], d1[8];
-                    digits_f32(scaled_mantissa(x[2 * i], e, s0), d0);
-                    digits_f32(scaled_mantissa(x[2 * i + 1], e, s1), d1);
-                    const uint32_t sm = (s0 << 15) | (s1 << 31);
-#pragma unroll
-                    for (int t = 0; t < S; t++) w[t][i] = bf16x2_bits(__floats2bfloat162_rn(d0[t], d1[t])) ^ sm;
-                }
+                if (fast) convert16<true>(x, e, w);
+                else convert16<false>(x, e, w);
 #pragma unroll
                 for (int t = 0; t < S; t++) {
                     uint32_t regs[8];
@@ -285,60 +430,129 @@ __global__ void __launch_bounds__(NT, 1)
                 }
             }
         }
-    } else {                 // drain + epilogue: thread = row q*32 + lane of the tile
-        const int q = warp % 4;
+    } else if (warp < 14) {  // scan chunk c+1, drain chunk c, epilogue: thread = row q*32 + lane of the tile
+        const int q = warp % 4, r = q * 32 + lane;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        int ch = 0;
+        Walk sw, dw;
+        sw.first(p, nkb);
+        dw.first(p, nkb);
+        int sg = 0, sch = 0;            // scan-ring k blocks, scanned chunks
+        int ex0 = NO_EXP, ex1 = NO_EXP;  // this row's exponents of the chunks in slots 0 / 1
         bool go = true;
-        for (int u = blockIdx.x; u < units && go; u += gridDim.x) {
-            const int rt = u / p.splits, sp = u - rt * p.splits;
-            const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
-            double acc[NB];
+        // scan of the chunk at sw: the row's maximum |x| bit pattern -> its exponent
+        auto scan = [&]() -> bool {
+            // the largest |high word| gives the exponent unless it is subnormal; then the
+            // bit length of the largest |x| is that of the OR of all (high, low) words
+            uint32_t mx = 0, lor = 0;
+            for (int kb = sw.c0; kb < sw.c1(); kb++, sg++) {
+                const int s = sg % SSTAGES;
+                if (!ptx::mbar_wait(&sfull[s], (sg / SSTAGES) & 1, p.err, 69)) return false;
 #pragma unroll
-            for (int j = 0; j < NB; j++) acc[j] = 0.0;
-            for (int c0 = kb0; c0 < kb1; c0 += CHUNK_KB, ch++) {
-                const int lb = ch & 1;
-                if (!ptx::mbar_wait(&lfull[lb], (ch >> 1) & 1, p.err, 67)) { go = false; break; }
-                ptx::tc_fence_after();
-                // least significant level first, each level sum exact, scaled exactly
+                for (int bx = 0; bx < 2; bx++) {
+                    double x[16];
+                    load_row16<XCOLS>(sring + s * XS + bx * (XS / 2), r, x);
 #pragma unroll
-                for (int L = S + 1; L >= 2; L--) {
-                    uint32_t v[16];
-                    ptx::tmem_ld_32x32b_x16(tmem + lane_off + (uint32_t)(lb * LV_COLS + (L - 2) * NB), v);
-                    ptx::tmem_ld_wait();
-                    const double sc = __longlong_as_double((long long)(1023 - 6 * L) << 52);   // 2^-6L
-#pragma unroll
-                    for (int j = 0; j < NB; j++) acc[j] = fma((double)__uint_as_float(v[j]), sc, acc[j]);
+                    for (int k = 0; k < 16; k += 2) {
+                        const uint32_t h0 = (uint32_t)__double2hiint(x[k]) & 0x7FFFFFFFu;
+                        const uint32_t h1 = (uint32_t)__double2hiint(x[k + 1]) & 0x7FFFFFFFu;
+                        mx = __vimax3_u32(mx, h0, h1);
+                        lor |= (uint32_t)__double2loint(x[k]) | (uint32_t)__double2loint(x[k + 1]);
+                    }
                 }
-                ptx::tc_fence_before();
                 __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(&lempty[lb]);
+                if (lane == 0) ptx::mbar_arrive(&sempty[s]);
             }
-            if (!go) break;
-            const int64_t row = (int64_t)rt * BM + q * 32 + lane;
-            if (row >= p.rows) continue;
-            if (p.splits > 1) {
-                double *pp = p.part + ((int64_t)sp * p.rows + row) * NB;
+            int e;
+            if (mx >> 20) e = (int)(mx >> 20) - 1022;                  // normal, Inf, NaN
+            else if (mx) e = 64 - __clz(mx) - 1074;                    // subnormal, high word set
+            else e = lor ? 32 - __clz(lor) - 1074 : NO_EXP;            // subnormal below 2^-1042, or zeros
+            const int xs = sch & 1;
+            exps[xs * BM + r] = e;
+            if (xs) ex1 = e;
+            else ex0 = e;
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&xready[xs]);
+            sch++;
+            sw.next(p, nkb);
+            return true;
+        };
+        if (sw.u < units) go = scan();
+        double acc[NB];
 #pragma unroll
-                for (int j = 0; j < NB; j++) pp[j] = acc[j];
-                continue;
-            }
-            const int er = __ldg(p.erow + row);
-            double *cr = p.C + row * p.cs_r;
+        for (int j = 0; j < NB; j++) acc[j] = 0.0;
+        int eref = NO_EXP;   // the row's largest chunk exponent so far: acc is in units of 2^eref
+        bool nf = false;     // the row holds an Inf / NaN
+        for (int ch = 0; go && dw.u < units; ch++) {
+            if (sw.u < units && !scan()) break;
+            const int lb = ch & 1;
+            if (!ptx::mbar_wait(&lfull[lb], (ch >> 1) & 1, p.err, 67)) break;
+            ptx::tc_fence_after();
+            const int ec = lb ? ex1 : ex0;
+            nf |= ec == kNonFiniteLineExp;
+            if (ec != NO_EXP) {
+                if (eref == NO_EXP) {
+                    eref = ec;
+                } else if (ec > eref) {
 #pragma unroll
-            for (int j = 0; j < NB; j++) {
-                if (j >= p.n) break;
-                double *cp = cr + (int64_t)j * p.cs_c;
-                double v = p.alpha * scalbn(scalbn(acc[j], er), __ldg(p.fcol + j));
-                if (p.semantics == GB_SEM_BLAS) {
-                    if (p.beta != 0.0) v = fma(p.beta, *cp, v);
-                } else if (p.semantics == GB_SEM_SCALAR_BETA) {
-                    v = v + p.beta;
-                } else {
-                    v = *cp + (v + p.beta);
+                    for (int j = 0; j < NB; j++) acc[j] = mul_pow2(acc[j], eref - ec);
+                    eref = ec;
                 }
-                *cp = v;
             }
+            // T = sum_L S_L 2^(6(9-L)) exactly in 64-bit integers (|S_L| < (L-1) 256 63^2, so
+            // |T| < 2^62.1), then one rounding to FP64: sum_L S_L 2^-6L = T 2^-54
+            const double sc = pow2_or_zero(ec == NO_EXP ? -100000 : ec - eref - 54);
+#pragma unroll
+            for (int h = 0; h < NB / 8; h++) {   // eight columns at a time
+                long long T[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) T[j] = 0;
+#pragma unroll
+                for (int L = 2; L <= S + 1; L++) {
+                    uint32_t v[8];
+                    ptx::tmem_ld_32x32b_x8(tmem + lane_off + (uint32_t)(lb * LV_COLS + (S + 1 - L) * NB + 8 * h), v);
+                    ptx::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 8; j++) T[j] = T[j] * 64 + (long long)__float2int_rn(__uint_as_float(v[j]));
+                }
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[8 * h + j] = fma((double)T[j], sc, acc[8 * h + j]);
+            }
+            ptx::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&lempty[lb]);
+            if (dw.last()) {   // the unit's sums are complete
+                const int rt = dw.u / p.splits, sp = dw.u - rt * p.splits;
+                const int64_t row = (int64_t)rt * BM + r;
+                if (row < p.rows) {
+                    const int er = eref == NO_EXP ? 0 : eref;
+                    if (p.splits > 1) {
+                        double *pp = p.part + ((int64_t)sp * p.rows + row) * NB;
+#pragma unroll
+                        for (int j = 0; j < NB; j++)
+                            if (j < p.n) pp[j] = mul_pow2(acc[j], er + __ldg(p.fcol + j));
+                        if (nf) p.nfrow[row] = 1;
+                    } else {
+                        double *cr = p.C + row * p.cs_r;
+#pragma unroll
+                        for (int j = 0; j < NB; j++) {
+                            if (j >= p.n) break;
+                            const int fc = __ldg(p.fcol + j);
+                            if (!nf && fc != kNonFiniteLineExp)
+                                store_out(p, cr + (int64_t)j * p.cs_c, mul_pow2(acc[j], er + fc));
+                        }
+#pragma unroll 1
+                        for (int j = 0; j < p.n; j++)   // a row or column that holds an Inf / NaN
+                            if (nf || __ldg(p.fcol + j) == kNonFiniteLineExp)
+                                store_out(p, cr + (int64_t)j * p.cs_c,
+                                          native_dot(p.X, p.ldx, p.tx, row, p.W, p.ldw, p.tw, (int64_t)p.j0 + j, p.K));
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < NB; j++) acc[j] = 0.0;
+                eref = NO_EXP;
+                nf = false;
+            }
+            dw.next(p, nkb);
         }
     }
 
@@ -350,7 +564,8 @@ __global__ void __launch_bounds__(NT, 1)
     }
 }
 
-// Split-K: sum the parts in order, then scale and apply the epilogue.
+// Split-K: sum the parts (already scaled) in order, then the epilogue; a
+// row or column holding an Inf / NaN gets the plain dot product.
 __global__ void thin_oz_reduce_kernel(OzThinParams p) {
     const int64_t total = p.rows * p.n;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
@@ -358,23 +573,18 @@ __global__ void thin_oz_reduce_kernel(OzThinParams p) {
         const int64_t r = e / p.n;
         const int j = (int)(e - r * p.n);
         double s = 0.0;
-        for (int sp = 0; sp < p.splits; sp++) s += p.part[((int64_t)sp * p.rows + r) * NB + j];
-        double *cp = p.C + r * p.cs_r + (int64_t)j * p.cs_c;
-        double v = p.alpha * scalbn(scalbn(s, p.erow[r]), p.fcol[j]);
-        if (p.semantics == GB_SEM_BLAS) {
-            if (p.beta != 0.0) v = fma(p.beta, *cp, v);
-        } else if (p.semantics == GB_SEM_SCALAR_BETA) {
-            v = v + p.beta;
+        if (p.nfrow[r] || __ldg(p.fcol + j) == kNonFiniteLineExp) {
+            s = native_dot(p.X, p.ldx, p.tx, r, p.W, p.ldw, p.tw, (int64_t)p.j0 + j, p.K);
         } else {
-            v = *cp + (v + p.beta);
+            for (int sp = 0; sp < p.splits; sp++) s += p.part[((int64_t)sp * p.rows + r) * NB + j];
         }
-        *cp = v;
+        store_out(p, p.C + r * p.cs_r + (int64_t)j * p.cs_c, s);
     }
 }
 
 // Digits of W columns j0 .. j0+15 (logical K x n; tw: stored n x K), relative
-// to the column exponents: out[(u-1)*16 + jj][k] for u = 1..8, K-major, kp
-// columns, zero beyond n and K.
+// to the column exponents: out[(8-u)*16 + jj][k] for u = 1..8 (the least
+// significant digit first), K-major, kp columns, zero beyond n and K.
 __global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw, int n, int j0, int64_t K,
                                int64_t kp, const int *__restrict__ fcol, unsigned short *__restrict__ out) {
     const int64_t total = (int64_t)NB * kp;
@@ -397,7 +607,7 @@ __global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw
             const unsigned short h =
                 d ? (unsigned short)(__bfloat16_as_ushort(__float2bfloat16_rn(small_int_to_float(d))) | (sg << 15))
                   : 0;
-            out[((int64_t)(u - 1) * NB + jj) * kp + k] = h;
+            out[((int64_t)(S - u) * NB + jj) * kp + k] = h;
         }
     }
 }
@@ -411,7 +621,7 @@ __global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw
 // thin_oz_workspace_bytes() bytes.
 size_t thin_oz_workspace_bytes(int64_t rows, int64_t K, int n, int splits) {
     const int64_t kp = ceil_div(K, thin_oz::KB) * thin_oz::KB;
-    size_t b = (size_t)(rows + 64) * 4 + 256;                            // row exponents (+ column exponents)
+    size_t b = (size_t)(rows + 64) * 4 + 256;                            // row flags (+ column exponents)
     b += (size_t)thin_oz::S * thin_oz::NB * kp * 2 + 256;              // W digit slices of one pass
     if (splits > 1) b += (size_t)splits * rows * thin_oz::NB * 8;      // split-K parts
     (void)n;
@@ -432,8 +642,8 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
     using namespace thin_oz;
     const int64_t kp = ceil_div(K, KB) * KB;
     uint8_t *w8 = (uint8_t *)ws;
-    int *erow = (int *)w8;
-    int *fcol = erow + rows;   // up to 64 columns
+    int *nfrow = (int *)w8;    // split-K: rows holding an Inf / NaN
+    int *fcol = nfrow + rows;  // up to 64 columns
     size_t off = ((size_t)(rows + 64) * 4 + 255) / 256 * 256;
     unsigned short *wd = (unsigned short *)(w8 + off);
     off += ((size_t)S * NB * kp * 2 + 255) / 256 * 256;
@@ -441,10 +651,9 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
     int *err = error_word();
     if (!err) return set_status(GB_ERR_OOM, "skinny: no device error word");
 
-    gb_status s = ozaki_line_exponents(X, ldx, tx != 0, rows, K, erow, st);
+    gb_status s = ozaki_line_exponents(W, ldw, tw == 0, n, K, fcol, st);
     if (s != GB_OK) return s;
-    s = ozaki_line_exponents(W, ldw, tw == 0, n, K, fcol, st);
-    if (s != GB_OK) return s;
+    if (splits > 1) GB_CUDA_TRY(cudaMemsetAsync(nfrow, 0, (size_t)rows * 4, st));
 
     CUtensorMap tx_map, tw_map;
     const bool okx = tx ? make_tmap_f64(&tx_map, X, (uint64_t)rows, (uint64_t)K, (uint64_t)ldx * 8, BM, 16, false)
@@ -468,7 +677,8 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
         wdigits_kernel<<<blocks, 256, 0, st>>>(W, ldw, tw, n, j0, K, kp, fcol + j0, wd);
         GB_LAUNCH_CHECK("wdigits_kernel");
         OzThinParams p{rows, K, nc, splits, (int)(kchunk / KB), rtiles,
-                       C + j0 * cs_c, cs_r, cs_c, alpha, beta, semantics, part, erow, fcol + j0, err};
+                       C + j0 * cs_c, cs_r, cs_c, alpha, beta, semantics, part, nfrow, fcol + j0, err,
+                       X, W, ldx, ldw, tx, tw, j0};
         if (tx) thin_oz_kernel<true><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
         else thin_oz_kernel<false><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
         GB_LAUNCH_CHECK("thin_oz_kernel");

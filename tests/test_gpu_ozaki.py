@@ -134,3 +134,35 @@ def test_ozaki_k_chunked_matches_unchunked_error(torch):
     rows, cols = np.arange(0, M, 20), np.arange(0, N, 4)
     err, _ = oracle.normwise_error(host(dC), "N", "N", M, N, K, 1.0, A, K, B, N, -1.0, C0, N, rows, cols)
     assert err <= 2 * K * 2.0 ** -53, err
+
+
+@pytest.mark.parametrize("mode", ["NN", "TN", "NT", "TT"])
+def test_ozaki_nonfinite_propagate(torch, mode):
+    """Inf and NaN in a row of op(A) or a column of op(B) reach exactly the
+    outputs that IEEE arithmetic gives them (those outputs are recomputed as
+    plain dot products); the others keep FP64-level accuracy."""
+    import gbblas
+    ta, tb = mode
+    M, N, K = 300, 260, 700
+    rng = np.random.default_rng(11)
+    opA = rng.uniform(-1, 1, (M, K))
+    opB = rng.uniform(-1, 1, (K, N))
+    opA[7, 100] = np.inf
+    opA[M - 1, 0] = np.nan
+    opB[9, 33] = -np.inf
+    opB[K - 1, N - 1] = np.nan
+    opA[150, 4] = opA[150, 5] = np.inf      # Inf + (-Inf) -> NaN in output (150, 200)
+    opB[4, 200], opB[5, 200] = 1.0, -1.0
+    A = np.ascontiguousarray(opA.T if ta == "T" else opA)
+    B = np.ascontiguousarray(opB.T if tb == "T" else opB)
+    want = opA @ opB
+    dC = dev(np.zeros((M, N)))
+    gbblas.dgemm(ta, tb, M, N, K, 1.0, dev(A), A.shape[1], dev(B), B.shape[1], 0.0, dC, N,
+                 algo=gbblas.ALGO_OZAKI, ozaki_slices=7)
+    got = host(dC)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    inf = np.isinf(want)
+    assert np.array_equal(np.isinf(got), inf)
+    assert np.array_equal(np.sign(got[inf]), np.sign(want[inf]))
+    fin = np.isfinite(want)
+    assert np.abs(got[fin] - want[fin]).max() <= 1e-12 * np.abs(want[fin]).max()

@@ -109,3 +109,65 @@ def test_thin_f64_deterministic(torch):
         gbblas.dgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=gbblas.ALGO_SKINNY)
         outs.append(host(dC))
     assert outs[0].tobytes() == outs[1].tobytes()
+
+
+@pytest.mark.parametrize("kind", ["thinB", "shortA"])
+@pytest.mark.parametrize("xscale,wscale", [(-1000, 0), (-1060, 500), (600, -700)])
+def test_thin_f64_exact_on_scaled_integers(torch, kind, xscale, wscale):
+    """Small integers times 2^xscale (tiny and subnormal rows take the general
+    mantissa path, normal rows the fast one; one warp mixes both) and W times
+    2^wscale: the products stay exact, so the result must be bit-exact."""
+    import gbblas
+    big, small, K = 1000, 16, 700
+    M, N = (big, small) if kind == "thinB" else (small, big)
+    A = _ints(M, K, 5, K)
+    B = _ints(K, N, 6, N)
+    # the large operand gets the scale on every other row / column of 32
+    if kind == "thinB":
+        A[::2] *= 2.0 ** xscale
+        B *= 2.0 ** wscale
+    else:
+        B[:, ::2] *= 2.0 ** xscale
+        A *= 2.0 ** wscale
+    want = A @ B
+    dC = dev(np.zeros((M, N), np.float64))
+    gbblas.dgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=gbblas.ALGO_SKINNY)
+    got = host(dC)
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (kind, bad[:5], got[tuple(bad[0])] if bad.size else None)
+
+
+def _check_nonfinite(got, want):
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    inf = np.isinf(want)
+    assert np.array_equal(np.isinf(got), inf)
+    assert np.array_equal(np.sign(got[inf]), np.sign(want[inf]))
+    fin = np.isfinite(want)
+    scale = np.abs(want[fin]).max()
+    assert np.abs(got[fin] - want[fin]).max() <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("kind", ["thinB", "shortA"])
+@pytest.mark.parametrize("mode", ["NN", "TT"])
+def test_thin_f64_nonfinite_propagate(torch, kind, mode):
+    """An Inf or a NaN in the large operand's line or in a column of the
+    small one reaches exactly the outputs that IEEE arithmetic gives it."""
+    import gbblas
+    ta, tb = mode
+    big, small, K = 900, 24, 513
+    M, N = (big, small) if kind == "thinB" else (small, big)
+    rng = np.random.default_rng(7)
+    opA = rng.uniform(-1, 1, (M, K))
+    opB = rng.uniform(-1, 1, (K, N))
+    opA[M // 3, 17] = np.inf
+    opA[M - 1, K - 1] = np.nan
+    opB[5, N // 2] = -np.inf
+    opB[K // 2, 0] = np.nan
+    opA[M // 2, 3] = opA[M // 2, 4] = np.inf      # Inf + (-Inf) -> NaN in one output
+    opB[3, N - 1], opB[4, N - 1] = 1.0, -1.0
+    A = np.ascontiguousarray(opA.T if ta == "T" else opA)
+    B = np.ascontiguousarray(opB.T if tb == "T" else opB)
+    want = opA @ opB
+    dC = dev(np.zeros((M, N), np.float64))
+    gbblas.dgemm(ta, tb, M, N, K, 1.0, dev(A), A.shape[1], dev(B), B.shape[1], 0.0, dC, N, algo=gbblas.ALGO_SKINNY)
+    _check_nonfinite(host(dC), want)
