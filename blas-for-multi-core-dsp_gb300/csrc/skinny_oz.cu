@@ -258,7 +258,61 @@ __device__ __forceinline__ double mul_pow2(double x, int k) {
     return x * pow2_or_zero(a) * pow2_or_zero(b) * pow2_or_zero(c);
 }
 
+// X leading dimensions that TMA cannot describe (odd, or a base that is not
+// 16-byte aligned): the producer warp copies k block kb of row tile rt with
+// 8-byte cp.async into the layout the TMA boxes have (two 16-k boxes, SW128
+// rows or [16 k][128 rows]), lane = k (row-major X: one row per instruction,
+// 256 contiguous bytes) or lane = row (K-major X: 32 rows of one k), zeros
+// outside X.
 template <bool XCOLS>
+__device__ __forceinline__ void copy_x_block(uint32_t st, const OzThinParams &p, int rt, int kb, int lane) {
+    const int64_t r0 = (int64_t)rt * BM, k0 = (int64_t)kb * KB;
+    const bool full_tile = r0 + BM <= p.rows && k0 + KB <= p.K;
+    if (XCOLS) {   // k line k: rows r0 + 32q + lane, 256 contiguous bytes per q
+        const double *src = p.X + k0 * p.ldx + r0 + lane;
+        const uint32_t dst = st + (uint32_t)lane * 8;
+        if (full_tile) {
+#pragma unroll 4
+            for (int k = 0; k < KB; k++, src += p.ldx) {
+                const uint32_t d = dst + (uint32_t)((k / 16) * (XS / 2) + (k % 16) * BM * 8);
+#pragma unroll
+                for (int q = 0; q < BM / 32; q++) ptx::cp_async8(d + q * 256, src + 32 * q, 8u);
+            }
+        } else {
+            for (int k = 0; k < KB; k++, src += p.ldx) {
+                const uint32_t d = dst + (uint32_t)((k / 16) * (XS / 2) + (k % 16) * BM * 8);
+                const bool kin = k0 + k < p.K;
+#pragma unroll
+                for (int q = 0; q < BM / 32; q++) {
+                    const bool in = kin && r0 + 32 * q + lane < p.rows;
+                    ptx::cp_async8(d + q * 256, in ? src + 32 * q : p.X, in ? 8u : 0u);
+                }
+            }
+        }
+    } else {       // row r: k0 + lane, 256 contiguous bytes per row; SW128 chunk (lane/2)%8 ^ r%8
+        const double *src = p.X + r0 * p.ldx + k0 + lane;
+        const int c = (lane % 16) / 2;
+        const uint32_t dst = st + (uint32_t)((lane / 16) * (XS / 2) + (lane & 1) * 8);
+        if (full_tile) {
+            for (int r8 = 0; r8 < BM; r8 += 8) {
+#pragma unroll
+                for (int j = 0; j < 8; j++, src += p.ldx)
+                    ptx::cp_async8(dst + (uint32_t)((r8 + j) * 128 + ((c ^ j) << 4)), src, 8u);
+            }
+        } else {
+            const bool kin = k0 + lane < p.K;
+            for (int r8 = 0; r8 < BM; r8 += 8) {
+#pragma unroll
+                for (int j = 0; j < 8; j++, src += p.ldx) {
+                    const bool in = kin && r0 + r8 + j < p.rows;
+                    ptx::cp_async8(dst + (uint32_t)((r8 + j) * 128 + ((c ^ j) << 4)), in ? src : p.X, in ? 8u : 0u);
+                }
+            }
+        }
+    }
+}
+
+template <bool XCOLS, bool CPA>
 __global__ void __launch_bounds__(NT, 1)
     thin_oz_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, OzThinParams p) {
     extern __shared__ uint8_t smem_raw[];
@@ -282,11 +336,11 @@ __global__ void __launch_bounds__(NT, 1)
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
-            ptx::mbar_init(&full[s], 1);
+            ptx::mbar_init(&full[s], CPA ? 33 : 1);   // (the 32 copying lanes +) the W box's expect_tx
             ptx::mbar_init(&empty[s], 1 + NCONV);   // the MMA commit + the converter warps
         }
         for (int s = 0; s < SSTAGES; s++) {
-            ptx::mbar_init(&sfull[s], 1);
+            ptx::mbar_init(&sfull[s], CPA ? 32 : 1);
             ptx::mbar_init(&sempty[s], 4);
         }
         for (int a = 0; a < 2; a++) {
@@ -307,10 +361,12 @@ __global__ void __launch_bounds__(NT, 1)
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0 || warp == 14) {
-        if (lane == 0) {   // TMA producers: warp 0 the converter stages (X + W digits), warp 14 the scan ring
-            const bool scan = warp == 14;
-            const int nst = scan ? SSTAGES : STAGES;
-            uint64_t *fb = scan ? sfull : full, *eb = scan ? sempty : empty;
+        // producers: warp 0 the converter stages (X + W digits), warp 14 the scan ring; X by TMA
+        // (lane 0) or, for leading dimensions TMA cannot take, by cp.async from all lanes
+        const bool scan = warp == 14;
+        const int nst = scan ? SSTAGES : STAGES;
+        uint64_t *fb = scan ? sfull : full, *eb = scan ? sempty : empty;
+        if (CPA || lane == 0) {
             int g = 0;
             bool go = true;
             for (int u = blockIdx.x; u < units && go; u += gridDim.x) {
@@ -323,13 +379,21 @@ __global__ void __launch_bounds__(NT, 1)
                         break;
                     }
                     uint8_t *st = scan ? sring + s * XS : smem + s * STAGE;
-                    ptx::mbar_arrive_expect_tx(&fb[s], scan ? XS : XS + WS);
+                    if (lane == 0 && !(CPA && scan)) {   // TMA bytes: X boxes (TMA loads) + the W digit box
+                        ptx::mbar_arrive_expect_tx(&fb[s], (CPA ? 0 : XS) + (scan ? 0 : WS));
+                        if (!CPA) {
 #pragma unroll
-                    for (int b = 0; b < 2; b++) {
-                        if (XCOLS) ptx::tma_load_2d(st + b * (XS / 2), &tmx, &fb[s], rt * BM, kb * KB + 16 * b);
-                        else ptx::tma_load_2d(st + b * (XS / 2), &tmx, &fb[s], kb * KB + 16 * b, rt * BM);
+                            for (int b = 0; b < 2; b++) {
+                                if (XCOLS) ptx::tma_load_2d(st + b * (XS / 2), &tmx, &fb[s], rt * BM, kb * KB + 16 * b);
+                                else ptx::tma_load_2d(st + b * (XS / 2), &tmx, &fb[s], kb * KB + 16 * b, rt * BM);
+                            }
+                        }
+                        if (!scan) ptx::tma_load_2d(st + XS, &tmw, &fb[s], kb * KB, 0);
                     }
-                    if (!scan) ptx::tma_load_2d(st + XS, &tmw, &fb[s], kb * KB, 0);
+                    if (CPA) {
+                        copy_x_block<XCOLS>(ptx::smem_u32(st), p, rt, kb, lane);
+                        ptx::cp_async_mbar_arrive_noinc(&fb[s]);
+                    }
                 }
             }
         }
@@ -632,8 +696,8 @@ bool thin_oz_eligible(int tx, int64_t ldx, const void *X, int64_t rows, int64_t 
     const char *e = getenv("GB_SKINNY_OZ");   // "0": native FP64 kernels (measurement)
     if (e && e[0] == '0') return false;
     (void)tx;
-    return K >= 64 && rows < (int64_t(1) << 31) && K < (int64_t(1) << 30) && ldx % 2 == 0 &&
-           (uintptr_t)X % 16 == 0;
+    (void)ldx;
+    return K >= 64 && rows < (int64_t(1) << 31) && K < (int64_t(1) << 30) && (uintptr_t)X % 8 == 0;
 }
 
 gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, int tx, const double *W, int64_t ldw,
@@ -655,16 +719,23 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
     if (s != GB_OK) return s;
     if (splits > 1) GB_CUDA_TRY(cudaMemsetAsync(nfrow, 0, (size_t)rows * 4, st));
 
+    // X through TMA when its rows (or k lines) start on 16-byte boundaries, else by cp.async
+    const char *force = getenv("GB_SKINNY_OZ_CPASYNC");   // "1": the cp.async loader for any X (tests)
+    const bool cpa = ldx % 2 != 0 || (uintptr_t)X % 16 != 0 || (force && force[0] == '1');
     CUtensorMap tx_map, tw_map;
-    const bool okx = tx ? make_tmap_f64(&tx_map, X, (uint64_t)rows, (uint64_t)K, (uint64_t)ldx * 8, BM, 16, false)
-                        : make_tmap_f64(&tx_map, X, (uint64_t)K, (uint64_t)rows, (uint64_t)ldx * 8, 16, BM, true);
     const bool okw = make_tmap_bf16(&tw_map, wd, (uint64_t)kp, (uint64_t)S * NB, (uint64_t)kp * 2, KB, S * NB, 64);
+    bool okx = true;
+    if (cpa) tx_map = tw_map;   // unused
+    else if (tx) okx = make_tmap_f64(&tx_map, X, (uint64_t)rows, (uint64_t)K, (uint64_t)ldx * 8, BM, 16, false);
+    else okx = make_tmap_f64(&tx_map, X, (uint64_t)K, (uint64_t)rows, (uint64_t)ldx * 8, 16, BM, true);
     if (!okx || !okw) return set_status(GB_ERR_CUDA, "skinny: cuTensorMapEncodeTiled failed");
 
     static bool attr = false;
     if (!attr) {
-        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
-        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
         attr = true;
     }
     const int rtiles = (int)ceil_div(rows, BM);
@@ -679,8 +750,10 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
         OzThinParams p{rows, K, nc, splits, (int)(kchunk / KB), rtiles,
                        C + j0 * cs_c, cs_r, cs_c, alpha, beta, semantics, part, nfrow, fcol + j0, err,
                        X, W, ldx, ldw, tx, tw, j0};
-        if (tx) thin_oz_kernel<true><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
-        else thin_oz_kernel<false><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
+        if (tx && cpa) thin_oz_kernel<true, true><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
+        else if (tx) thin_oz_kernel<true, false><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
+        else if (cpa) thin_oz_kernel<false, true><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
+        else thin_oz_kernel<false, false><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
         GB_LAUNCH_CHECK("thin_oz_kernel");
         if (splits > 1) {
             const int rb = (int)(ceil_div(rows * nc, 256) < 4 * sm_count() ? ceil_div(rows * nc, 256) : 4 * sm_count());
