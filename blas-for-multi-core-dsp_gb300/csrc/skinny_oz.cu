@@ -24,9 +24,9 @@
 //   pass 2 (thin_oz_kernel, per 16 columns of W):
 //     warp 0     TMA: 128 rows x 32 k of X (FP64) + the 8 digit tiles of W;
 //     warp 14    TMA: the same X boxes, one chunk ahead, for the scan;
-//     warps 10-13 scan chunk c+1 (thread = row: the maximum |x| bit
-//                pattern -> e_rc in shared memory), then drain chunk c:
-//                level sums -> FP64, and the epilogue;
+//     warp 15    scan of chunk c+1 (four rows per lane: the maximum |x| bit
+//                pattern -> e_rc in shared memory);
+//     warps 10-13 drain chunk c: level sums -> FP64, and the epilogue;
 //     warps 2-9  converters, two per TMEM lane quarter (one per 16-k box),
 //                thread = row: the row's values -> 8 digit slices written
 //                into tensor memory (the A operand of the MMA, never in
@@ -61,27 +61,37 @@ namespace {
 namespace thin_oz {
 
 // warps: 0 TMA (converter stages), 1 MMA, 2-9 converters (two per TMEM lane
-// quarter, one per 16-k box), 10-13 scan + drain / epilogue, 14 TMA (scan)
-constexpr int BM = 128, KB = 32, S = 8, NB = 16, STAGES = 4, SSTAGES = 2, CHUNK_KB = 8, NCONV = 8, NT = 480;
+// quarter, one per 16-k box), 10-13 drain / epilogue, 14 TMA (scan ring),
+// 15 scan
+constexpr int BM = 128, KB = 32, S = 8, NB = 16, SSTAGES = 2, CHUNK_KB = 8, NCONV = 8, NT = 512;
 constexpr uint32_t LV_COLS = S * NB;        // 128: one set of level accumulators (level L at (S+1-L)*NB)
 constexpr uint32_t SLOT0 = 2 * LV_COLS;     // 256: digit slots (digit t at +16(t-1)), two of them
 constexpr uint32_t SLOT_COLS = S * 16;      // 128
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int XS = BM * KB * 8;             // 32 KB: two 16-k boxes of FP64
-constexpr int WS = S * NB * KB * 2;         // 8 KB: the 8 digit tiles of W (16 rows of 64 bytes each), u = 8 .. 1
-constexpr int STAGE = XS + WS;
 constexpr int BAR_BYTES = 512, EXP_BYTES = 2 * BM * 4;
-constexpr int SMEM = STAGES * STAGE + SSTAGES * XS + 1024 /*align*/ + BAR_BYTES + EXP_BYTES;
 constexpr int NO_EXP = -100000;             // chunk exponent of an all-zero row chunk
-static_assert(SMEM <= 232448, "shared memory");
+
+// NG groups of 16 columns of W per pass.  NG = 1: two level sets alternate per
+// chunk (tensor memory: 2 x 128 level columns + 2 x 128 digit-slot columns);
+// NG = 2: one level set per column group, drained in place between chunks.
+template <int NG>
+struct Cfg {
+    static constexpr int STAGES = NG == 1 ? 4 : 3;
+    static constexpr int WS = NG * S * NB * KB * 2;   // 8 KB per group: 8 digit tiles of 16 rows x 64 bytes, u = 8 .. 1
+    static constexpr int STAGE = XS + WS;
+    static constexpr int SMEM = STAGES * STAGE + SSTAGES * XS + 1024 /*align*/ + BAR_BYTES + EXP_BYTES;
+    static_assert(SMEM <= 232448, "shared memory");
+};
 
 struct OzThinParams {
     int64_t rows, K;
-    int n, splits, kchunk_kb, rtiles;       // kchunk_kb: a multiple of CHUNK_KB
+    int n, splits, kchunk_kb, rtiles;       // kchunk_kb: a multiple of CHUNK_KB; n <= 16 NG
+    int pw;                                 // columns of the pass: 16 NG
     double *C; int64_t cs_r, cs_c;
     double alpha, beta;
     int semantics;
-    double *part;                           // splits x rows x NB sums (split-K)
+    double *part;                           // splits x rows x pw sums (split-K)
     int *nfrow;                             // split-K: rows that hold an Inf / NaN
     const int *fcol;
     int *err;
@@ -242,6 +252,25 @@ __device__ __forceinline__ void load_row16(const uint8_t *box, int r, double (&x
     }
 }
 
+// The 8 values k = 8h .. 8h+7 of row r in one 16-k box of X (layouts as
+// load_row16).
+template <bool XCOLS>
+__device__ __forceinline__ void load_row8(const uint8_t *box, int r, int h, double (&x)[8]) {
+    if (XCOLS) {
+        const double *xs = reinterpret_cast<const double *>(box) + 8 * h * BM;
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = xs[k * BM + r];
+    } else {
+        const uint8_t *rowp = box + r * 128;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const double2 v = *reinterpret_cast<const double2 *>(rowp + (((4 * h + c) ^ (r & 7)) << 4));
+            x[2 * c] = v.x;
+            x[2 * c + 1] = v.y;
+        }
+    }
+}
+
 // 2^k as a double for k >= -1022, 0 below
 __device__ __forceinline__ double pow2_or_zero(int k) {
     return k >= -1022 ? __longlong_as_double((long long)(1023 + k) << 52) : 0.0;
@@ -312,9 +341,10 @@ __device__ __forceinline__ void copy_x_block(uint32_t st, const OzThinParams &p,
     }
 }
 
-template <bool XCOLS, bool CPA>
+template <bool XCOLS, bool CPA, int NG>
 __global__ void __launch_bounds__(NT, 1)
     thin_oz_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, OzThinParams p) {
+    constexpr int STAGES = Cfg<NG>::STAGES, STAGE = Cfg<NG>::STAGE, WS = Cfg<NG>::WS;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *sring = smem + STAGES * STAGE;
@@ -322,12 +352,13 @@ __global__ void __launch_bounds__(NT, 1)
     uint64_t *empty = full + STAGES;
     uint64_t *aready = empty + STAGES;     // [2] digit slots
     uint64_t *aempty = aready + 2;
-    uint64_t *lfull = aempty + 2;          // [2] level sets
+    uint64_t *lfull = aempty + 2;          // [2] level sets (NG = 1: alternating; NG = 2: one per group)
     uint64_t *lempty = lfull + 2;
     uint64_t *sfull = lempty + 2;          // [SSTAGES] scan ring
     uint64_t *sempty = sfull + SSTAGES;
-    uint64_t *xready = sempty + SSTAGES;   // [2] chunk exponents
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(xready + 2);
+    uint64_t *xready = sempty + SSTAGES;   // [2] chunk exponents written
+    uint64_t *xfree = xready + 2;          // [2] chunk exponents read (converters + drain)
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(xfree + 2);
     int *exps = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(full) + BAR_BYTES);   // [2][BM]
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -341,14 +372,15 @@ __global__ void __launch_bounds__(NT, 1)
         }
         for (int s = 0; s < SSTAGES; s++) {
             ptx::mbar_init(&sfull[s], CPA ? 32 : 1);
-            ptx::mbar_init(&sempty[s], 4);
+            ptx::mbar_init(&sempty[s], 1);
         }
         for (int a = 0; a < 2; a++) {
             ptx::mbar_init(&aready[a], NCONV);
             ptx::mbar_init(&aempty[a], 1);
             ptx::mbar_init(&lfull[a], 1);
             ptx::mbar_init(&lempty[a], 4);
-            ptx::mbar_init(&xready[a], 4);
+            ptx::mbar_init(&xready[a], 1);
+            ptx::mbar_init(&xfree[a], NCONV + 4);
         }
         ptx::fence_mbar_init();
         ptx::tma_prefetch_desc(&tmx);
@@ -405,15 +437,9 @@ __global__ void __launch_bounds__(NT, 1)
                 const int sp = u % p.splits;
                 const int kb0 = sp * p.kchunk_kb, kb1 = min(nkb, kb0 + p.kchunk_kb);
                 for (int c0 = kb0; c0 < kb1 && go; c0 += CHUNK_KB, ch++) {
-                    const int lb = ch & 1;
-                    if (ch >= 2 && !ptx::mbar_wait(&lempty[lb], ((ch >> 1) & 1) ^ 1, p.err, 62)) {
-                        go = false;
-                        break;
-                    }
-                    ptx::tc_fence_after();
-                    const uint32_t lv = tmem + (uint32_t)(lb * LV_COLS);
                     const int c1 = min(kb1, c0 + CHUNK_KB);
-                    for (int kb = c0; kb < c1; kb++, g++) {
+                    const int use = NG == 1 ? (ch >> 1) : ch;   // earlier uses of this chunk's level sets
+                    for (int kb = c0; kb < c1 && go; kb++, g++) {
                         const int s = g % STAGES, a = g & 1;
                         if (!ptx::mbar_wait(&full[s], (g / STAGES) & 1, p.err, 63) ||
                             !ptx::mbar_wait(&aready[a], (g >> 1) & 1, p.err, 64)) {
@@ -424,22 +450,39 @@ __global__ void __launch_bounds__(NT, 1)
                         const uint32_t wst = ptx::smem_u32(smem + s * STAGE + XS);
                         const uint32_t slot = tmem + SLOT0 + (uint32_t)(a * SLOT_COLS);
 #pragma unroll
-                        for (int kk = 0; kk < KB / 16; kk++) {
+                        for (int gr = 0; gr < NG; gr++) {
+                            const int lb = NG == 1 ? (ch & 1) : gr;
+                            if (kb == c0 && use >= 1) {   // the drain has read this level set's last chunk
+                                if (!ptx::mbar_wait(&lempty[lb], (use & 1) ^ 1, p.err, 62)) {
+                                    go = false;
+                                    break;
+                                }
+                                ptx::tc_fence_after();
+                            }
+                            const uint32_t lv = tmem + (uint32_t)(lb * LV_COLS);
+                            const uint32_t wg = wst + (uint32_t)(gr * S * NB * 64);
 #pragma unroll
-                            for (int t = 1; t <= S; t++) {
-                                // W digits u = 9-t .. 1: tile rows 16(t-1) .. 127, N = 16(9-t); the first
-                                // MMA of a chunk (t = 1, N = 128) writes every level column
-                                const uint64_t bdesc = ptx::sdesc_kmajor_sw64(wst + (uint32_t)((t - 1) * NB * 64)) +
-                                                       (uint64_t)((kk * 32) >> 4);
-                                ptx::umma_f16_ta(lv, slot + (uint32_t)((t - 1) * 16 + kk * 8), bdesc,
-                                                 ptx::idesc_bf16_f32(BM, NB * (S + 1 - t)),
-                                                 (kb != c0 || kk != 0 || t != 1) ? 1u : 0u);
+                            for (int kk = 0; kk < KB / 16; kk++) {
+#pragma unroll
+                                for (int t = 1; t <= S; t++) {
+                                    // W digits u = 9-t .. 1: tile rows 16(t-1) .. 127, N = 16(9-t); the first
+                                    // MMA of a chunk (t = 1, N = 128) writes every level column
+                                    const uint64_t bdesc = ptx::sdesc_kmajor_sw64(wg + (uint32_t)((t - 1) * NB * 64)) +
+                                                           (uint64_t)((kk * 32) >> 4);
+                                    ptx::umma_f16_ta(lv, slot + (uint32_t)((t - 1) * 16 + kk * 8), bdesc,
+                                                     ptx::idesc_bf16_f32(BM, NB * (S + 1 - t)),
+                                                     (kb != c0 || kk != 0 || t != 1) ? 1u : 0u);
+                                }
                             }
                         }
+                        if (!go) break;
                         ptx::umma_commit(&empty[s]);
                         ptx::umma_commit(&aempty[a]);
                     }
-                    if (go) ptx::umma_commit(&lfull[lb]);
+                    if (go) {
+#pragma unroll
+                        for (int gr = 0; gr < NG; gr++) ptx::umma_commit(&lfull[NG == 1 ? (ch & 1) : gr]);
+                    }
                 }
             }
         }
@@ -461,6 +504,8 @@ __global__ void __launch_bounds__(NT, 1)
                         break;
                     }
                     e = exps[xs * BM + r];
+                    __syncwarp();
+                    if (lane == 0) ptx::mbar_arrive(&xfree[xs]);
                     if (e == NO_EXP) e = 0;
                     fast = __all_sync(0xFFFFFFFFu, e >= -974);
                     ch++;
@@ -494,111 +539,81 @@ __global__ void __launch_bounds__(NT, 1)
                 }
             }
         }
-    } else if (warp < 14) {  // scan chunk c+1, drain chunk c, epilogue: thread = row q*32 + lane of the tile
+    } else if (warp < 14) {  // drain chunk c, epilogue: thread = row q*32 + lane of the tile
         const int q = warp % 4, r = q * 32 + lane;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        Walk sw, dw;
-        sw.first(p, nkb);
+        Walk dw;
         dw.first(p, nkb);
-        int sg = 0, sch = 0;            // scan-ring k blocks, scanned chunks
-        int ex0 = NO_EXP, ex1 = NO_EXP;  // this row's exponents of the chunks in slots 0 / 1
         bool go = true;
-        // scan of the chunk at sw: the row's maximum |x| bit pattern -> its exponent
-        auto scan = [&]() -> bool {
-            // the largest |high word| gives the exponent unless it is subnormal; then the
-            // bit length of the largest |x| is that of the OR of all (high, low) words
-            uint32_t mx = 0, lor = 0;
-            for (int kb = sw.c0; kb < sw.c1(); kb++, sg++) {
-                const int s = sg % SSTAGES;
-                if (!ptx::mbar_wait(&sfull[s], (sg / SSTAGES) & 1, p.err, 69)) return false;
+        double acc[NG * NB];
 #pragma unroll
-                for (int bx = 0; bx < 2; bx++) {
-                    double x[16];
-                    load_row16<XCOLS>(sring + s * XS + bx * (XS / 2), r, x);
-#pragma unroll
-                    for (int k = 0; k < 16; k += 2) {
-                        const uint32_t h0 = (uint32_t)__double2hiint(x[k]) & 0x7FFFFFFFu;
-                        const uint32_t h1 = (uint32_t)__double2hiint(x[k + 1]) & 0x7FFFFFFFu;
-                        mx = __vimax3_u32(mx, h0, h1);
-                        lor |= (uint32_t)__double2loint(x[k]) | (uint32_t)__double2loint(x[k + 1]);
-                    }
-                }
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(&sempty[s]);
-            }
-            int e;
-            if (mx >> 20) e = (int)(mx >> 20) - 1022;                  // normal, Inf, NaN
-            else if (mx) e = 64 - __clz(mx) - 1074;                    // subnormal, high word set
-            else e = lor ? 32 - __clz(lor) - 1074 : NO_EXP;            // subnormal below 2^-1042, or zeros
-            const int xs = sch & 1;
-            exps[xs * BM + r] = e;
-            if (xs) ex1 = e;
-            else ex0 = e;
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&xready[xs]);
-            sch++;
-            sw.next(p, nkb);
-            return true;
-        };
-        if (sw.u < units) go = scan();
-        double acc[NB];
-#pragma unroll
-        for (int j = 0; j < NB; j++) acc[j] = 0.0;
+        for (int j = 0; j < NG * NB; j++) acc[j] = 0.0;
         int eref = NO_EXP;   // the row's largest chunk exponent so far: acc is in units of 2^eref
         bool nf = false;     // the row holds an Inf / NaN
         for (int ch = 0; go && dw.u < units; ch++) {
-            if (sw.u < units && !scan()) break;
-            const int lb = ch & 1;
-            if (!ptx::mbar_wait(&lfull[lb], (ch >> 1) & 1, p.err, 67)) break;
-            ptx::tc_fence_after();
-            const int ec = lb ? ex1 : ex0;
+            const int xs = ch & 1;
+            if (!ptx::mbar_wait(&xready[xs], (ch >> 1) & 1, p.err, 70)) break;
+            const int ec = exps[xs * BM + r];
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&xfree[xs]);
             nf |= ec == kNonFiniteLineExp;
             if (ec != NO_EXP) {
                 if (eref == NO_EXP) {
                     eref = ec;
                 } else if (ec > eref) {
 #pragma unroll
-                    for (int j = 0; j < NB; j++) acc[j] = mul_pow2(acc[j], eref - ec);
+                    for (int j = 0; j < NG * NB; j++) acc[j] = mul_pow2(acc[j], eref - ec);
                     eref = ec;
                 }
             }
             // T = sum_L S_L 2^(6(9-L)) exactly in 64-bit integers (|S_L| < (L-1) 256 63^2, so
             // |T| < 2^62.1), then one rounding to FP64: sum_L S_L 2^-6L = T 2^-54
             const double sc = pow2_or_zero(ec == NO_EXP ? -100000 : ec - eref - 54);
+            const int use = NG == 1 ? (ch >> 1) : ch;
 #pragma unroll
-            for (int h = 0; h < NB / 8; h++) {   // eight columns at a time
-                long long T[8];
-#pragma unroll
-                for (int j = 0; j < 8; j++) T[j] = 0;
-#pragma unroll
-                for (int L = 2; L <= S + 1; L++) {
-                    uint32_t v[8];
-                    ptx::tmem_ld_32x32b_x8(tmem + lane_off + (uint32_t)(lb * LV_COLS + (S + 1 - L) * NB + 8 * h), v);
-                    ptx::tmem_ld_wait();
-#pragma unroll
-                    for (int j = 0; j < 8; j++) T[j] = T[j] * 64 + (long long)__float2int_rn(__uint_as_float(v[j]));
+            for (int gr = 0; gr < NG; gr++) {
+                const int lb = NG == 1 ? (ch & 1) : gr;
+                if (!ptx::mbar_wait(&lfull[lb], use & 1, p.err, 67)) {
+                    go = false;
+                    break;
                 }
+                ptx::tc_fence_after();
 #pragma unroll
-                for (int j = 0; j < 8; j++) acc[8 * h + j] = fma((double)T[j], sc, acc[8 * h + j]);
+                for (int h = 0; h < NB / 8; h++) {   // eight columns at a time
+                    long long T[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) T[j] = 0;
+#pragma unroll
+                    for (int L = 2; L <= S + 1; L++) {
+                        uint32_t v[8];
+                        ptx::tmem_ld_32x32b_x8(tmem + lane_off + (uint32_t)(lb * LV_COLS + (S + 1 - L) * NB + 8 * h), v);
+                        ptx::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 8; j++) T[j] = T[j] * 64 + (long long)__float2int_rn(__uint_as_float(v[j]));
+                    }
+#pragma unroll
+                    for (int j = 0; j < 8; j++) acc[gr * NB + 8 * h + j] = fma((double)T[j], sc, acc[gr * NB + 8 * h + j]);
+                }
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&lempty[lb]);
             }
-            ptx::tc_fence_before();
-            __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&lempty[lb]);
+            if (!go) break;
             if (dw.last()) {   // the unit's sums are complete
                 const int rt = dw.u / p.splits, sp = dw.u - rt * p.splits;
                 const int64_t row = (int64_t)rt * BM + r;
                 if (row < p.rows) {
                     const int er = eref == NO_EXP ? 0 : eref;
                     if (p.splits > 1) {
-                        double *pp = p.part + ((int64_t)sp * p.rows + row) * NB;
+                        double *pp = p.part + ((int64_t)sp * p.rows + row) * p.pw;
 #pragma unroll
-                        for (int j = 0; j < NB; j++)
+                        for (int j = 0; j < NG * NB; j++)
                             if (j < p.n) pp[j] = mul_pow2(acc[j], er + __ldg(p.fcol + j));
                         if (nf) p.nfrow[row] = 1;
                     } else {
                         double *cr = p.C + row * p.cs_r;
 #pragma unroll
-                        for (int j = 0; j < NB; j++) {
+                        for (int j = 0; j < NG * NB; j++) {
                             if (j >= p.n) break;
                             const int fc = __ldg(p.fcol + j);
                             if (!nf && fc != kNonFiniteLineExp)
@@ -612,11 +627,63 @@ __global__ void __launch_bounds__(NT, 1)
                     }
                 }
 #pragma unroll
-                for (int j = 0; j < NB; j++) acc[j] = 0.0;
+                for (int j = 0; j < NG * NB; j++) acc[j] = 0.0;
                 eref = NO_EXP;
                 nf = false;
             }
             dw.next(p, nkb);
+        }
+    } else if (warp == 15) {   // scan: chunk c+1 while chunk c converts; lane = rows lane + 32i
+        Walk sw;
+        sw.first(p, nkb);
+        int sg = 0;
+        for (int sch = 0; sw.u < units; sch++) {
+            // the largest |high word| gives the exponent unless it is subnormal; then the bit
+            // length of the largest |x| is that of the OR of all (high, low) words
+            uint32_t mx[4] = {0, 0, 0, 0}, lor[4] = {0, 0, 0, 0};
+            // NG = 2 (slower chunks): start once chunk sch - 1 is being converted, at most one
+            // chunk ahead, so that the conversion's re-read of this chunk still finds it in L2
+            // (two chunks ahead doubled the DRAM reads); NG = 1 keeps the scan two ahead
+            const int lag = NG == 2 ? 1 : 2;
+            if (sch >= lag && !ptx::mbar_wait(&xfree[(sch - lag) & 1], ((sch - lag) >> 1) & 1, p.err, 71)) break;
+            bool go = true;
+            for (int kb = sw.c0; kb < sw.c1(); kb++, sg++) {
+                const int s = sg % SSTAGES;
+                if (!ptx::mbar_wait(&sfull[s], (sg / SSTAGES) & 1, p.err, 69)) {
+                    go = false;
+                    break;
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+#pragma unroll
+                    for (int bh = 0; bh < 4; bh++) {
+                        double x[8];
+                        load_row8<XCOLS>(sring + s * XS + (bh >> 1) * (XS / 2), lane + 32 * i, bh & 1, x);
+#pragma unroll
+                        for (int k = 0; k < 8; k += 2) {
+                            const uint32_t h0 = (uint32_t)__double2hiint(x[k]) & 0x7FFFFFFFu;
+                            const uint32_t h1 = (uint32_t)__double2hiint(x[k + 1]) & 0x7FFFFFFFu;
+                            mx[i] = __vimax3_u32(mx[i], h0, h1);
+                            lor[i] |= (uint32_t)__double2loint(x[k]) | (uint32_t)__double2loint(x[k + 1]);
+                        }
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&sempty[s]);
+            }
+            if (!go) break;
+            const int xs = sch & 1;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                int e;
+                if (mx[i] >> 20) e = (int)(mx[i] >> 20) - 1022;                      // normal, Inf, NaN
+                else if (mx[i]) e = 64 - __clz(mx[i]) - 1074;                        // subnormal, high word set
+                else e = lor[i] ? 32 - __clz(lor[i]) - 1074 : NO_EXP;                // tiny subnormal, or zeros
+                exps[xs * BM + lane + 32 * i] = e;
+            }
+            __syncwarp();
+            if (lane == 0) ptx::mbar_arrive(&xready[xs]);
+            sw.next(p, nkb);
         }
     }
 
@@ -640,28 +707,29 @@ __global__ void thin_oz_reduce_kernel(OzThinParams p) {
         if (p.nfrow[r] || __ldg(p.fcol + j) == kNonFiniteLineExp) {
             s = native_dot(p.X, p.ldx, p.tx, r, p.W, p.ldw, p.tw, (int64_t)p.j0 + j, p.K);
         } else {
-            for (int sp = 0; sp < p.splits; sp++) s += p.part[((int64_t)sp * p.rows + r) * NB + j];
+            for (int sp = 0; sp < p.splits; sp++) s += p.part[((int64_t)sp * p.rows + r) * p.pw + j];
         }
         store_out(p, p.C + r * p.cs_r + (int64_t)j * p.cs_c, s);
     }
 }
 
-// Digits of W columns j0 .. j0+15 (logical K x n; tw: stored n x K), relative
-// to the column exponents: out[(8-u)*16 + jj][k] for u = 1..8 (the least
-// significant digit first), K-major, kp columns, zero beyond n and K.
-__global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw, int n, int j0, int64_t K,
+// Digits of W columns j0 .. j0+pw-1 (logical K x n; tw: stored n x K),
+// relative to the column exponents, group by group of 16 columns:
+// out[(g*8 + 8-u)*16 + jj][k] for column j0 + 16g + jj and u = 1..8 (the
+// least significant digit first), K-major, kp columns, zero beyond n and K.
+__global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw, int n, int j0, int pw, int64_t K,
                                int64_t kp, const int *__restrict__ fcol, unsigned short *__restrict__ out) {
-    const int64_t total = (int64_t)NB * kp;
+    const int64_t total = (int64_t)pw * kp;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
-        const int jj = (int)(e / kp);
-        const int64_t k = e - (int64_t)jj * kp;
-        const int j = j0 + jj;
+        const int jp = (int)(e / kp);
+        const int64_t k = e - (int64_t)jp * kp;
+        const int j = j0 + jp, gr = jp / NB, jj = jp % NB;
         double x = 0.0;
         int f = 0;
         if (j < n && k < K) {
             x = tw ? W[(int64_t)j * ldw + k] : W[k * ldw + j];
-            f = fcol[jj];
+            f = fcol[jp];
         }
         uint32_t sg;
         const uint64_t F = scaled_mantissa(x, f, sg);
@@ -671,23 +739,29 @@ __global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw
             const unsigned short h =
                 d ? (unsigned short)(__bfloat16_as_ushort(__float2bfloat16_rn(small_int_to_float(d))) | (sg << 15))
                   : 0;
-            out[((int64_t)(S - u) * NB + jj) * kp + k] = h;
+            out[((int64_t)(gr * S + S - u) * NB + jj) * kp + k] = h;
         }
     }
+}
+
+template <bool XCOLS, bool CPA, int NG>
+cudaError_t set_smem() {
+    return cudaFuncSetAttribute(thin_oz_kernel<XCOLS, CPA, NG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                Cfg<NG>::SMEM);
 }
 
 }  // namespace thin_oz
 }  // namespace
 
 // FP64 skinny product through digits on the tensor cores.  X rows x K
-// (tx: stored K x rows), W K x n (tw: stored n x K), n <= 64 in passes of 16
-// columns, C(r, j) at C[r*cs_r + j*cs_c].  Scratch: `ws` of
+// (tx: stored K x rows), W K x n (tw: stored n x K), n <= 64 in passes of up
+// to 32 columns, C(r, j) at C[r*cs_r + j*cs_c].  Scratch: `ws` of
 // thin_oz_workspace_bytes() bytes.
 size_t thin_oz_workspace_bytes(int64_t rows, int64_t K, int n, int splits) {
     const int64_t kp = ceil_div(K, thin_oz::KB) * thin_oz::KB;
-    size_t b = (size_t)(rows + 64) * 4 + 256;                            // row flags (+ column exponents)
-    b += (size_t)thin_oz::S * thin_oz::NB * kp * 2 + 256;              // W digit slices of one pass
-    if (splits > 1) b += (size_t)splits * rows * thin_oz::NB * 8;      // split-K parts
+    size_t b = (size_t)(rows + 64) * 4 + 256;                                // row flags (+ column exponents)
+    b += (size_t)thin_oz::S * 2 * thin_oz::NB * kp * 2 + 256;              // W digit slices of one pass
+    if (splits > 1) b += (size_t)splits * rows * 2 * thin_oz::NB * 8;      // split-K parts
     (void)n;
     return b;
 }
@@ -705,12 +779,12 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
                          int semantics, int splits, int64_t kchunk, void *ws, cudaStream_t st) {
     using namespace thin_oz;
     const int64_t kp = ceil_div(K, KB) * KB;
-    uint8_t *w8 = (uint8_t *)ws;
+    uint8_t *w8 = (uint8_t *)ws;   // row flags, column exponents, W digits of a pass, split-K parts
     int *nfrow = (int *)w8;    // split-K: rows holding an Inf / NaN
     int *fcol = nfrow + rows;  // up to 64 columns
     size_t off = ((size_t)(rows + 64) * 4 + 255) / 256 * 256;
     unsigned short *wd = (unsigned short *)(w8 + off);
-    off += ((size_t)S * NB * kp * 2 + 255) / 256 * 256;
+    off += ((size_t)S * 2 * NB * kp * 2 + 255) / 256 * 256;
     double *part = splits > 1 ? (double *)(w8 + off) : nullptr;
     int *err = error_word();
     if (!err) return set_status(GB_ERR_OOM, "skinny: no device error word");
@@ -722,44 +796,62 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
     // X through TMA when its rows (or k lines) start on 16-byte boundaries, else by cp.async
     const char *force = getenv("GB_SKINNY_OZ_CPASYNC");   // "1": the cp.async loader for any X (tests)
     const bool cpa = ldx % 2 != 0 || (uintptr_t)X % 16 != 0 || (force && force[0] == '1');
-    CUtensorMap tx_map, tw_map;
-    const bool okw = make_tmap_bf16(&tw_map, wd, (uint64_t)kp, (uint64_t)S * NB, (uint64_t)kp * 2, KB, S * NB, 64);
+    CUtensorMap tx_map, tw_map[2];   // W digit boxes of one or two column groups
+    const bool okw =
+        make_tmap_bf16(&tw_map[0], wd, (uint64_t)kp, (uint64_t)2 * S * NB, (uint64_t)kp * 2, KB, S * NB, 64) &&
+        make_tmap_bf16(&tw_map[1], wd, (uint64_t)kp, (uint64_t)2 * S * NB, (uint64_t)kp * 2, KB, 2 * S * NB, 64);
     bool okx = true;
-    if (cpa) tx_map = tw_map;   // unused
+    if (cpa) tx_map = tw_map[0];   // unused
     else if (tx) okx = make_tmap_f64(&tx_map, X, (uint64_t)rows, (uint64_t)K, (uint64_t)ldx * 8, BM, 16, false);
     else okx = make_tmap_f64(&tx_map, X, (uint64_t)K, (uint64_t)rows, (uint64_t)ldx * 8, 16, BM, true);
     if (!okx || !okw) return set_status(GB_ERR_CUDA, "skinny: cuTensorMapEncodeTiled failed");
 
     static bool attr = false;
     if (!attr) {
-        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
-        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
-        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
-        GB_CUDA_TRY(cudaFuncSetAttribute(thin_oz_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+        GB_CUDA_TRY((set_smem<false, false, 1>()));
+        GB_CUDA_TRY((set_smem<true, false, 1>()));
+        GB_CUDA_TRY((set_smem<false, true, 1>()));
+        GB_CUDA_TRY((set_smem<true, true, 1>()));
+        GB_CUDA_TRY((set_smem<false, false, 2>()));
+        GB_CUDA_TRY((set_smem<true, false, 2>()));
+        GB_CUDA_TRY((set_smem<false, true, 2>()));
+        GB_CUDA_TRY((set_smem<true, true, 2>()));
         attr = true;
     }
     const int rtiles = (int)ceil_div(rows, BM);
     const int units = rtiles * splits;
     const int grid = units < sm_count() ? units : sm_count();
-    for (int j0 = 0; j0 < n; j0 += NB) {   // 16 columns of W per pass over X
-        const int nc = n - j0 < NB ? n - j0 : NB;
-        const int blocks = (int)(ceil_div((int64_t)NB * kp, 256) < 2 * sm_count() ? ceil_div((int64_t)NB * kp, 256)
-                                                                                    : 2 * sm_count());
-        wdigits_kernel<<<blocks, 256, 0, st>>>(W, ldw, tw, n, j0, K, kp, fcol + j0, wd);
+    for (int j0 = 0; j0 < n;) {   // up to 32 columns of W per pass over X
+        const int ng = n - j0 > NB ? 2 : 1;
+        const int pw = ng * NB, nc = n - j0 < pw ? n - j0 : pw;
+        const int64_t wtot = (int64_t)pw * kp;
+        const int blocks = (int)(ceil_div(wtot, 256) < 2 * sm_count() ? ceil_div(wtot, 256) : 2 * sm_count());
+        wdigits_kernel<<<blocks, 256, 0, st>>>(W, ldw, tw, n, j0, pw, K, kp, fcol + j0, wd);
         GB_LAUNCH_CHECK("wdigits_kernel");
-        OzThinParams p{rows, K, nc, splits, (int)(kchunk / KB), rtiles,
+        OzThinParams p{rows, K, nc, splits, (int)(kchunk / KB), rtiles, pw,
                        C + j0 * cs_c, cs_r, cs_c, alpha, beta, semantics, part, nfrow, fcol + j0, err,
                        X, W, ldx, ldw, tx, tw, j0};
-        if (tx && cpa) thin_oz_kernel<true, true><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
-        else if (tx) thin_oz_kernel<true, false><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
-        else if (cpa) thin_oz_kernel<false, true><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
-        else thin_oz_kernel<false, false><<<grid, NT, SMEM, st>>>(tx_map, tw_map, p);
+        const CUtensorMap &twm = tw_map[ng - 1];
+        if (ng == 1) {
+            const int sm = Cfg<1>::SMEM;
+            if (tx && cpa) thin_oz_kernel<true, true, 1><<<grid, NT, sm, st>>>(tx_map, twm, p);
+            else if (tx) thin_oz_kernel<true, false, 1><<<grid, NT, sm, st>>>(tx_map, twm, p);
+            else if (cpa) thin_oz_kernel<false, true, 1><<<grid, NT, sm, st>>>(tx_map, twm, p);
+            else thin_oz_kernel<false, false, 1><<<grid, NT, sm, st>>>(tx_map, twm, p);
+        } else {
+            const int sm = Cfg<2>::SMEM;
+            if (tx && cpa) thin_oz_kernel<true, true, 2><<<grid, NT, sm, st>>>(tx_map, twm, p);
+            else if (tx) thin_oz_kernel<true, false, 2><<<grid, NT, sm, st>>>(tx_map, twm, p);
+            else if (cpa) thin_oz_kernel<false, true, 2><<<grid, NT, sm, st>>>(tx_map, twm, p);
+            else thin_oz_kernel<false, false, 2><<<grid, NT, sm, st>>>(tx_map, twm, p);
+        }
         GB_LAUNCH_CHECK("thin_oz_kernel");
         if (splits > 1) {
             const int rb = (int)(ceil_div(rows * nc, 256) < 4 * sm_count() ? ceil_div(rows * nc, 256) : 4 * sm_count());
             thin_oz_reduce_kernel<<<rb, 256, 0, st>>>(p);
             GB_LAUNCH_CHECK("thin_oz_reduce_kernel");
         }
+        j0 += pw;
     }
     return ok();
 }
