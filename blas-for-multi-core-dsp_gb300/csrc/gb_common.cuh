@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "gbblas.h"
 
 namespace gb {
@@ -49,6 +51,12 @@ int smem_optin();
 // buffer stays valid until the next call on the same stream needs more;
 // work on that stream uses it in stream order.
 void *workspace(size_t bytes, void *stream);
+
+// Per-device one-time setup (kernel attributes such as the dynamic shared
+// memory limit hold per device): `done` has one bit per device.  Running the
+// setup twice is harmless, so concurrent first calls may both do it.
+bool device_setup_needed(const std::atomic<uint64_t> &done);
+void device_setup_done(std::atomic<uint64_t> &done);
 
 // Per-device error word (4 bytes of device memory, zero = no error) that
 // kernels with bounded waits set on timeout; gb_sync() reports and clears it.

@@ -53,6 +53,18 @@ int sm_count() {
     return cache[dev];
 }
 
+static uint64_t device_bit() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return 1ull << (dev & 63);
+}
+
+bool device_setup_needed(const std::atomic<uint64_t> &done) {
+    return (done.load(std::memory_order_acquire) & device_bit()) == 0;
+}
+
+void device_setup_done(std::atomic<uint64_t> &done) { done.fetch_or(device_bit(), std::memory_order_acq_rel); }
+
 int smem_optin() {
     static int cache[kMaxDev] = {0};
     int dev = 0;

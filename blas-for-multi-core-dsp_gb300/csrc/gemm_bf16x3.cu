@@ -921,11 +921,11 @@ gb_status launch(const GemmArgs &g, int *err) {
     if (g.tb) okm = okm && make_tmap_f32(&tB, g.B, g.K, g.N, g.ldb * 4, BK, BN, true);
     else okm = okm && make_tmap_f32(&tB, g.B, g.N, g.K, g.ldb * 4, BN, BK, false);
     if (!okm) return set_status(GB_ERR_CUDA, "bf16x3: cuTensorMapEncodeTiled (FP32) failed");
-    static bool attr[2] = {false, false};
-    if (!attr[0]) {
+    static std::atomic<uint64_t> attr{0};
+    if (device_setup_needed(attr)) {
         GB_CUDA_TRY(cudaFuncSetAttribute(bf16x3_fused_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          C::SMEM));
-        attr[0] = true;
+        device_setup_done(attr);
     }
     Params p;
     p.C = (float *)g.C; p.M = g.M; p.N = g.N; p.ldc = g.ldc;
@@ -1011,11 +1011,11 @@ template <int NP, int BN, bool FOLD>
 static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64_t kp, int *err, int fold_kb,
                                  float *sk_part, int *sk_cnt) {
     using CF = TwoPass<NP, BN>;
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::atomic<uint64_t> attr{0};
+    if (device_setup_needed(attr)) {
         GB_CUDA_TRY(cudaFuncSetAttribute(bf16x3_gemm_kernel<NP, BN, FOLD>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM_BYTES));
-        attr_set = true;
+        device_setup_done(attr);
     }
     const int tiles_m = (int)ceil_div(g.M, BM), tiles_n = (int)ceil_div(g.N, BN);
     const int tiles = tiles_m * tiles_n;

@@ -534,10 +534,10 @@ static gb_status ozaki_one(const GemmArgs &g, int s) {
         }
     p.npairs = n;
 
-    static bool attr_set = false;
-    if (!attr_set) {
+    static std::atomic<uint64_t> attr{0};
+    if (device_setup_needed(attr)) {
         GB_CUDA_TRY(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        attr_set = true;
+        device_setup_done(attr);
     }
     const int tiles = p.tiles_m * p.tiles_n;
     const int grid = tiles < sm_count() ? tiles : sm_count();

@@ -694,11 +694,11 @@ __global__ void wpack_kernel(const float *__restrict__ W, int64_t ldw, int tw, i
 template <int NS, bool XCOLS, bool WT>
 gb_status launch_thin(const thin::TMaps &maps, const thin::TParams &tp, int grid, cudaStream_t st) {
     using CF = thin::TCfg<thin::rows_per_thread<NS>()>;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<uint64_t> attr{0};
+    if (device_setup_needed(attr)) {
         GB_CUDA_TRY(cudaFuncSetAttribute(thin::thin_tma_kernel<NS, XCOLS, WT>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM));
-        attr = true;
+        device_setup_done(attr);
     }
     thin::thin_tma_kernel<NS, XCOLS, WT><<<grid, CF::NTH, CF::SMEM, st>>>(maps, tp);
     GB_LAUNCH_CHECK("thin_tma_kernel");

@@ -806,8 +806,8 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
     else okx = make_tmap_f64(&tx_map, X, (uint64_t)K, (uint64_t)rows, (uint64_t)ldx * 8, 16, BM, true);
     if (!okx || !okw) return set_status(GB_ERR_CUDA, "skinny: cuTensorMapEncodeTiled failed");
 
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<uint64_t> attr{0};
+    if (device_setup_needed(attr)) {
         GB_CUDA_TRY((set_smem<false, false, 1>()));
         GB_CUDA_TRY((set_smem<true, false, 1>()));
         GB_CUDA_TRY((set_smem<false, true, 1>()));
@@ -816,7 +816,7 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
         GB_CUDA_TRY((set_smem<true, false, 2>()));
         GB_CUDA_TRY((set_smem<false, true, 2>()));
         GB_CUDA_TRY((set_smem<true, true, 2>()));
-        attr = true;
+        device_setup_done(attr);
     }
     const int rtiles = (int)ceil_div(rows, BM);
     const int units = rtiles * splits;

@@ -360,11 +360,11 @@ __global__ void wsplit_kernel(const float *__restrict__ W, int64_t ldw, int tw, 
 
 template <int NB, int XL>
 gb_status launch_nb(const ThinTcArgs &a, const Maps &maps, const TcParams &tp, int grid) {
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<uint64_t> attr{0};
+    if (device_setup_needed(attr)) {
         GB_CUDA_TRY(cudaFuncSetAttribute(thin_tc_kernel<NB, XL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          Cfg<NB>::SMEM));
-        attr = true;
+        device_setup_done(attr);
     }
     thin_tc_kernel<NB, XL><<<grid, NT, Cfg<NB>::SMEM, a.stream>>>(maps, tp);
     GB_LAUNCH_CHECK("thin_tc_kernel");
