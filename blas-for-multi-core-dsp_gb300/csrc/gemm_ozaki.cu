@@ -8,14 +8,17 @@
 // counterpart in the reference.
 //
 // Each row i of op(A) is scaled by 2^-e_i (e_i: max_k |a_ik| < 2^e_i) and
-// written as s base-128 digits, a_ik = 2^e_i * sum_t v_ikt 2^-7t (+ a
-// remainder < 2^(e_i-7s)), v in [-127, 127]; columns of op(B) likewise with
-// exponents f_j and digits w.  Then
-//     C_ij ~= 2^(e_i+f_j) sum_{t+u <= s+1} 2^-7(t+u) (V_t W_u^T)_ij .
-// The digits are integers that BF16 holds exactly, so each slice product
-// runs on tcgen05.mma kind::f16 with an FP32 accumulator in TMEM, and every
-// partial sum of a 1024-long K chunk is an integer below 1024*127^2 < 2^24:
-// exact.  Chunk sums are added exactly in int32 registers (up to 127 chunks),
+// written as s balanced base-256 digits, a_ik = 2^(e_i+1) * sum_t v_ikt 2^-8t
+// (+ a remainder below 2^(e_i+1-8s)), v in [-128, 127] (the leading digit
+// in [-128, 128]); columns of op(B) likewise with exponents f_j and digits w.
+// Then
+//     C_ij ~= 2^(e_i+f_j+2) sum_{t+u <= s+1} 2^-8(t+u) (V_t W_u^T)_ij .
+// The digits are integers that BF16 holds exactly (|v| <= 128), so each slice
+// product runs on tcgen05.mma kind::f16 with an FP32 accumulator in TMEM, and
+// every partial sum of a 1024-long K chunk is an integer of magnitude at most
+// 1024*128^2 = 2^24: exact.  Eight bits per slice (balanced digits keep the
+// products within 2^14 although they carry a full byte) give FP64-level
+// results with 7 slices, 28 slice products.  Chunk sums are added exactly in int32 registers (up to 127 chunks),
 // and FP64 appears only in the per-pair scaled sum kept in TMEM and in the
 // final 2^(e_i+f_j), alpha, beta epilogue.  (sm_103a has no kind::i8 MMA, so
 // the INT8 products are carried in BF16; products and sums stay exact.)
@@ -41,13 +44,17 @@ bool make_tmap_bf16(CUtensorMap *map, const void *base, uint64_t inner, uint64_t
                     uint32_t box_inner, uint32_t box_outer, int swizzle_bytes);
 
 int ozaki_pick_slices(double target_err, int64_t K) {
-    // truncation error of the triangular slice sum ~ 2^(-7s) * sqrt(K) * small
-    // constant relative to |A||B|; pick the smallest s meeting the target
-    if (target_err <= 0) target_err = 0x1.0p-52;
+    // Each input is truncated at 2^(1-8s) of its row (column) maximum, so a
+    // product term errs by at most ~2^(2-8s) |a||b|; FP64's own rounding is
+    // u = 2^-53 per term, and both grow like sqrt(K) over a dot product.
+    // target_err 0 (FP64-equivalent): 2^(2-8s) <= u/2, s = 7 (measured on
+    // 8192^3 with entries u*2^e, e in [-20, 20]: 7.56e-18 vs native 7.51e-18).
+    // A target: the smallest s with 2^(2-8s) sqrt(K) * 4 <= target.
+    if (target_err <= 0) return 7;
     double logk = 0;
     for (int64_t k = K; k > 1; k >>= 1) logk += 0.5;
     for (int s = 2; s <= 9; s++)
-        if (-7.0 * s + logk + 2.0 <= __builtin_log2(target_err)) return s;
+        if (2.0 - 8.0 * s + logk + 2.0 <= __builtin_log2(target_err)) return s;
     return 9;
 }
 
@@ -138,10 +145,12 @@ static void launch_maxexp_strided(const double *X, int64_t ld, int64_t cols, int
 }
 
 // ---------------------------------------------------------------- digits
-// s base-128 digits of x * 2^-e (|x| < 2^e), truncated, sign of x, as BF16.
+// s balanced base-256 digits of x (|x| < 2^e): N = +-trunc(|x| 2^(8s-1-e)),
+// |N| < 2^(8s-1), cut from the least significant digit up (d = N mod 256 in
+// [-128, 127], N = (N - d) / 256), so x ~= 2^(e+1) sum_t d_t 2^-8t; the
+// leading digit is in [-128, 128].  Written as BF16, most significant first.
 __device__ __forceinline__ void digits(double x, int e, int s, unsigned short *out, int64_t stride) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned short sign = (unsigned short)((b >> 48) & 0x8000);
     const int E = (int)((b >> 52) & 0x7FF);
     unsigned long long m = b & 0xFFFFFFFFFFFFFull;
     int ex;
@@ -151,14 +160,15 @@ __device__ __forceinline__ void digits(double x, int e, int s, unsigned short *o
         m |= 1ull << 52;
         ex = E - 1075;
     }
-    const int shift = ex + 7 * s - e;   // F = m * 2^shift < 2^(7s) <= 2^63
-    unsigned long long F;
-    if (m == 0 || shift <= -64) F = 0;
-    else if (shift >= 0) F = m << shift;
-    else F = m >> (-shift);
-    for (int t = 1; t <= s; t++) {
-        unsigned v = (unsigned)((F >> (7 * (s - t))) & 0x7F);
-        unsigned short h = v ? (unsigned short)(__bfloat16_as_ushort(__float2bfloat16_rn((float)v)) | sign) : 0;
+    const int shift = ex + 8 * s - 1 - e;   // F = m * 2^shift < 2^(8s-1) <= 2^71
+    unsigned __int128 F = 0;
+    if (m != 0 && shift > -64) F = shift >= 0 ? ((unsigned __int128)m << shift) : (unsigned __int128)(m >> (-shift));
+    __int128 N = (b >> 63) ? -(__int128)F : (__int128)F;
+    for (int t = s; t >= 1; t--) {
+        const int d = (int)(((long long)N + 128) & 255) - 128;
+        N = (N - d) >> 8;
+        const int v = t == 1 ? d + 256 * (int)N : d;   // the leading digit takes what is left (|v| <= 128)
+        const unsigned short h = v ? __bfloat16_as_ushort(__float2bfloat16_rn((float)v)) : 0;
         out[(int64_t)(t - 1) * stride] = h;
     }
 }
@@ -333,7 +343,7 @@ __global__ void __launch_bounds__(NT, 1)
                 int iacc[BN];
 #pragma unroll
                 for (int j = 0; j < BN; j++) iacc[j] = 0;
-                const double scale = __longlong_as_double((long long)(1023 - 7 * (p.pt[qq] + p.pu[qq])) << 52);
+                const double scale = __longlong_as_double((long long)(1023 + 2 - 8 * (p.pt[qq] + p.pu[qq])) << 52);
                 for (int c = 0; c < nchunks; c++, gi++) {
                     const int b = gi & 1;
                     if (!ptx::mbar_wait(&acc_full[b], (gi >> 1) & 1, p.err, 14)) { go = false; break; }
@@ -350,7 +360,7 @@ __global__ void __launch_bounds__(NT, 1)
                     __syncwarp();
                     if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
                     const bool flush = (c == nchunks - 1) || ((c + 1) % MAX_CHUNKS_INT32 == 0);
-                    if (flush) {   // FP64 sum += 2^-7(t+u) * iacc (exact scaling, one rounding)
+                    if (flush) {   // FP64 sum += 2^(2-8(t+u)) * iacc (exact scaling, one rounding)
 #pragma unroll
                         for (int cb = 0; cb < (2 * BN) / 32; cb++) {
                             uint32_t r[32];

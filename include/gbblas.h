@@ -110,9 +110,10 @@ typedef struct gb_gemm_opts {
                               irr_thinB_sgemm V1.2), 0 -> two-level sum        */
     int32_t alpha_on_b;    /* ORDERED: alpha pre-scales op(B) (thinB V1.2)
                               instead of op(A) (sgemm V1.3.x)                  */
-    int32_t ozaki_slices;  /* OZAKI: 7-bit slices per operand (2..9), 0 ->
-                              the fewest meeting target_err                   */
-    double  target_err;    /* OZAKI: normwise error target, 0 -> 2^-52         */
+    int32_t ozaki_slices;  /* OZAKI: 8-bit (balanced) slices per operand
+                              (2..9), 0 -> the fewest meeting target_err      */
+    double  target_err;    /* OZAKI: normwise error target, 0 -> FP64 level
+                              (7 slices)                                      */
     int32_t reserved[4];
 } gb_gemm_opts;
 

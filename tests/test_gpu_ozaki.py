@@ -49,9 +49,10 @@ def test_ozaki_exact_on_integers(torch, mode, M, N, K):
 
 def test_ozaki_exact_products_on_wide_exponents(torch):
     """14 significant bits per entry, exponents spread over +-6 inside each row
-    (at most 26 bits below the row maximum): every entry is at most 4 base-128
-    digits, so with 8 slices every digit product t + u <= 8 is kept and exact;
-    only the FP64 summation of the 36 scaled pair sums rounds."""
+    (at most 26 bits below the row maximum): every entry is at most 4 balanced
+    base-256 digits (7 + 8 + 8 + 8 bits), so with 8 slices every digit
+    product t + u <= 8 is kept and exact; only the FP64 summation of the 36
+    scaled pair sums rounds."""
     import gbblas
     rng = np.random.default_rng(7)
     M, N, K = 160, 144, 700
