@@ -210,9 +210,9 @@ def base_line(ctx, metric, value, unit, ms, steps, dtype, config, hib=True):
             "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config}
 
 
-def memcpy(ctx, dst, src, nbytes, kind):
+def memcpy(ctx, dst, src, nbytes, kind, stream=None):
     st = ctx.gb.lib().gb_memcpy(ctypes.c_void_p(dst.data_ptr()), ctypes.c_void_p(src.data_ptr()), nbytes, kind,
-                                ctypes.c_void_p(ctx.stream.cuda_stream))
+                                ctypes.c_void_p((stream or ctx.stream).cuda_stream))
     assert st == 0, ctx.gb.lib().gb_last_error()
 
 
@@ -424,19 +424,41 @@ def run_sgemm(ctx):
                                     if other == "bf16x6" else "three BF16 products per FP32 product")
 
     pin = {k: v.cpu().pin_memory() for k, v in bufs.items()}
-    hostC = torch.empty((M, LD), dtype=torch.float32).pin_memory()
+    hostC = [torch.empty((M, LD), dtype=torch.float32).pin_memory() for _ in range(2)]
     nbytes = M * LD * 4
+    # End to end, pipelined over the four modes as a caller would: mode i+1's operands go up on
+    # one stream while mode i computes and mode i-1's C comes down on another (the host link
+    # carries both directions at once); device operands are double-buffered by mode parity.
+    slots = [{k: torch.empty_like(bufs["C"]) for k in ("A", "B", "C")} for _ in range(2)]
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
 
     def step_host():
         h2d = d2h = 0
-        for mode in MODES:
+        e0 = torch.cuda.Event()
+        e0.record(ctx.stream)
+        s_in.wait_event(e0)
+        used = [None, None]   # per slot: D2H of the C of the last mode that used it
+        for i, mode in enumerate(MODES):
+            sl = slots[i % 2]
             an, bn = ("A_T" if mode[0] == "T" else "A_N"), ("B_T" if mode[1] == "T" else "B_N")
-            for name in (an, bn, "C"):
-                memcpy(ctx, bufs[name], pin[name], nbytes, 0)
+            if used[i % 2] is not None:
+                s_in.wait_event(used[i % 2])
+            for dst, src in ((sl["A"], pin[an]), (sl["B"], pin[bn]), (sl["C"], pin["C"])):
+                memcpy(ctx, dst, src, nbytes, 0, s_in)
                 h2d += nbytes
-            gemm(mode, algo)
-            memcpy(ctx, hostC, bufs["C"], nbytes, 1)
+            e_in = torch.cuda.Event()
+            e_in.record(s_in)
+            ctx.stream.wait_event(e_in)
+            gb.sgemm(mode[0], mode[1], M, N, K, ALPHA, sl["A"], LD, sl["B"], LD, BETA, sl["C"], LD,
+                     algo=algo, stream=ctx.stream)
+            e_c = torch.cuda.Event()
+            e_c.record(ctx.stream)
+            s_out.wait_event(e_c)
+            memcpy(ctx, hostC[i % 2], sl["C"], nbytes, 1, s_out)
             d2h += nbytes
+            used[i % 2] = torch.cuda.Event()
+            used[i % 2].record(s_out)
+        ctx.stream.wait_stream(s_out)
         return h2d, d2h
 
     e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 5)), len(MODES) * flops, 1e12)

@@ -534,14 +534,23 @@ static gb_status ozaki_one(const GemmArgs &g, int s) {
     p.mp = mp; p.np = np;
     p.erow = erow; p.fcol = fcol; p.err = err;
     p.A = A; p.B = B; p.lda = g.lda; p.ldb = g.ldb; p.K = g.K; p.ta = g.ta ? 1 : 0; p.tb = g.tb ? 1 : 0;
-    // slice pairs t + u <= s + 1, least significant diagonals first (the FP64
-    // sum then adds terms in increasing magnitude)
+    // slice pairs t + u <= s + 1, grouped by the W digit u: the 152 tiles in
+    // flight (8 tile rows x 19 tile columns) keep W_u's 19 column panels hot in
+    // L2 while V_t's 8 row panels change (diagonal order, pair by pair, read
+    // the slices from DRAM about twice as often); within a group the smaller
+    // terms come first.  GB_OZAKI_PAIR_ORDER=diag: the diagonal order.
+    const char *ord = getenv("GB_OZAKI_PAIR_ORDER");
     int n = 0;
-    for (int d = s + 1; d >= 2; d--)
-        for (int t = 1; t <= s; t++) {
-            int u = d - t;
-            if (u >= 1 && u <= s) { p.pt[n] = (signed char)t; p.pu[n] = (signed char)u; n++; }
-        }
+    if (ord && ord[0] == 'd') {
+        for (int d = s + 1; d >= 2; d--)
+            for (int t = 1; t <= s; t++) {
+                int u = d - t;
+                if (u >= 1 && u <= s) { p.pt[n] = (signed char)t; p.pu[n] = (signed char)u; n++; }
+            }
+    } else {
+        for (int u = s; u >= 1; u--)
+            for (int t = s + 1 - u; t >= 1; t--) { p.pt[n] = (signed char)t; p.pu[n] = (signed char)u; n++; }
+    }
     p.npairs = n;
 
     static std::atomic<uint64_t> attr{0};
