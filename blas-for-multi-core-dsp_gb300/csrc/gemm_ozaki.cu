@@ -60,7 +60,7 @@ int ozaki_pick_slices(double target_err, int64_t K) {
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 5, GROUP_M = 8;
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 6, GROUP_M = 8;
 constexpr int KCHUNK_BLOCKS = 16;              // 1024-long exact FP32 chunk
 constexpr int MAX_CHUNKS_INT32 = 127;          // chunk sums per int32 accumulator
 constexpr int MAXS = 9, MAXPAIRS = MAXS * (MAXS + 1) / 2;
@@ -68,6 +68,7 @@ constexpr int TILE_BYTES = BM * BK * 2;        // 16 KB (BM == BN)
 constexpr int STAGE_BYTES = 2 * TILE_BYTES;
 constexpr int EPI_BYTES = 4 * 32 * 33 * 8;     // per-warp 32 x 32 FP64 staging
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_BYTES + 1024 + 256;
+static_assert(SMEM_BYTES <= 232448, "shared memory");
 constexpr int NT = 192;
 constexpr uint32_t TMEM_COLS = 512;            // [0,256): two FP32 accumulators, [256,512): FP64 sum
 
@@ -339,11 +340,16 @@ __global__ void __launch_bounds__(NT, 1)
             int tm, tn;
             tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
             bool first_flush = true;
-            for (int qq = 0; qq < p.npairs && go; qq++) {
-                int iacc[BN];
+            // exact int32 sums of the chunk sums of consecutive pairs on one diagonal t + u (one
+            // scale): one FP64 flush per diagonal, or after MAX_CHUNKS_INT32 chunk sums
+            int iacc[BN];
 #pragma unroll
-                for (int j = 0; j < BN; j++) iacc[j] = 0;
-                const double scale = __longlong_as_double((long long)(1023 + 2 - 8 * (p.pt[qq] + p.pu[qq])) << 52);
+            for (int j = 0; j < BN; j++) iacc[j] = 0;
+            int nacc = 0;
+            for (int qq = 0; qq < p.npairs && go; qq++) {
+                const int lev = p.pt[qq] + p.pu[qq];
+                const bool lev_ends = qq == p.npairs - 1 || p.pt[qq + 1] + p.pu[qq + 1] != lev;
+                const double scale = __longlong_as_double((long long)(1023 + 2 - 8 * lev) << 52);
                 for (int c = 0; c < nchunks; c++, gi++) {
                     const int b = gi & 1;
                     if (!ptx::mbar_wait(&acc_full[b], (gi >> 1) & 1, p.err, 14)) { go = false; break; }
@@ -359,8 +365,9 @@ __global__ void __launch_bounds__(NT, 1)
                     ptx::tc_fence_before();
                     __syncwarp();
                     if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
-                    const bool flush = (c == nchunks - 1) || ((c + 1) % MAX_CHUNKS_INT32 == 0);
+                    const bool flush = (c == nchunks - 1 && lev_ends) || ++nacc == MAX_CHUNKS_INT32;
                     if (flush) {   // FP64 sum += 2^(2-8(t+u)) * iacc (exact scaling, one rounding)
+                        nacc = 0;
 #pragma unroll
                         for (int cb = 0; cb < (2 * BN) / 32; cb++) {
                             uint32_t r[32];
@@ -534,14 +541,16 @@ static gb_status ozaki_one(const GemmArgs &g, int s) {
     p.mp = mp; p.np = np;
     p.erow = erow; p.fcol = fcol; p.err = err;
     p.A = A; p.B = B; p.lda = g.lda; p.ldb = g.ldb; p.K = g.K; p.ta = g.ta ? 1 : 0; p.tb = g.tb ? 1 : 0;
-    // slice pairs t + u <= s + 1, grouped by the W digit u: the 152 tiles in
-    // flight (8 tile rows x 19 tile columns) keep W_u's 19 column panels hot in
-    // L2 while V_t's 8 row panels change (diagonal order, pair by pair, read
-    // the slices from DRAM about twice as often); within a group the smaller
-    // terms come first.  GB_OZAKI_PAIR_ORDER=diag: the diagonal order.
+    // slice pairs t + u <= s + 1, diagonal by diagonal, least significant
+    // first: the pairs of a diagonal share a scale, so the epilogue sums them
+    // exactly in int32 and flushes to FP64 once per diagonal (GB300's FP64
+    // pipe made one flush per pair the limiter).  GB_OZAKI_PAIR_ORDER=w
+    // groups the pairs by the W digit u instead: the tiles in flight (8 tile
+    // rows x 19 tile columns) keep W_u's panels hot in L2, halving the DRAM
+    // reads, at one flush per pair.
     const char *ord = getenv("GB_OZAKI_PAIR_ORDER");
     int n = 0;
-    if (ord && ord[0] == 'd') {
+    if (!(ord && ord[0] == 'w')) {
         for (int d = s + 1; d >= 2; d--)
             for (int t = 1; t <= s; t++) {
                 int u = d - t;
