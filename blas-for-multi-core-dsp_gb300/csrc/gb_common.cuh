@@ -51,6 +51,9 @@ int smem_optin();
 // buffer stays valid until the next call on the same stream needs more;
 // work on that stream uses it in stream order.
 void *workspace(size_t bytes, void *stream);
+// The same, and *seq = the number of earlier calls of this form on the
+// stream (callers that alternate between two halves of the buffer).
+void *workspace(size_t bytes, void *stream, unsigned *seq);
 
 // Per-device one-time setup (kernel attributes such as the dynamic shared
 // memory limit hold per device): `done` has one bit per device.  Running the

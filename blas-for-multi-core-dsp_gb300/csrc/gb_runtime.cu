@@ -86,8 +86,21 @@ struct WsEntry {
     void *stream;
     void *ptr;
     size_t size;
+    unsigned seq;   // calls that asked for a sequence number (workspace halves by parity)
 };
 static std::vector<WsEntry> g_ws;
+
+void *workspace(size_t bytes, void *stream, unsigned *seq) {
+    void *p = workspace(bytes, stream);
+    if (p && seq) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        std::lock_guard<std::mutex> lk(g_ws_mu);
+        for (auto &e : g_ws)
+            if (e.dev == dev && e.stream == stream) *seq = e.seq++;
+    }
+    return p;
+}
 
 void *workspace(size_t bytes, void *stream) {
     int dev = 0;
@@ -113,7 +126,7 @@ void *workspace(size_t bytes, void *stream) {
         return nullptr;
     }
     if (!w) {
-        g_ws.push_back(WsEntry{dev, stream, nullptr, 0});
+        g_ws.push_back(WsEntry{dev, stream, nullptr, 0, 0});
         w = &g_ws.back();
     }
     w->ptr = p;

@@ -142,6 +142,10 @@ __global__ void __launch_bounds__(256) split_kernel(const float *__restrict__ X,
             if (out_lo2) out_lo2[r * kp + k] = __float2bfloat16_rn(rem - __bfloat162float(l));
         }
     }
+    // launched to overlap the previous call's GEMM (programmatic stream serialization): one
+    // thread keeps the grid from completing before that grid has, so the stream order of the
+    // GEMM that follows is unchanged
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) ptx::pdl_wait();
 }
 
 // Vectorised split of both operands in one launch (16-byte aligned sources
@@ -208,6 +212,7 @@ __global__ void __launch_bounds__(256) split_vec_kernel(const __grid_constant__ 
             }
             split_store4(a, o, r, k, v);
         }
+        if (blockIdx.x == 0 && threadIdx.x == 0) ptx::pdl_wait();   // as split_kernel
         return;
     }
 #pragma unroll
@@ -236,6 +241,7 @@ __global__ void __launch_bounds__(256) split_vec_kernel(const __grid_constant__ 
         const float v[4] = {tile[c4][rr], tile[c4 + 1][rr], tile[c4 + 2][rr], tile[c4 + 3][rr]};
         split_store4(a, o, r, k0 + c4, v);
     }
+    if (blockIdx.x == 0 && threadIdx.x == 0) ptx::pdl_wait();   // as split_kernel
 }
 
 // ------------------------------------------------------------------- gemm
@@ -364,6 +370,8 @@ __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int
 // BN = 128; the MMAs of chunk c+1 overlap the fold of chunk c.
 template <int NP, int BN, bool FOLD>
 __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constant__ PieceMaps maps, EpiParams p) {
+    // the next call's split pass may start beside this grid (it writes the other workspace half)
+    if (threadIdx.x == 0) ptx::pdl_launch_dependents();
     using CF = TwoPass<NP, BN>;
     static_assert(!FOLD || BN == 128, "the folding form keeps a 128-column total per thread");
     constexpr int B_TILE = CF::B_TILE, STAGE_BYTES = CF::STAGE_BYTES;
@@ -1047,14 +1055,32 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
     const size_t pieces = (np * (a_bytes + b_bytes) + 255) / 256 * 256;
     const bool sk = np == 2 && fold_kb == 0;
     const size_t sk_bytes = sk ? (size_t)sm_count() * 2 * BM * 256 * 4 + (size_t)sm_count() * 4 : 0;
-    uint8_t *ws = (uint8_t *)workspace(pieces + sk_bytes + 4096, g.stream);
+    // Two halves for the pieces, alternating per call on the stream: the split of a call then
+    // writes the half the previous call's GEMM is not reading, and is launched to run beside
+    // that GEMM (programmatic stream serialization; the GEMM triggers it at its start).  One
+    // half, launched in plain order, when the pieces are large or GB_BF16X3_PDL=0.
+    const char *pe = getenv("GB_BF16X3_PDL");
+    const bool pdl = !(pe && pe[0] == '0') && pieces <= (size_t(8) << 30);
+    const int halves = pdl ? 2 : 1;
+    unsigned seq = 0;
+    uint8_t *ws = (uint8_t *)workspace(halves * pieces + sk_bytes + 4096, g.stream, &seq);
     if (!ws) return (gb_status)gb_get_last_status();
-    float *sk_part = sk ? (float *)(ws + pieces) : nullptr;
-    int *sk_cnt = sk ? (int *)(ws + pieces + (size_t)sm_count() * 2 * BM * 256 * 4) : nullptr;
+    float *sk_part = sk ? (float *)(ws + halves * pieces) : nullptr;
+    int *sk_cnt = sk ? (int *)(ws + halves * pieces + (size_t)sm_count() * 2 * BM * 256 * 4) : nullptr;
+    uint8_t *pw = ws + (pdl ? (size_t)(seq & 1) * pieces : 0);
     __nv_bfloat16 *ap[3], *bp[3];
     for (int i = 0; i < np; i++) {
-        ap[i] = (__nv_bfloat16 *)(ws + i * a_bytes);
-        bp[i] = (__nv_bfloat16 *)(ws + np * a_bytes + i * b_bytes);
+        ap[i] = (__nv_bfloat16 *)(pw + i * a_bytes);
+        bp[i] = (__nv_bfloat16 *)(pw + np * a_bytes + i * b_bytes);
+    }
+    cudaLaunchAttribute pdl_attr[1];
+    pdl_attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl_attr[0].val.programmaticStreamSerializationAllowed = 1;
+    static std::atomic<uint64_t> carve{0};
+    if (pdl && device_setup_needed(carve)) {   // the GEMM's shared-memory configuration, so both fit on an SM
+        GB_CUDA_TRY(cudaFuncSetAttribute(split_vec_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        GB_CUDA_TRY(cudaFuncSetAttribute(split_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        device_setup_done(carve);
     }
     int *err = error_word();
     if (!err) return set_status(GB_ERR_OOM, "bf16x3: no device error word");
@@ -1072,14 +1098,26 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
                            {bp[0], bp[1], np == 3 ? bp[2] : nullptr}};
         const int64_t blocks = sa.op[0].tiles + sa.op[1].tiles;
         if (blocks > 0x7fffffff) return set_status(GB_ERR_UNSUPPORTED, "bf16x3: operands too large");
-        split_vec_kernel<<<(unsigned)blocks, 256, 0, g.stream>>>(sa);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)blocks);
+        cfg.blockDim = dim3(256);
+        cfg.stream = g.stream;
+        cfg.attrs = pdl_attr;
+        cfg.numAttrs = pdl ? 1 : 0;
+        GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_vec_kernel, sa));
         GB_LAUNCH_CHECK("bf16x3 split");
     } else {
         dim3 sgA((unsigned)ceil_div(kp, 32), (unsigned)ceil_div(g.M, 32));
         dim3 sgB((unsigned)ceil_div(kp, 32), (unsigned)ceil_div(g.N, 32));
         if (sgA.y > 65535u || sgB.y > 65535u) return set_status(GB_ERR_UNSUPPORTED, "bf16x3: M or N too large");
-        split_kernel<<<sgA, 256, 0, g.stream>>>((const float *)g.A, g.lda, g.ta ? 1 : 0, g.M, g.K, kp, ap[0], ap[1],
-                                                np == 3 ? ap[2] : nullptr);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = sgA;
+        cfg.blockDim = dim3(256);
+        cfg.stream = g.stream;
+        cfg.attrs = pdl_attr;
+        cfg.numAttrs = pdl ? 1 : 0;
+        GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_kernel, (const float *)g.A, g.lda, g.ta ? 1 : 0, g.M, g.K, kp,
+                                       ap[0], ap[1], np == 3 ? ap[2] : (__nv_bfloat16 *)nullptr));
         GB_LAUNCH_CHECK("bf16x3 split A");
         split_kernel<<<sgB, 256, 0, g.stream>>>((const float *)g.B, g.ldb, g.tb ? 0 : 1, g.N, g.K, kp, bp[0], bp[1],
                                                 np == 3 ? bp[2] : nullptr);

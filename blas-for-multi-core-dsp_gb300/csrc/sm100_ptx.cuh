@@ -27,6 +27,14 @@ __device__ __forceinline__ uint64_t globaltimer() {
     return t;
 }
 
+// ------------------------------------------------------------- programmatic dependent launch
+// Let the grid launched after this one with programmatic stream serialization
+// start before this grid completes (once every CTA has issued it or exited).
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+// Wait until the grids this one depends on have completed and their memory
+// operations are visible.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ------------------------------------------------------------- mbarrier
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");

@@ -279,3 +279,33 @@ def test_bf16x3_half_tile_tail_exact(torch, mode, M, N, K):
     got = host(dC)
     bad = np.argwhere(got != want)
     assert bad.size == 0, (mode, bad[:5])
+
+
+@pytest.mark.parametrize("algo_name", ["BF16X3", "BF16X6"])
+def test_back_to_back_calls_overlap_safely(torch, algo_name):
+    """Calls issued back to back on one stream: each call's split pass may run
+    beside the previous call's GEMM (programmatic dependent launch, pieces in
+    alternating workspace halves).  A chain C <- A_i B_i + C over eight
+    calls with different operands must give the same bits as the calls run
+    one after another (GB_BF16X3_PDL=0)."""
+    import os
+    import gbblas
+    algo = getattr(gbblas, "ALGO_" + algo_name)
+    M, N, K = 1536, 1280, 1024
+    As = [dev(oracle.fill(M, K, 300 + i, dtype=np.float32)) for i in range(8)]
+    Bs = [dev(oracle.fill(K, N, 400 + i, dtype=np.float32)) for i in range(8)]
+    C0 = oracle.fill(M, N, 500, dtype=np.float32)
+    outs = []
+    for pdl in ("1", "0"):
+        os.environ["GB_BF16X3_PDL"] = pdl
+        try:
+            dC = dev(C0)
+            for i in range(8):   # no host synchronisation between the calls
+                mode = "NN" if i % 2 == 0 else "NT"
+                B = Bs[i] if mode == "NN" else Bs[i].t().contiguous()
+                ldb = N if mode == "NN" else K
+                gbblas.sgemm(mode[0], mode[1], M, N, K, 1.0, As[i], K, B, ldb, 1.0, dC, N, algo=algo)
+            outs.append(host(dC))
+        finally:
+            os.environ.pop("GB_BF16X3_PDL", None)
+    assert outs[0].tobytes() == outs[1].tobytes()
