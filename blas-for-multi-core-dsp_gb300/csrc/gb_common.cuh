@@ -52,8 +52,10 @@ int smem_optin();
 // work on that stream uses it in stream order.
 void *workspace(size_t bytes, void *stream);
 // The same, and *seq = the number of earlier calls of this form on the
-// stream (callers that alternate between two halves of the buffer).
-void *workspace(size_t bytes, void *stream, unsigned *seq);
+// stream, *size = the buffer's size (>= bytes): callers that alternate
+// between two halves of the buffer place them by *size, so that calls of
+// different sizes never overlap each other's half.
+void *workspace(size_t bytes, void *stream, unsigned *seq, size_t *size);
 
 // Per-device one-time setup (kernel attributes such as the dynamic shared
 // memory limit hold per device): `done` has one bit per device.  Running the

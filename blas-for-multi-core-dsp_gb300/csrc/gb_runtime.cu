@@ -90,14 +90,17 @@ struct WsEntry {
 };
 static std::vector<WsEntry> g_ws;
 
-void *workspace(size_t bytes, void *stream, unsigned *seq) {
+void *workspace(size_t bytes, void *stream, unsigned *seq, size_t *size) {
     void *p = workspace(bytes, stream);
-    if (p && seq) {
+    if (p) {
         int dev = 0;
         cudaGetDevice(&dev);
         std::lock_guard<std::mutex> lk(g_ws_mu);
         for (auto &e : g_ws)
-            if (e.dev == dev && e.stream == stream) *seq = e.seq++;
+            if (e.dev == dev && e.stream == stream) {
+                *seq = e.seq++;
+                *size = e.size;
+            }
     }
     return p;
 }

@@ -1063,11 +1063,16 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
     const bool pdl = !(pe && pe[0] == '0') && pieces <= (size_t(8) << 30);
     const int halves = pdl ? 2 : 1;
     unsigned seq = 0;
-    uint8_t *ws = (uint8_t *)workspace(halves * pieces + sk_bytes + 4096, g.stream, &seq);
+    size_t ws_size = 0;
+    // [half 0 | half 1 | stream-K slots]: the halves at fixed places in the buffer, whatever the
+    // size of this call and the last (the buffer only grows after its stream has drained)
+    const size_t tail = (sk_bytes + 4096 + 255) / 256 * 256;
+    uint8_t *ws = (uint8_t *)workspace(halves * pieces + tail + 512, g.stream, &seq, &ws_size);
     if (!ws) return (gb_status)gb_get_last_status();
-    float *sk_part = sk ? (float *)(ws + halves * pieces) : nullptr;
-    int *sk_cnt = sk ? (int *)(ws + halves * pieces + (size_t)sm_count() * 2 * BM * 256 * 4) : nullptr;
-    uint8_t *pw = ws + (pdl ? (size_t)(seq & 1) * pieces : 0);
+    const size_t half = (ws_size - tail) / 2 / 256 * 256;   // >= pieces
+    float *sk_part = sk ? (float *)(ws + ws_size - tail) : nullptr;
+    int *sk_cnt = sk ? (int *)(ws + ws_size - tail + (size_t)sm_count() * 2 * BM * 256 * 4) : nullptr;
+    uint8_t *pw = ws + (pdl ? (size_t)(seq & 1) * half : 0);
     __nv_bfloat16 *ap[3], *bp[3];
     for (int i = 0; i < np; i++) {
         ap[i] = (__nv_bfloat16 *)(pw + i * a_bytes);

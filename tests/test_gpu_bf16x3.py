@@ -309,3 +309,28 @@ def test_back_to_back_calls_overlap_safely(torch, algo_name):
         finally:
             os.environ.pop("GB_BF16X3_PDL", None)
     assert outs[0].tobytes() == outs[1].tobytes()
+
+
+def test_back_to_back_calls_of_mixed_sizes(torch):
+    """Large and small calls alternating without host synchronisation: a small
+    call's split pass (beside the large call's GEMM) writes its own half of
+    the workspace wherever the large call's pieces end.  Same bits as the
+    calls run one after another."""
+    import os
+    import gbblas
+    shapes = [(2048, 1792, 2048), (384, 256, 320), (1536, 2048, 1024), (256, 512, 768)]
+    ops = [(dev(oracle.fill(M, K, 600 + i, dtype=np.float32)), dev(oracle.fill(K, N, 700 + i, dtype=np.float32)))
+           for i, (M, N, K) in enumerate(shapes)]
+    outs = []
+    for pdl in ("1", "0"):
+        os.environ["GB_BF16X3_PDL"] = pdl
+        try:
+            Cs = [dev(oracle.fill(M, N, 800 + i, dtype=np.float32)) for i, (M, N, K) in enumerate(shapes)]
+            for rep in range(3):
+                for i, (M, N, K) in enumerate(shapes):
+                    A, B = ops[i]
+                    gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B, N, 1.0, Cs[i], N, algo=gbblas.ALGO_BF16X3)
+            outs.append([host(c).tobytes() for c in Cs])
+        finally:
+            os.environ.pop("GB_BF16X3_PDL", None)
+    assert outs[0] == outs[1]
