@@ -88,6 +88,22 @@ __device__ __forceinline__ int exp_of_maxbits(unsigned long long mb) {
     return E - 1022;   // value in [2^(E-1023), 2^(E-1022))
 }
 
+// 2^k as a double for k >= -1022, 0 below
+__device__ __forceinline__ double pow2_or_zero(int k) {
+    return k >= -1022 ? __longlong_as_double((long long)(1023 + k) << 52) : 0.0;
+}
+
+// x * 2^k for |k| up to 3069 without a library call: up to three factors in
+// the normal range, the largest first, so that only a result outside the
+// normal range rounds.
+__device__ __forceinline__ double mul_pow2(double x, int k) {
+    const int a = max(-1022, min(1023, k));
+    k -= a;
+    const int b = max(-1022, min(1023, k));
+    const int c = max(-1022, min(1023, k - b));
+    return x * pow2_or_zero(a) * pow2_or_zero(b) * pow2_or_zero(c);
+}
+
 // Plain FP64 dot product of row `row` of X (rows x K; tx: stored K x rows)
 // and column `col` of W (K x cols; tw: stored cols x K), in k order.  The
 // digit paths use it for the outputs whose row or column holds an Inf or a
@@ -101,6 +117,13 @@ __device__ inline double native_dot(const double *X, int64_t ldx, int tx, int64_
         s = fma(x, w, s);
     }
     return s;
+}
+
+// native_dot kept out of line, for the rare outputs that need it inside
+// unrolled epilogue loops.
+__device__ __noinline__ inline double native_dot_cold(const double *X, int64_t ldx, int tx, int64_t row,
+                                                      const double *W, int64_t ldw, int tw, int64_t col, int64_t K) {
+    return native_dot(X, ldx, tx, row, W, ldw, tw, col, K);
 }
 #endif
 

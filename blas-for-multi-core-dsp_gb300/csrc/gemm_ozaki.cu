@@ -404,28 +404,42 @@ __global__ void __launch_bounds__(NT, 1)
                     ptx::tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 16; j++)
-                        stage[lane * 33 + h * 16 + j] = scalbn(__hiloint2double((int)r[2 * j + 1], (int)r[2 * j]), erow);
+                        stage[lane * 33 + h * 16 + j] = mul_pow2(__hiloint2double((int)r[2 * j + 1], (int)r[2 * j]), erow);
                 }
                 __syncwarp();
                 const int64_t col = n0 + cb * 32 + lane;
                 if (col < p.N) {
                     const int fc = p.fcol[col];
                     const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
-                    for (int rr = 0; rr < rows; rr++) {
-                        double *cp = p.C + (row0 + rr) * p.ldc + col;
-                        double v;
-                        if (fc == kNonFiniteLineExp || __ldg(p.erow + row0 + rr) == kNonFiniteLineExp)
-                            v = p.alpha * native_dot(p.A, p.lda, p.ta, row0 + rr, p.B, p.ldb, p.tb, col, p.K);
-                        else
-                            v = p.alpha * scalbn(stage[rr * 33 + lane], fc);
-                        if (p.semantics == GB_SEM_BLAS) {
-                            if (p.beta != 0.0) v = fma(p.beta, *cp, v);
-                        } else if (p.semantics == GB_SEM_SCALAR_BETA) {
-                            v = v + p.beta;
-                        } else {
-                            v = *cp + (v + p.beta);
+                    const bool needc = p.semantics == GB_SEM_ACCUM_SCALAR_BETA ||
+                                       (p.semantics == GB_SEM_BLAS && p.beta != 0.0);
+                    for (int rb = 0; rb < rows; rb += 16) {   // sixteen rows' loads in flight at once
+                        double cv[16];
+                        int er[16];
+#pragma unroll
+                        for (int j = 0; j < 16; j++) {
+                            const int rr = rb + j;
+                            er[j] = rr < rows ? __ldg(p.erow + row0 + rr) : 0;
+                            cv[j] = (rr < rows && needc) ? p.C[(row0 + rr) * p.ldc + col] : 0.0;
                         }
-                        *cp = v;
+#pragma unroll
+                        for (int j = 0; j < 16; j++) {
+                            const int rr = rb + j;
+                            if (rr >= rows) break;
+                            double v;
+                            if (fc == kNonFiniteLineExp || er[j] == kNonFiniteLineExp)
+                                v = p.alpha * native_dot_cold(p.A, p.lda, p.ta, row0 + rr, p.B, p.ldb, p.tb, col, p.K);
+                            else
+                                v = p.alpha * mul_pow2(stage[rr * 33 + lane], fc);
+                            if (p.semantics == GB_SEM_BLAS) {
+                                if (p.beta != 0.0) v = fma(p.beta, cv[j], v);
+                            } else if (p.semantics == GB_SEM_SCALAR_BETA) {
+                                v = v + p.beta;
+                            } else {
+                                v = cv[j] + (v + p.beta);
+                            }
+                            p.C[(row0 + rr) * p.ldc + col] = v;
+                        }
                     }
                 }
                 __syncwarp();

@@ -271,21 +271,6 @@ __device__ __forceinline__ void load_row8(const uint8_t *box, int r, int h, doub
     }
 }
 
-// 2^k as a double for k >= -1022, 0 below
-__device__ __forceinline__ double pow2_or_zero(int k) {
-    return k >= -1022 ? __longlong_as_double((long long)(1023 + k) << 52) : 0.0;
-}
-
-// x * 2^k for |k| up to 3069 without a library call: up to three factors in
-// the normal range, the largest first, so that only a result outside the
-// normal range rounds.
-__device__ __forceinline__ double mul_pow2(double x, int k) {
-    const int a = max(-1022, min(1023, k));
-    k -= a;
-    const int b = max(-1022, min(1023, k));
-    const int c = max(-1022, min(1023, k - b));
-    return x * pow2_or_zero(a) * pow2_or_zero(b) * pow2_or_zero(c);
-}
 
 // X leading dimensions that TMA cannot describe (odd, or a base that is not
 // 16-byte aligned): the producer warp copies k block kb of row tile rt with
