@@ -564,24 +564,26 @@ __global__ void __launch_bounds__(NT, 1)
                 }
                 ptx::tc_fence_after();
 #pragma unroll
-                for (int h = 0; h < NB / 8; h++) {   // eight columns at a time
-                    long long T[8];
+                for (int h = 0; h < NB / 4; h++) {   // four columns at a time, the 8 level loads in flight together
+                    uint32_t v[S][4];
 #pragma unroll
-                    for (int j = 0; j < 8; j++) T[j] = 0;
-#pragma unroll
-                    for (int L = 2; L <= S + 1; L++) {
-                        uint32_t v[8];
-                        ptx::tmem_ld_32x32b_x8(tmem + lane_off + (uint32_t)(lb * LV_COLS + (S + 1 - L) * NB + 8 * h), v);
-                        ptx::tmem_ld_wait();
-#pragma unroll
-                        for (int j = 0; j < 8; j++) T[j] = T[j] * 64 + (long long)__float2int_rn(__uint_as_float(v[j]));
+                    for (int L = 2; L <= S + 1; L++)
+                        ptx::tmem_ld_32x32b_x4(tmem + lane_off + (uint32_t)(lb * LV_COLS + (S + 1 - L) * NB + 4 * h),
+                                               v[L - 2]);
+                    ptx::tmem_ld_wait();
+                    if (h == NB / 4 - 1) {   // the whole level set is in registers: hand it back to the MMA
+                        ptx::tc_fence_before();
+                        __syncwarp();
+                        if (lane == 0) ptx::mbar_arrive(&lempty[lb]);
                     }
+                    long long T[4] = {0, 0, 0, 0};
 #pragma unroll
-                    for (int j = 0; j < 8; j++) acc[gr * NB + 8 * h + j] = fma((double)T[j], sc, acc[gr * NB + 8 * h + j]);
+                    for (int L = 0; L < S; L++)
+#pragma unroll
+                        for (int j = 0; j < 4; j++) T[j] = T[j] * 64 + (long long)__float2int_rn(__uint_as_float(v[L][j]));
+#pragma unroll
+                    for (int j = 0; j < 4; j++) acc[gr * NB + 4 * h + j] = fma((double)T[j], sc, acc[gr * NB + 4 * h + j]);
                 }
-                ptx::tc_fence_before();
-                __syncwarp();
-                if (lane == 0) ptx::mbar_arrive(&lempty[lb]);
             }
             if (!go) break;
             if (dw.last()) {   // the unit's sums are complete
