@@ -886,7 +886,7 @@ def _serve_stream(rate, duration, seed, max_dim):
 
 
 def run_serve(ctx):
-    """BASELINE serving config: Poisson arrivals (seed 4) of a mixed stream
+    """Serving workload: Poisson arrivals (seed 4) of a mixed stream
     (40% GEMM M=N=K log-uniform 256-4096, 25% thinB N 4-64 / M,K log-uniform
     1024-65536, 25% shortA mirror, 5% transpose, 5% Jacobi 10-100 sweeps on
     512-4096 grids; 70/30 FP32/FP64; uniform modes; alpha, beta ~ U[-2,2];
@@ -1025,8 +1025,8 @@ def run_serve(ctx):
 # ================================================================== reference arm
 def run_reference_arm(args):
     """The reference's own CPU implementation of the path (the oracle's port of
-    its host loop; the reference is not installable -- see the design doc), timed on
-    the host cores, rank 0 only."""
+    its host loop: the reference's device code needs the MT-3000 toolchain and
+    its package does not install), timed on the host cores, rank 0 only."""
     if int(os.environ.get("RANK", "0")) != 0:
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))

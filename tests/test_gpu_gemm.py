@@ -5,7 +5,7 @@
   launch-by-name boundary and the reference-named entry points, and the
   oracle on seeded U[-1,1] inputs (512^3 DGEMM, all four modes).
 * Fast algorithms: normwise error against the Dot2 oracle <= 2*K*u
-  (u = 2^-24 FP32, 2^-53 FP64), the tolerance BASELINE sets for GEMM.
+  (u = 2^-24 FP32, 2^-53 FP64), the GEMM tolerance.
 """
 import numpy as np
 import pytest
@@ -152,7 +152,7 @@ def test_sgemm_ordered_scalar_beta_bit_exact(torch, mode):
 
 
 @pytest.mark.parametrize("mode", MODES)
-def test_sgemm_simt_config2_shape_normwise(torch, mode):
+def test_sgemm_simt_4096_ld4112_normwise(torch, mode):
     """SGEMM BLAS semantics, alpha=1.5 beta=-0.5, padded leading dimensions."""
     import gbblas
     ta, tb = mode

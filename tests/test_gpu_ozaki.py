@@ -6,7 +6,7 @@
   must equal the exact product (checked against Dot2 to the last bit where
   the exact result is representable).
 * U[-1,1] and the precision-study distribution u*2^e, e in [-20, 20]
-  (BASELINE's DGEMM precision config): normwise error against Dot2 falls
+  (the DGEMM precision workload): normwise error against Dot2 falls
   with the slice count and at 7-8 slices is at FP64 level (<= 2*K*u64).
 """
 import numpy as np
