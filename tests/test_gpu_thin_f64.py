@@ -223,3 +223,40 @@ def test_thin_f64_cpasync_loader_matches_tma(torch, mode, kind):
         finally:
             os.environ.pop("GB_SKINNY_OZ_CPASYNC", None)
     assert outs[0].tobytes() == outs[1].tobytes()
+
+
+@pytest.mark.parametrize("kind", ["thinB", "shortA"])
+def test_thin_f64_split_k_nonfinite_and_odd_ld(torch, kind):
+    """Few rows, long K: the digit kernel splits K (partials summed by the
+    reduce kernel, Inf/NaN rows flagged per split); n = 40 takes a pass of
+    two 16-column groups and one of one group; odd leading dimensions take the
+    cp.async loader.  Finite outputs within 2*K*u normwise; Inf/NaN where
+    numpy's product has them."""
+    import gbblas
+    small, big, K = 40, 300, 8192
+    M, N = (big, small) if kind == "thinB" else (small, big)
+    rng = np.random.default_rng(17)
+    opA = rng.uniform(-1, 1, (M, K))
+    opB = rng.uniform(-1, 1, (K, N))
+    # one non-finite value in the large operand's line (row of A for thinB, column of B for shortA)
+    if kind == "thinB":
+        opA[7, 5000] = np.inf
+        opA[M - 2, 100] = np.nan
+    else:
+        opB[5000, 7] = -np.inf
+        opB[100, N - 2] = np.nan
+    lda, ldb = K | 1, N | 1
+    A = np.zeros((M, lda)); A[:, :K] = opA
+    B = np.zeros((K, ldb)); B[:, :N] = opB
+    want = opA @ opB
+    dC = dev(np.zeros((M, N)))
+    gbblas.dgemm("N", "N", M, N, K, 1.0, dev(A), lda, dev(B), ldb, 0.0, dC, N, algo=gbblas.ALGO_SKINNY)
+    got = host(dC)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    inf = np.isinf(want)
+    assert np.array_equal(np.isinf(got), inf)
+    assert np.array_equal(np.sign(got[inf]), np.sign(want[inf]))
+    fin = np.isfinite(want)
+    num = np.linalg.norm(got[fin] - want[fin])
+    den = np.linalg.norm(np.abs(opA[np.isfinite(opA).all(1)]), "fro") * np.linalg.norm(opB[:, np.isfinite(opB).all(0)], "fro")
+    assert num <= 2 * K * 2.0 ** -53 * den, num / den
