@@ -342,8 +342,12 @@ __global__ void __launch_bounds__(NT, 1)
     uint64_t *sfull = lempty + 2;          // [SSTAGES] scan ring
     uint64_t *sempty = sfull + SSTAGES;
     uint64_t *xready = sempty + SSTAGES;   // [2] chunk exponents written
-    uint64_t *xfree = xready + 2;          // [2] chunk exponents read (converters + drain)
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(xfree + 2);
+    // [2] chunk exponents read, by the converters (xfree_c) and by the drain (xfree_d): apart,
+    // because the converters can run two chunks ahead of a drain held up in an epilogue, and
+    // their arrivals for chunk c + 2 must not complete the phase of chunk c
+    uint64_t *xfree_c = xready + 2;
+    uint64_t *xfree_d = xfree_c + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(xfree_d + 2);
     int *exps = reinterpret_cast<int *>(reinterpret_cast<uint8_t *>(full) + BAR_BYTES);   // [2][BM]
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -365,7 +369,8 @@ __global__ void __launch_bounds__(NT, 1)
             ptx::mbar_init(&lfull[a], 1);
             ptx::mbar_init(&lempty[a], 4);
             ptx::mbar_init(&xready[a], 1);
-            ptx::mbar_init(&xfree[a], NCONV + 4);
+            ptx::mbar_init(&xfree_c[a], NCONV);
+            ptx::mbar_init(&xfree_d[a], 4);
         }
         ptx::fence_mbar_init();
         ptx::tma_prefetch_desc(&tmx);
@@ -490,7 +495,7 @@ __global__ void __launch_bounds__(NT, 1)
                     }
                     e = exps[xs * BM + r];
                     __syncwarp();
-                    if (lane == 0) ptx::mbar_arrive(&xfree[xs]);
+                    if (lane == 0) ptx::mbar_arrive(&xfree_c[xs]);
                     if (e == NO_EXP) e = 0;
                     fast = __all_sync(0xFFFFFFFFu, e >= -974);
                     ch++;
@@ -540,7 +545,7 @@ __global__ void __launch_bounds__(NT, 1)
             if (!ptx::mbar_wait(&xready[xs], (ch >> 1) & 1, p.err, 70)) break;
             const int ec = exps[xs * BM + r];
             __syncwarp();
-            if (lane == 0) ptx::mbar_arrive(&xfree[xs]);
+            if (lane == 0) ptx::mbar_arrive(&xfree_d[xs]);
             nf |= ec == kNonFiniteLineExp;
             if (ec != NO_EXP) {
                 if (eref == NO_EXP) {
@@ -632,7 +637,10 @@ __global__ void __launch_bounds__(NT, 1)
             // chunk ahead, so that the conversion's re-read of this chunk still finds it in L2
             // (two chunks ahead doubled the DRAM reads); NG = 1 keeps the scan two ahead
             const int lag = NG == 2 ? 1 : 2;
-            if (sch >= lag && !ptx::mbar_wait(&xfree[(sch - lag) & 1], ((sch - lag) >> 1) & 1, p.err, 71)) break;
+            if (sch >= lag) {
+                const int ps = (sch - lag) & 1, ph = ((sch - lag) >> 1) & 1;
+                if (!ptx::mbar_wait(&xfree_c[ps], ph, p.err, 71) || !ptx::mbar_wait(&xfree_d[ps], ph, p.err, 72)) break;
+            }
             bool go = true;
             for (int kb = sw.c0; kb < sw.c1(); kb++, sg++) {
                 const int s = sg % SSTAGES;

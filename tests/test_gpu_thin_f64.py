@@ -260,3 +260,32 @@ def test_thin_f64_split_k_nonfinite_and_odd_ld(torch, kind):
     num = np.linalg.norm(got[fin] - want[fin])
     den = np.linalg.norm(np.abs(opA[np.isfinite(opA).all(1)]), "fro") * np.linalg.norm(opB[:, np.isfinite(opB).all(0)], "fro")
     assert num <= 2 * K * 2.0 ** -53 * den, num / den
+
+
+@pytest.mark.parametrize("small", [8, 24])
+def test_thin_f64_slow_epilogues_keep_chunk_exponents(torch, small):
+    """Three row tiles per CTA, eight 256-k chunks each, and an Inf in one row
+    of every tile: each tile's epilogue recomputes that row as a plain dot
+    product (slow), while the converters run ahead into the next tile.  The
+    exponents of every chunk must still reach the drain: finite outputs within
+    2*K*u normwise, the Inf rows as numpy has them."""
+    import gbblas
+    M, N, K = 152 * 128 * 3, small, 2048
+    rng = np.random.default_rng(23)
+    A = rng.uniform(-1, 1, (M, K))
+    A *= np.ldexp(1.0, rng.integers(-30, 30, size=(M, 1)))   # row scales differ
+    B = rng.uniform(-1, 1, (K, N))
+    A[5::128, 77] = np.inf
+    want = A @ B
+    dC = dev(np.zeros((M, N)))
+    gbblas.dgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=gbblas.ALGO_SKINNY)
+    got = host(dC)
+    inf_rows = np.zeros(M, bool)
+    inf_rows[5::128] = True
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    assert np.array_equal(np.isinf(got), np.isinf(want))
+    fin = ~inf_rows
+    # per-row normwise error (rows have their own scales)
+    num = np.linalg.norm(got[fin] - want[fin], axis=1)
+    den = np.linalg.norm(A[fin], axis=1) * np.linalg.norm(B)
+    assert np.all(num <= 2 * K * 2.0 ** -53 * den), (num / den).max()
