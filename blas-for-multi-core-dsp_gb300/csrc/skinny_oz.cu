@@ -329,7 +329,7 @@ __device__ __forceinline__ void copy_x_block(uint32_t st, const OzThinParams &p,
 template <bool XCOLS, bool CPA, int NG>
 __global__ void __launch_bounds__(NT, 1)
     thin_oz_kernel(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, OzThinParams p) {
-    constexpr int STAGES = Cfg<NG>::STAGES, STAGE = Cfg<NG>::STAGE, WS = Cfg<NG>::WS;
+    constexpr int STAGES = Cfg<NG>::STAGES, STAGE = Cfg<NG>::STAGE, WS = Cfg<NG>::WS, PW = NG * NB;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint8_t *sring = smem + STAGES * STAGE;
@@ -439,40 +439,35 @@ __global__ void __launch_bounds__(NT, 1)
                         ptx::tc_fence_after();
                         const uint32_t wst = ptx::smem_u32(smem + s * STAGE + XS);
                         const uint32_t slot = tmem + SLOT0 + (uint32_t)(a * SLOT_COLS);
-#pragma unroll
-                        for (int gr = 0; gr < NG; gr++) {
-                            const int lb = NG == 1 ? (ch & 1) : gr;
-                            if (kb == c0 && use >= 1) {   // the drain has read this level set's last chunk
-                                if (!ptx::mbar_wait(&lempty[lb], (use & 1) ^ 1, p.err, 62)) {
-                                    go = false;
-                                    break;
-                                }
-                                ptx::tc_fence_after();
+                        // level sets: NG = 1 alternates two 128-column sets per chunk; NG = 2 has one
+                        // 256-column set, the two groups' columns interleaved level by level
+                        const int lb = NG == 1 ? (ch & 1) : 0;
+                        if (kb == c0 && use >= 1) {   // the drain has read this level set's last chunk
+                            if (!ptx::mbar_wait(&lempty[lb], (use & 1) ^ 1, p.err, 62)) {
+                                go = false;
+                                break;
                             }
-                            const uint32_t lv = tmem + (uint32_t)(lb * LV_COLS);
-                            const uint32_t wg = wst + (uint32_t)(gr * S * NB * 64);
+                            ptx::tc_fence_after();
+                        }
+                        const uint32_t lv = tmem + (uint32_t)(lb * LV_COLS);
 #pragma unroll
-                            for (int kk = 0; kk < KB / 16; kk++) {
+                        for (int kk = 0; kk < KB / 16; kk++) {
 #pragma unroll
-                                for (int t = 1; t <= S; t++) {
-                                    // W digits u = 9-t .. 1: tile rows 16(t-1) .. 127, N = 16(9-t); the first
-                                    // MMA of a chunk (t = 1, N = 128) writes every level column
-                                    const uint64_t bdesc = ptx::sdesc_kmajor_sw64(wg + (uint32_t)((t - 1) * NB * 64)) +
-                                                           (uint64_t)((kk * 32) >> 4);
-                                    ptx::umma_f16_ta(lv, slot + (uint32_t)((t - 1) * 16 + kk * 8), bdesc,
-                                                     ptx::idesc_bf16_f32(BM, NB * (S + 1 - t)),
-                                                     (kb != c0 || kk != 0 || t != 1) ? 1u : 0u);
-                                }
+                            for (int t = 1; t <= S; t++) {
+                                // W digits u = 9-t .. 1 of all NG groups: tile rows PW(t-1) .. 8PW-1,
+                                // N = PW(9-t); the first MMA of a chunk (t = 1) writes every level column
+                                const uint64_t bdesc = ptx::sdesc_kmajor_sw64(wst + (uint32_t)((t - 1) * PW * 64)) +
+                                                       (uint64_t)((kk * 32) >> 4);
+                                ptx::umma_f16_ta(lv, slot + (uint32_t)((t - 1) * 16 + kk * 8), bdesc,
+                                                 ptx::idesc_bf16_f32(BM, PW * (S + 1 - t)),
+                                                 (kb != c0 || kk != 0 || t != 1) ? 1u : 0u);
                             }
                         }
                         if (!go) break;
                         ptx::umma_commit(&empty[s]);
                         ptx::umma_commit(&aempty[a]);
                     }
-                    if (go) {
-#pragma unroll
-                        for (int gr = 0; gr < NG; gr++) ptx::umma_commit(&lfull[NG == 1 ? (ch & 1) : gr]);
-                    }
+                    if (go) ptx::umma_commit(&lfull[NG == 1 ? (ch & 1) : 0]);
                 }
             }
         }
@@ -560,23 +555,21 @@ __global__ void __launch_bounds__(NT, 1)
             // |T| < 2^62.1), then one rounding to FP64: sum_L S_L 2^-6L = T 2^-54
             const double sc = pow2_or_zero(ec == NO_EXP ? -100000 : ec - eref - 54);
             const int use = NG == 1 ? (ch >> 1) : ch;
+            const int lb = NG == 1 ? (ch & 1) : 0;
+            if (!ptx::mbar_wait(&lfull[lb], use & 1, p.err, 67)) break;
+            ptx::tc_fence_after();
 #pragma unroll
             for (int gr = 0; gr < NG; gr++) {
-                const int lb = NG == 1 ? (ch & 1) : gr;
-                if (!ptx::mbar_wait(&lfull[lb], use & 1, p.err, 67)) {
-                    go = false;
-                    break;
-                }
-                ptx::tc_fence_after();
 #pragma unroll
                 for (int h = 0; h < NB / 4; h++) {   // four columns at a time, the 8 level loads in flight together
                     uint32_t v[S][4];
 #pragma unroll
                     for (int L = 2; L <= S + 1; L++)
-                        ptx::tmem_ld_32x32b_x4(tmem + lane_off + (uint32_t)(lb * LV_COLS + (S + 1 - L) * NB + 4 * h),
+                        ptx::tmem_ld_32x32b_x4(tmem + lane_off +
+                                                   (uint32_t)(lb * LV_COLS + (S + 1 - L) * PW + gr * NB + 4 * h),
                                                v[L - 2]);
                     ptx::tmem_ld_wait();
-                    if (h == NB / 4 - 1) {   // the whole level set is in registers: hand it back to the MMA
+                    if (gr == NG - 1 && h == NB / 4 - 1) {   // the whole level set is in registers: back to the MMA
                         ptx::tc_fence_before();
                         __syncwarp();
                         if (lane == 0) ptx::mbar_arrive(&lempty[lb]);
@@ -709,9 +702,9 @@ __global__ void thin_oz_reduce_kernel(OzThinParams p) {
 }
 
 // Digits of W columns j0 .. j0+pw-1 (logical K x n; tw: stored n x K),
-// relative to the column exponents, group by group of 16 columns:
-// out[(g*8 + 8-u)*16 + jj][k] for column j0 + 16g + jj and u = 1..8 (the
-// least significant digit first), K-major, kp columns, zero beyond n and K.
+// relative to the column exponents: out[(8-u)*pw + jp][k] for column j0 + jp
+// and u = 1..8 (the least significant digit first, the pass's columns within
+// a digit), K-major, kp columns, zero beyond n and K.
 __global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw, int n, int j0, int pw, int64_t K,
                                int64_t kp, const int *__restrict__ fcol, unsigned short *__restrict__ out) {
     const int64_t total = (int64_t)pw * kp;
@@ -719,7 +712,7 @@ __global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw
          e += (int64_t)gridDim.x * blockDim.x) {
         const int jp = (int)(e / kp);
         const int64_t k = e - (int64_t)jp * kp;
-        const int j = j0 + jp, gr = jp / NB, jj = jp % NB;
+        const int j = j0 + jp;
         double x = 0.0;
         int f = 0;
         if (j < n && k < K) {
@@ -734,7 +727,7 @@ __global__ void wdigits_kernel(const double *__restrict__ W, int64_t ldw, int tw
             const unsigned short h =
                 d ? (unsigned short)(__bfloat16_as_ushort(__float2bfloat16_rn(small_int_to_float(d))) | (sg << 15))
                   : 0;
-            out[((int64_t)(gr * S + S - u) * NB + jj) * kp + k] = h;
+            out[((int64_t)(S - u) * pw + jp) * kp + k] = h;
         }
     }
 }
