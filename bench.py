@@ -129,6 +129,50 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ================================================================== ranks
+class Ranks:
+    """One process per GPU (replicas): rank / world from the launcher's
+    environment, a barrier, the maximum of a per-rank time, and rank 0 alone
+    printing the result line.  `backend` nccl with a CUDA device on the GPU
+    box; gloo with the CPU in the CPU tests."""
+
+    def __init__(self, backend="nccl", device=None):
+        import torch
+        self.torch = torch
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.device = device
+        self.dist = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v):
+        if not self.dist:
+            return v
+        t = self.torch.tensor([float(v)], dtype=self.torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def finish(self, line, out=None):
+        if self.dist:
+            self.dist.barrier()
+            self.dist.destroy_process_group()
+        if self.rank == 0:
+            print(json.dumps(line), file=out or sys.stdout, flush=True)
+
+
+def aggregate(world, steps, units_per_step, ms):
+    """Whole-job throughput: the units all ranks processed / the slowest rank's time (s)."""
+    return world * steps * units_per_step / (ms * 1e-3)
+
+
 # ================================================================== context
 class Ctx:
     def __init__(self, args):
@@ -136,15 +180,10 @@ class Ctx:
         import gbblas
         self.args = args
         self.torch, self.gb = torch, gbblas
-        self.rank = int(os.environ.get("RANK", "0"))
-        self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         torch.cuda.set_device(self.local)
-        self.dist = None
-        if self.world > 1:
-            import torch.distributed as dist
-            dist.init_process_group("nccl")
-            self.dist = dist
+        self.ranks = Ranks("nccl", torch.device("cuda", self.local))
+        self.rank, self.world, self.dist = self.ranks.rank, self.ranks.world, self.ranks.dist
         gbblas.lib()
         arch = gbblas.arch()
         if arch != 103:
@@ -157,16 +196,11 @@ class Ctx:
         return self.torch.cuda.Event(enable_timing=True)
 
     def barrier(self):
-        if self.dist:
-            self.dist.barrier()
+        self.ranks.barrier()
         self.torch.cuda.synchronize()
 
     def max_over_ranks(self, ms):
-        if not self.dist:
-            return ms
-        t = self.torch.tensor([ms], device=self.dev)
-        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
-        return float(t.item())
+        return self.ranks.max(ms)
 
     def timed(self, step, steps, per_launch=None):
         """Run `steps` steps between barriers; returns (elapsed ms max over ranks,
@@ -197,11 +231,7 @@ class Ctx:
                 for i, m in enumerate(modes)} if evs else {}
 
     def finish(self, line):
-        if self.dist:
-            self.dist.barrier()
-            self.dist.destroy_process_group()
-        if self.rank == 0:
-            print(json.dumps(line), flush=True)
+        self.ranks.finish(line)
 
 
 def base_line(ctx, metric, value, unit, ms, steps, dtype, config, hib=True):
@@ -228,7 +258,7 @@ def e2e_measure(ctx, step_host, steps, flops_or_bytes, unit_div):
     t1.record(ctx.stream)
     ctx.torch.cuda.synchronize()
     ms = ctx.max_over_ranks(t0.elapsed_time(t1))
-    return ctx.world * steps * flops_or_bytes / (ms * 1e-3) / unit_div, h2d, d2h
+    return aggregate(ctx.world, steps, flops_or_bytes, ms) / unit_div, h2d, d2h
 
 
 # ================================================================== CPU legs
@@ -392,7 +422,7 @@ def run_sgemm(ctx):
             gemm(mode, algo)
 
     ms, _, clocks, launches = ctx.timed(step, args.steps)
-    value = ctx.world * args.steps * len(MODES) * flops / (ms * 1e-3) / 1e12
+    value = aggregate(ctx.world, args.steps, len(MODES) * flops, ms) / 1e12
 
     def step_events(evs):
         for mode in MODES:
@@ -598,7 +628,7 @@ def run_dgemm(ctx):
             evs.append((a, b))
 
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
-    value = ctx.world * args.steps * len(modes) * flops / (ms * 1e-3) / 1e12
+    value = aggregate(ctx.world, args.steps, len(modes) * flops, ms) / 1e12
     npairs = slices * (slices + 1) // 2
     roof = {"bound": "tensor", "achieved": flops * npairs / (kms * 1e-3) / 1e12, "peak": ctx.peaks["bf16_tflops"],
             "unit": "TFLOP/s", "peak_note": "BF16 slice-product flops (%d pairs x 2MNK) / mean gb_dgemm duration "
@@ -691,7 +721,7 @@ def run_skinny(ctx):
             evs.append((a, b))
 
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
-    value = ctx.world * args.steps * len(MODES) * nbytes_alg / (ms * 1e-3) / 1e9
+    value = aggregate(ctx.world, args.steps, len(MODES) * nbytes_alg, ms) / 1e9
     tflops = flops / (kms * 1e-3) / 1e12
     cpeak = FP64_PEAK if bits == 64 else FP32_SIMT_PEAK
     roof = bw_roof(ctx, nbytes_alg / (kms * 1e-3) / 1e9, None, "%s_%s_n%d" % (args.workload, "f%d" % bits, small),
@@ -755,7 +785,7 @@ def run_transpose(ctx):
         evs.append((a, b))
 
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
-    value = ctx.world * args.steps * nbytes / (ms * 1e-3) / 1e9
+    value = aggregate(ctx.world, args.steps, nbytes, ms) / 1e9
     roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "transpose_f%d_%s" % (bits, args.shape), {"kernel_ms": kms})
     hA = A.cpu().pin_memory()
     hB = torch.empty_like(B, device="cpu").pin_memory()
@@ -815,7 +845,7 @@ def run_jacobi(ctx):
         evs.append((a, b))
 
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
-    value = ctx.world * args.steps * nbytes / (ms * 1e-3) / 1e9
+    value = aggregate(ctx.world, args.steps, nbytes, ms) / 1e9
     gflops = (17.0 if nine else 5.0) * M * N * iters / (kms * 1e-3) / 1e12
     extra = {"kernel_ms": kms, "points_per_s": M * N * iters / (kms * 1e-3),
              "fp_tflops": gflops, "note": "achieved = algorithmic bytes (2*M*N*s per sweep) / time; temporal "

@@ -1,0 +1,73 @@
+"""bench.py's replica logic on CPU: two ranks over gloo (127.0.0.1).
+
+The path has no exchange step (one process per GPU runs its own replica), so
+what has to hold across ranks is the measurement: every rank passes the
+barriers, the reported time is the slowest rank's, the throughput counts the
+units of all ranks, and rank 0 alone prints the JSON line; the reference arm
+runs on rank 0 only and the other ranks exit 0 without output."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out_dir):
+    os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    sys.path.insert(0, REPO)
+    import bench
+    r = bench.Ranks("gloo", "cpu")
+    r.barrier()
+    ms = 10.0 * (rank + 1)                    # the ranks' own elapsed times differ
+    slowest = r.max(ms)
+    value = bench.aggregate(r.world, 3, 1e9, slowest)   # 3 steps of 1e9 units per rank
+    with open(os.path.join(out_dir, "rank%d.out" % rank), "w") as f:
+        r.finish({"value": value, "ms": slowest, "n_gpus": r.world}, out=f)
+    with open(os.path.join(out_dir, "rank%d.max" % rank), "w") as f:
+        f.write(repr(slowest))
+
+
+def test_two_ranks_gloo(tmp_path):
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    port = _free_port()
+    ctx = mp.get_context("spawn")
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, str(tmp_path))) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    # both ranks agree on the slowest time
+    assert float((tmp_path / "rank0.max").read_text()) == 20.0
+    assert float((tmp_path / "rank1.max").read_text()) == 20.0
+    # rank 0 alone prints; throughput = units of both ranks / the slowest time
+    line = json.loads((tmp_path / "rank0.out").read_text())
+    assert (tmp_path / "rank1.out").read_text() == ""
+    assert line["n_gpus"] == 2 and line["ms"] == 20.0
+    assert line["value"] == pytest.approx(2 * 3 * 1e9 / 20e-3)
+
+
+def test_aggregate_single_rank():
+    sys.path.insert(0, REPO)
+    import bench
+    assert bench.aggregate(1, 4, 2.5e12, 1000.0) == pytest.approx(1e13)
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.strip() == ""
