@@ -21,8 +21,10 @@
 // FP64 conversion and one FMA per output and chunk, as GB300's FP64 pipe is
 // narrow.
 //   pass 1: column exponents and the digit slices of W (small);
-//   pass 2 (thin_oz_kernel, per 16 columns of W):
-//     warp 0     TMA: 128 rows x 32 k of X (FP64) + the 8 digit tiles of W;
+//   pass 2 (thin_oz_kernel, per 16 or 32 columns of W -- one or two groups):
+//     warp 0     TMA: 128 rows x 32 k of X (FP64) + the 8 digit tiles of W
+//                (or, for leading dimensions TMA cannot take, all lanes
+//                copying X by 8-byte cp.async into the same layout);
 //     warp 14    TMA: the same X boxes, one chunk ahead, for the scan;
 //     warp 15    scan of chunk c+1 (four rows per lane: the maximum |x| bit
 //                pattern -> e_rc in shared memory);
@@ -32,11 +34,17 @@
 //                into tensor memory (the A operand of the MMA, never in
 //                shared memory);
 //     warp 1     MMA: one MMA per digit t of X against W's digits
-//                u = 1 .. 9-t at once (N = 16(9-t)): W's digit tiles lie in
-//                shared memory in the order u = 8 .. 1, so the pair (t, u)
+//                u = 1 .. 9-t of all the pass's columns at once
+//                (N = PW(9-t), PW = 16 or 32): W's digit rows lie in shared
+//                memory in the order [u = 8 .. 1][column], so the pair (t, u)
 //                lands in accumulator column block 9 - t - u for every t,
-//                i.e. level L = t + u at columns 16(9-L) .. 16(9-L)+15;
-//                two level sets alternate per chunk.
+//                i.e. level L = t + u at columns PW(9-L) .. PW(9-L)+PW-1;
+//                one group: two level sets alternate per chunk; two groups:
+//                one 256-column set, handed back by the drain between chunks.
+// The exponent slots of a chunk are freed separately by the converters and
+// by the drain (each arrives in chunk order on its own barrier), so that
+// converters two chunks ahead of a drain held up in an epilogue cannot
+// release a slot the drain has not read.
 // Truncation: digits beyond 2^-48 of the chunk's row maximum (or the column
 // maximum) and pairs below 2^-54 are dropped -- well inside the 2*K*u64
 // normwise bound.  An output whose row of X or column of W holds an Inf or a
