@@ -123,7 +123,13 @@ void gb_gemm_opts_init(gb_gemm_opts *opts);
 /* transA/transB: 'N' or 'T' (case-insensitive).  Shapes: op(A) is M x K,
  * op(B) is K x N, C is M x N.  lda >= (transA=='N' ? K : M),
  * ldb >= (transB=='N' ? N : K), ldc >= N.  M, N or K == 0 is valid
- * (K == 0 still applies beta).  opts may be NULL. */
+ * (K == 0 still applies beta).  opts may be NULL.
+ * Stream-ordered: work queued after a call sees its C.  Two BF16X3 / BF16X6
+ * calls back to back on one stream may overlap the second's operand split
+ * with the first's GEMM (never its GEMM with the first's).  FP64 through the
+ * digit forms (OZAKI, FP64 SKINNY): an output whose row of op(A) or column of
+ * op(B) holds an Inf or a NaN is computed as a plain FP64 dot product, so
+ * they propagate as in IEEE arithmetic. */
 gb_status gb_sgemm(char transA, char transB, int64_t M, int64_t N, int64_t K,
                    float alpha, const float *A, int64_t lda, const float *B, int64_t ldb,
                    float beta, float *C, int64_t ldc, const gb_gemm_opts *opts);
