@@ -109,3 +109,27 @@ def test_auto_algorithm_choice(L):
     assert gbblas.pick_algo(64, "N", "N", 1024, 1024, 1024) == gbblas.ALGO_OZAKI
     assert gbblas.pick_algo(32, "N", "N", 4096, 4096, 4096) == gbblas.ALGO_BF16X3
     assert gbblas.pick_algo(32, "N", "N", 256, 256, 256) == gbblas.ALGO_SIMT
+
+
+@pytest.mark.parametrize("lang", ["c99", "c++17"])
+def test_headers_compile_and_link(lang, tmp_path):
+    """The public headers as a reference-side host program uses them: valid
+    C99 and C++ with all warnings as errors, every call family links."""
+    import shutil
+    import subprocess
+    import gbblas
+    if not os.path.exists(gbblas.LIB_PATH):
+        pytest.skip("libgbblas.so not built")
+    cc = "gcc" if lang == "c99" else "g++"
+    if not shutil.which(cc):
+        pytest.skip(cc + " not found")
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = os.path.join(repo, "tests", "c", "abi_compile.c")
+    flags = ["-std=c99", "-x", "c"] if lang == "c99" else ["-std=c++17", "-x", "c++"]
+    out = str(tmp_path / "abi")
+    libdir = os.path.dirname(gbblas.LIB_PATH)
+    r = subprocess.run([cc] + flags + ["-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(repo, "include"),
+                        src, "-x", "none", "-L" + libdir, "-lgbblas", "-Wl,-rpath," + libdir, "-o", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert subprocess.run([out], capture_output=True).returncode == 0
