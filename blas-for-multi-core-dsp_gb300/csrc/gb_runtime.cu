@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "gb_common.cuh"
+#include "sm100_ptx.cuh"
 
 namespace gb {
 
@@ -137,6 +138,10 @@ void *workspace(size_t bytes, void *stream) {
     return p;
 }
 
+// The error word lives in a file-scope device variable (zero when the module
+// loads), so finding it needs no allocation: its device address is looked up
+// once per device, with that device current.
+static __device__ int g_err_word_dev;
 static int *g_err_word[kMaxDev] = {nullptr};
 
 int *error_word() {
@@ -145,15 +150,27 @@ int *error_word() {
     if (dev < 0 || dev >= kMaxDev) return nullptr;
     std::lock_guard<std::mutex> lk(g_ws_mu);
     if (!g_err_word[dev]) {
-        int *p = nullptr;
-        if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_err_word_dev) != cudaSuccess || p == nullptr) {
             cudaGetLastError();
             return nullptr;
         }
-        cudaMemset(p, 0, sizeof(int));
-        g_err_word[dev] = p;
+        g_err_word[dev] = (int *)p;
     }
     return g_err_word[dev];
+}
+
+// ------------------------------------------------------------ self-test
+// One thread waits on an mbarrier that nothing arrives at, through the same
+// bounded wait the TMA / tensor-core kernels use, with a caller-given limit:
+// the wait gives up, records code 99 in the error word and the kernel
+// returns.  Nothing else is in flight (no TMA, no tensor memory).
+__global__ void bounded_wait_selftest_kernel(int *err, uint64_t limit_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x != 0) return;
+    ptx::mbar_init(&bar, 1);
+    ptx::fence_mbar_init();
+    ptx::mbar_wait_limit(&bar, 0, err, 99, limit_ns);
 }
 
 // -------------------------------------------------------------- generator
@@ -295,6 +312,16 @@ gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int kind, void *st
 gb_status gb_workspace_reserve(size_t bytes, void *stream) {
     if (bytes == 0) return ok();
     if (!workspace(bytes, stream)) return (gb_status)gb_get_last_status();
+    return ok();
+}
+
+gb_status gb_selftest_bounded_wait(uint64_t limit_ns, void *stream) {
+    GB_CHECK_ARG(limit_ns >= 1000 && limit_ns <= 100000000ull,
+                 "gb_selftest_bounded_wait: limit %llu ns not in [1 us, 100 ms]", (unsigned long long)limit_ns);
+    int *err = error_word();
+    if (!err) return set_status(GB_ERR_CUDA, "gb_selftest_bounded_wait: no device error word");
+    bounded_wait_selftest_kernel<<<1, 32, 0, as_stream(stream)>>>(err, limit_ns);
+    GB_LAUNCH_CHECK("bounded_wait_selftest_kernel");
     return ok();
 }
 

@@ -67,20 +67,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 
 // Wait for the completion of the phase with the given parity; false (and the
 // device error word *err set to `code`) if it did not complete within
-// kWaitLimitNs or if another thread already reported an error.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
+// limit_ns or if another thread already reported an error.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t *bar, uint32_t parity, int *err, int code,
+                                                uint64_t limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer();
     for (uint32_t it = 1;; it++) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 63) == 0) {
             if (*(volatile int *)err != 0) return false;
-            if (globaltimer() - t0 > kWaitLimitNs) {
+            if (globaltimer() - t0 > limit_ns) {
                 atomicCAS(err, 0, code);
                 return false;
             }
         }
     }
+}
+
+// The same with the library's limit, kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
+    return mbar_wait_limit(bar, parity, err, code, kWaitLimitNs);
 }
 
 // ----------------------------------------------------------------- TMA

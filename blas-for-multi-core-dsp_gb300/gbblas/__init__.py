@@ -122,6 +122,7 @@ _SIGS = {
     "gb_exec": ([ctypes.c_char_p, _int, _int, ctypes.POINTER(_ul)], _int),
     "gb_ref_set_stream": ([_vp], None),
     "gb_workspace_reserve": ([ctypes.c_size_t, _vp], _int),
+    "gb_selftest_bounded_wait": ([ctypes.c_uint64, _vp], _int),
     "gb_gemm_batch": ([ctypes.POINTER(GemmDesc), _int, _vp], _int),
     "gb_server_config_init": ([ctypes.POINTER(ServerConfig)], None),
     "gb_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)], _int),

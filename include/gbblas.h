@@ -69,6 +69,17 @@ gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int kind, void *st
  * cudaMalloc off the call path of later calls on `stream`. */
 gb_status gb_workspace_reserve(size_t bytes, void *stream);
 
+/* Self-test of the bounded device waits (no reference counterpart; the
+ * reference's kernels have no waits that can give up).  Every mbarrier wait
+ * of the TMA / tensor-core kernels gives up after 2 s, records a code in a
+ * per-device error word, and the kernel winds down; gb_sync() then returns
+ * GB_ERR_DEVICE_TIMEOUT and clears the word.  This call runs one such wait on
+ * a barrier that nothing arrives at, with a limit of limit_ns (1 us .. 100
+ * ms), so that it gives up: the next gb_sync() on `stream` returns
+ * GB_ERR_DEVICE_TIMEOUT, the one after that GB_OK, and the device stays
+ * usable. */
+gb_status gb_selftest_bounded_wait(uint64_t limit_ns, void *stream);
+
 /* ------------------------------------------------------------ inputs */
 /* Seeded counter-based generator (bit-identical to the oracle's): element
  * (r,c) of a rows x cols matrix (leading dimension ld) gets f(seed, r*cols+c).
@@ -153,8 +164,10 @@ gb_status gb_dgemm(char transA, char transB, int64_t M, int64_t N, int64_t K,
  * until the process exits.  A call whose split-K plan needs more than 16 MiB
  * (splits x max(M, N) x padded min(M, N) x 4 bytes) is rejected with
  * GB_ERR_INVALID_ARG before anything runs.  The first call on each device
- * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls share
+ * looks up the device addresses of that array and of the library's device
+ * error word (both file-scope device variables, found with
+ * cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share
  * the one array: calls that overlap on the GPU (different streams, or
  * different host threads) race on it and must be serialised by the caller.
  * `semantics` is a gb_semantics value; `stream` as in gb_gemm_opts. */

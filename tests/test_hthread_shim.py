@@ -11,7 +11,7 @@ import gbblas
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(REPO, "include")
 LIBDIR = os.path.dirname(gbblas.LIB_PATH)
-REF = "/root/reference"
+REF = os.environ.get("REF_ROOT", "/root/reference")
 DEMOS = ["dgemm_release_V1.1/host_code/dgemm_demo.c", "sgemm_release_V1.3.2/host_code/sgemm_demo.c",
          "irr_shortA_sgemm_release_V0.0/host_code/irr_shortA_sgemm_demo.c",
          "irr_thinB_sgemm_release_V1.2/host_code/irr_thinB_sgemm_demo.c",
