@@ -160,6 +160,7 @@ gb_status launch_sgemm_simt(const GemmArgs &g);
 gb_status launch_dgemm_dmma(const GemmArgs &g);
 gb_status launch_sgemm_bf16x3(const GemmArgs &g);
 gb_status launch_sgemm_bf16x6(const GemmArgs &g);
+gb_status launch_sgemm_fp16x3(const GemmArgs &g);
 gb_status launch_dgemm_ozaki(const GemmArgs &g, int slices);
 // Slice count (2..8) whose truncation error meets a normwise target for this K.
 int ozaki_pick_slices(double target_err, int64_t K);

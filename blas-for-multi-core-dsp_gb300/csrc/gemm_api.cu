@@ -83,7 +83,7 @@ gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alph
     GB_CHECK_ARG(ldb >= (bcols > 1 ? bcols : 1), "%s: ldb (%lld) < %lld", fn, (long long)ldb, (long long)bcols);
     GB_CHECK_ARG(ldc >= (N > 1 ? N : 1), "%s: ldc (%lld) < N (%lld)", fn, (long long)ldc, (long long)N);
     GB_CHECK_ARG(o.semantics >= 0 && o.semantics <= 2, "%s: unknown semantics %d", fn, o.semantics);
-    GB_CHECK_ARG(o.algo >= 0 && o.algo <= 7, "%s: unknown algo %d", fn, o.algo);
+    GB_CHECK_ARG(o.algo >= 0 && o.algo <= 8, "%s: unknown algo %d", fn, o.algo);
     GB_CHECK_ARG(o.k_block >= 0 && o.k_slab >= 0, "%s: negative k_block/k_slab", fn);
     if (M == 0 || N == 0) return ok();
     GB_CHECK_ARG(C != nullptr, "%s: C is null", fn);
@@ -115,6 +115,9 @@ gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alph
         case GB_ALGO_BF16X6:
             if (sizeof(T) != 4) return set_status(GB_ERR_UNSUPPORTED, "gb_dgemm: BF16X6 is an FP32 algorithm");
             return launch_sgemm_bf16x6(g);
+        case GB_ALGO_FP16X3:
+            if (sizeof(T) != 4) return set_status(GB_ERR_UNSUPPORTED, "gb_dgemm: FP16X3 is an FP32 algorithm");
+            return launch_sgemm_fp16x3(g);
         case GB_ALGO_OZAKI: {
             if (sizeof(T) != 8) return set_status(GB_ERR_UNSUPPORTED, "gb_sgemm: OZAKI is an FP64 algorithm");
             int s = o.ozaki_slices;

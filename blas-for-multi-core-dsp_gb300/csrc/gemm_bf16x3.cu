@@ -1,29 +1,45 @@
-// gemm_bf16x3.cu -- SGEMM as three BF16 products on the tcgen05 tensor cores.
+// gemm_bf16x3.cu -- SGEMM as sums of 16-bit piece products on the tcgen05
+// tensor cores, FP32 accumulation.
 //
 // C = alpha * op(A) op(B) (+ beta C / + beta), FP32 in and out.  Each FP32
-// operand x is split into x_hi = bf16(x) and x_lo = bf16(x - x_hi); the
-// product is accumulated in FP32 in tensor memory as
-//     a_hi*b_hi + a_hi*b_lo + a_lo*b_hi
-// (the a_lo*b_lo term, ~2^-16 relative, is dropped).  This is the precision
-// form of the reference's FP32 SGEMM (sgemm_release_V1.3.2/device_code/
-// sgemm_kernel.c:2476-4505); it has no counterpart in the reference.
+// operand value is cut into 16-bit pieces and the piece products that carry
+// FP32's precision are accumulated in FP32 in tensor memory.  These are the
+// precision forms of the reference's FP32 SGEMM (sgemm_release_V1.3.2/
+// device_code/sgemm_kernel.c:2476-4505); none has a counterpart there.
+//  - BF16X3: x_hi = bf16(x), x_lo = bf16(x - x_hi); a_hi*b_hi + a_hi*b_lo +
+//    a_lo*b_hi (the a_lo*b_lo term, ~2^-16 relative, is dropped; hi + lo
+//    carry ~16 of FP32's 24 bits).
+//  - BF16X6: three BF16 pieces (24 bits), the six products of weight >=
+//    2^-16, the accumulator restarted every 256 k and folded in registers.
+//  - FP16X3: every row of op(A) and column of op(B) scaled by a power of two
+//    that puts its largest magnitude in [2^14, 2^15), then x_hi = fp16(x),
+//    x_lo = fp16(x - x_hi) (22 bits), the same three products as BF16X3, the
+//    accumulator restarted every 128 k and folded in registers, and the
+//    scales undone exactly in the epilogue.
 //
-// Two kernels:
-//  1. split: op(A) -> A_hi, A_lo (M x Kp, K-major BF16), op(B) -> B_hi, B_lo
-//     (N x Kp, K-major), Kp = K rounded up to 64 with zeros.  The transpose
-//     modes are absorbed here (a row-major or a transposed read, always a
-//     K-major write), so the GEMM kernel has one operand layout.
-//  2. gemm: persistent, one CTA per SM over 128 x 256 C tiles, K in blocks of
+// Kernels:
+//  1. (FP16X3) scan: the largest |x| of every row of op(A) and column of op(B).
+//  2. split: op(A) -> pieces (M x Kp, K-major), op(B) -> pieces (N x Kp,
+//     K-major), Kp = K rounded up to 64 with zeros.  The transpose modes are
+//     absorbed here (a row-major or a transposed read, always a K-major
+//     write), so the GEMM kernel has one operand layout.
+//  3. gemm: persistent, one CTA per SM over 128 x 256 C tiles, K in blocks of
 //     32 (one 64-byte swizzle atom), a 4-stage TMA -> shared memory pipeline
 //     with mbarriers; warp 0 issues TMA, warp 1 issues tcgen05.mma (M=128,
 //     N=256, K=16, three products per K step into a TMEM accumulator of 256
-//     columns, two accumulators alternating between tiles), warps 2-5 read
-//     the finished accumulator with tcgen05.ld, stage it through shared memory
-//     and write C row-contiguously with alpha/beta applied.
+//     columns, two accumulators alternating), the epilogue warps read the
+//     finished accumulator with tcgen05.ld and write C with alpha/beta.
+// Skinny products (min(M, N) <= 64) run BF16X3 in one fused kernel instead
+// (TMA of the FP32 tiles, converter warps, MMA).
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdlib.h>
 #include <string.h>
+
+#include <atomic>
+#include <mutex>
+#include <vector>
 
 #include "gb_common.cuh"
 #include "sm100_ptx.cuh"
@@ -103,16 +119,214 @@ bool make_tmap_f64(CUtensorMap *map, const void *base, uint64_t inner, uint64_t 
 
 namespace {
 
+// ------------------------------------------------------------ FP16 scaling
+// The FP16 form (FP16X3) carries each FP32 value as two FP16 pieces, 11 + 11
+// significand bits, after scaling its line -- a row of op(A) or a column of
+// op(B) -- by a power of two that puts the line's largest magnitude in
+// [2^14, 2^15): FP16 cannot overflow there, and what falls below FP16's
+// subnormal floor (2^-24) is 2^-38 of the line's maximum or less.  The
+// epilogue undoes both scalings exactly.  (Three-product FP16 splitting
+// with scaling is the method of Ootomo & Yokota, "Recovering single
+// precision accuracy from Tensor Cores while surpassing the FP32 theoretical
+// peak performance", IJHPCA 2022; the per-line power-of-two scaling and the
+// folded accumulation here are this library's.)
+
+// Scale exponent s of a line from the bit pattern of its largest |x|:
+// max * 2^s in [2^14, 2^15).  0 for an all-zero line; kNonFiniteScale for a
+// line holding an Inf or a NaN (whose outputs the epilogue recomputes as
+// plain dot products).
+constexpr int kNonFiniteScale = -100000;
+__device__ __forceinline__ int f16_line_scale(unsigned mb) {
+    if (mb == 0u) return 0;
+    if (mb >= 0x7f800000u) return kNonFiniteScale;
+    const int e = mb >= 0x00800000u ? (int)(mb >> 23) - 127 : (31 - __clz((int)mb)) - 149;
+    return 14 - e;   // -113 .. 163
+}
+
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }   // -126 <= k <= 127
+
+// x * 2^s for s in [-113, 163]: exact, in two steps above 2^127 (the line's
+// maximum is then below 2^-113, so the first step cannot overflow)
+__device__ __forceinline__ float scale_line(float x, int s) {
+    return s > 127 ? (x * pow2f(127)) * pow2f(s - 127) : x * pow2f(s);
+}
+
+// x * 2^k for |k| <= 378: one exact multiply in the normal range, else
+// factors applied largest first (only a result outside the normal range rounds)
+__device__ __forceinline__ float mul_pow2f(float x, int k) {
+    if (k >= -126 && k <= 127) return x * pow2f(k);
+    const int a = max(-126, min(127, k));
+    k -= a;
+    const int b = max(-126, min(127, k));
+    k -= b;
+    return x * pow2f(a) * pow2f(b) * pow2f(max(-126, min(127, k)));
+}
+
+// Plain FP32 dot product of row i of op(A) and column j of op(B), in k order:
+// the outputs whose line holds an Inf or a NaN, so that those propagate as
+// IEEE arithmetic has them.
+__device__ __noinline__ float dot_f32_cold(const float *A, int64_t lda, int ta, int64_t i, const float *B, int64_t ldb,
+                                           int tb, int64_t j, int64_t K) {
+    float s = 0.f;
+    for (int64_t k = 0; k < K; k++) {
+        const float a = ta ? A[k * lda + i] : A[i * lda + k];
+        const float b = tb ? B[j * ldb + k] : B[k * ldb + j];
+        s = fmaf(a, b, s);
+    }
+    return s;
+}
+
+// ------------------------------------------------------ programmatic launch
+// A split pass may be launched (programmatic stream serialization) to run
+// beside the previous call's GEMM on the same stream, which triggers its
+// dependents as it starts.  The host allows that only when this call's A and
+// B do not overlap the previous GEMM's C.  What the host cannot see is work
+// the caller queued between the two calls: with such work in between, the
+// split starts only once that work has finished (it does not trigger early),
+// and by then the previous GEMM has finished as well.  So each CTA reads the
+// count of finished GEMM CTAs: below `expect` (the CTAs launched up to and
+// including the previous GEMM), the previous GEMM is still running and is the
+// split's immediate predecessor, and A and B are safe to read; otherwise it
+// waits for the preceding grid's completion and memory flush before reading.
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void split_entry_guard(const unsigned long long *done, unsigned long long expect) {
+    __shared__ int must_wait;
+    if (threadIdx.x == 0) must_wait = done == nullptr || ld_acquire_u64(done) >= expect;
+    __syncthreads();
+    if (must_wait) ptx::pdl_wait();   // returns at once when not launched as a dependent
+}
+
+// ------------------------------------------------------------------ scan
+// Largest |x| bit pattern of every row of op(X) (rows x K) -- non-negative
+// floats order as their bit patterns -- by atomicMax from 64 x 64 tiles
+// (out cleared first).  Both operands in one launch; `vec`: 16-byte loads.
+struct ScanOp {
+    const float *X;
+    int64_t ldx, rows, tiles_k, tiles;
+    int trans;                      // element (r, k) at X[k*ldx + r]
+    unsigned *out;
+};
+struct ScanArgs {
+    ScanOp op[2];
+    int64_t K;
+    int vec;
+};
+
+__device__ __forceinline__ unsigned absbits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+
+__global__ void __launch_bounds__(256) maxbits_kernel(const __grid_constant__ ScanArgs a) {
+    __shared__ unsigned red[16][65];
+    int64_t b = blockIdx.x;
+    const int w = b < a.op[0].tiles ? 0 : 1;
+    if (w) b -= a.op[0].tiles;
+    const ScanOp &o = a.op[w];
+    const int64_t r0 = (b / o.tiles_k) * 64, k0 = (b % o.tiles_k) * 64;
+    const int t = threadIdx.x, c4 = 4 * (t % 16), rl = t / 16;
+    if (!o.trans) {   // 16 threads (a half warp) per row, 4 k each
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int64_t r = r0 + rl + 16 * i, k = k0 + c4;
+            unsigned m = 0;
+            if (r < o.rows) {
+                const float *src = o.X + r * o.ldx + k;
+                if (a.vec && k + 3 < a.K) {
+                    const float4 x = __ldg(reinterpret_cast<const float4 *>(src));
+                    m = max(max(absbits(x.x), absbits(x.y)), max(absbits(x.z), absbits(x.w)));
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (k + q < a.K) m = max(m, absbits(src[q]));
+                }
+            }
+#pragma unroll
+            for (int s = 8; s >= 1; s >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, s));
+            if ((t & 15) == 0 && r < o.rows && m) atomicMax(&o.out[r], m);
+        }
+        return;
+    }
+    unsigned m[4] = {0u, 0u, 0u, 0u};   // 4 consecutive rows, 4 k each
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const int64_t k = k0 + rl + 16 * i, r = r0 + c4;
+        if (k >= a.K) continue;
+        const float *src = o.X + k * o.ldx + r;
+        if (a.vec && r + 3 < o.rows) {
+            const float4 x = __ldg(reinterpret_cast<const float4 *>(src));
+            m[0] = max(m[0], absbits(x.x)); m[1] = max(m[1], absbits(x.y));
+            m[2] = max(m[2], absbits(x.z)); m[3] = max(m[3], absbits(x.w));
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (r + q < o.rows) m[q] = max(m[q], absbits(src[q]));
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) red[rl][c4 + q] = m[q];
+    __syncthreads();
+    if (t < 64) {
+        unsigned mm = 0;
+#pragma unroll
+        for (int j = 0; j < 16; j++) mm = max(mm, red[j][t]);
+        if (r0 + t < o.rows && mm) atomicMax(&o.out[r0 + t], mm);
+    }
+}
+
 // ------------------------------------------------------------------ split
+// Pieces of one value.  BF16 (F16 = false): x = hi + lo (+ lo2) exactly up
+// to the last piece, each piece the rounded remainder.  FP16 (F16 = true):
+// x is first scaled by its line's 2^s (s = kNonFiniteScale: the line holds
+// an Inf or a NaN, its outputs are recomputed, and hi = x, lo = 0).
+template <bool F16>
+struct Pieces;
+
+template <>
+struct Pieces<false> {
+    using T = __nv_bfloat16;
+    static __device__ __forceinline__ void cut(float x, int, T &h, T &l, T &l2) {
+        h = __float2bfloat16_rn(x);
+        const float rem = x - __bfloat162float(h);   // exact
+        l = __float2bfloat16_rn(rem);
+        l2 = __float2bfloat16_rn(rem - __bfloat162float(l));
+    }
+    static __device__ __forceinline__ uint16_t bits(T v) { return __bfloat16_as_ushort(v); }
+};
+
+template <>
+struct Pieces<true> {
+    using T = __half;
+    static __device__ __forceinline__ void cut(float x, int s, T &h, T &l, T &l2) {
+        l2 = __float2half_rn(0.f);
+        if (s == kNonFiniteScale) {
+            h = __float2half_rn(x);
+            l = l2;
+            return;
+        }
+        const float v = scale_line(x, s);           // |v| < 2^15
+        h = __float2half_rn(v);
+        l = __float2half_rn(v - __half2float(h));   // the remainder is exact in FP32
+    }
+    static __device__ __forceinline__ uint16_t bits(T v) { return __half_as_ushort(v); }
+};
+
 // out_hi/out_lo(/out_lo2): rows x kp (K-major).  Source element (r, k):
 // trans ? X[k*ldx + r] : X[r*ldx + k].  32x32 tiles through shared memory
 // so both the read and the write are coalesced in either layout.  With
 // out_lo2 the value is cut in three BF16 pieces (hi, mid, lo: 24 bits).
+// mbits (FP16 form): the largest |x| bit pattern of each row.
+template <bool F16>
 __global__ void __launch_bounds__(256) split_kernel(const float *__restrict__ X, int64_t ldx, int trans, int64_t rows,
-                                                    int64_t K, int64_t kp, __nv_bfloat16 *__restrict__ out_hi,
-                                                    __nv_bfloat16 *__restrict__ out_lo,
-                                                    __nv_bfloat16 *__restrict__ out_lo2) {
+                                                    int64_t K, int64_t kp, uint16_t *__restrict__ out_hi,
+                                                    uint16_t *__restrict__ out_lo, uint16_t *__restrict__ out_lo2,
+                                                    const unsigned *__restrict__ mbits,
+                                                    const unsigned long long *done, unsigned long long expect) {
+    using P = Pieces<F16>;
     __shared__ float tile[32][33];
+    split_entry_guard(done, expect);
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;   // 32 x 8
     const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
 #pragma unroll
@@ -133,18 +347,15 @@ __global__ void __launch_bounds__(256) split_kernel(const float *__restrict__ X,
     for (int i = 0; i < 32; i += 8) {
         int64_t r = r0 + ty + i, k = k0 + tx;
         if (r < rows && k < kp) {
-            float x = tile[tx][ty + i];
-            __nv_bfloat16 h = __float2bfloat16_rn(x);
-            const float rem = x - __bfloat162float(h);   // exact
-            __nv_bfloat16 l = __float2bfloat16_rn(rem);
-            out_hi[r * kp + k] = h;
-            out_lo[r * kp + k] = l;
-            if (out_lo2) out_lo2[r * kp + k] = __float2bfloat16_rn(rem - __bfloat162float(l));
+            typename P::T h, l, l2;
+            P::cut(tile[tx][ty + i], F16 ? f16_line_scale(mbits[r]) : 0, h, l, l2);
+            out_hi[r * kp + k] = P::bits(h);
+            out_lo[r * kp + k] = P::bits(l);
+            if (out_lo2) out_lo2[r * kp + k] = P::bits(l2);
         }
     }
-    // launched to overlap the previous call's GEMM (programmatic stream serialization): one
-    // thread keeps the grid from completing before that grid has, so the stream order of the
-    // GEMM that follows is unchanged
+    // possibly launched to overlap the previous call's GEMM: one thread keeps the grid from
+    // completing before that grid has, so the stream order of the GEMM that follows is unchanged
     if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) ptx::pdl_wait();
 }
 
@@ -158,37 +369,42 @@ struct SplitOp {
     const float *X;
     int64_t ldx, rows, tiles_k, tiles;
     int trans;                      // source element (r, k) at X[k*ldx + r]
-    __nv_bfloat16 *out[3];
+    uint16_t *out[3];
+    const unsigned *mbits;          // FP16 form: largest |x| bit pattern per row
 };
 struct SplitArgs {
     SplitOp op[2];
     int64_t K, kp;
     int np;
+    const unsigned long long *done;
+    unsigned long long expect;
 };
 
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 a, __nv_bfloat16 b) {
-    return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
-}
-
+template <bool F16>
 __device__ __forceinline__ void split_store4(const SplitArgs &a, const SplitOp &o, int64_t r, int64_t k,
                                              const float (&v)[4]) {
-    __nv_bfloat16 h[4], l[4], l2[4];
+    using P = Pieces<F16>;
+    const int s = F16 ? f16_line_scale(o.mbits[r]) : 0;
+    uint32_t h[2], l[2], l2[2];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        h[q] = __float2bfloat16_rn(v[q]);
-        const float rem = v[q] - __bfloat162float(h[q]);   // exact
-        l[q] = __float2bfloat16_rn(rem);
-        l2[q] = __float2bfloat16_rn(rem - __bfloat162float(l[q]));
+    for (int q = 0; q < 4; q += 2) {
+        typename P::T h0, l0, m0, h1, l1, m1;
+        P::cut(v[q], s, h0, l0, m0);
+        P::cut(v[q + 1], s, h1, l1, m1);
+        h[q / 2] = (uint32_t)P::bits(h0) | ((uint32_t)P::bits(h1) << 16);
+        l[q / 2] = (uint32_t)P::bits(l0) | ((uint32_t)P::bits(l1) << 16);
+        l2[q / 2] = (uint32_t)P::bits(m0) | ((uint32_t)P::bits(m1) << 16);
     }
     const int64_t off = r * a.kp + k;
-    *reinterpret_cast<uint2 *>(o.out[0] + off) = make_uint2(pack2(h[0], h[1]), pack2(h[2], h[3]));
-    *reinterpret_cast<uint2 *>(o.out[1] + off) = make_uint2(pack2(l[0], l[1]), pack2(l[2], l[3]));
-    if (a.np == 3)
-        *reinterpret_cast<uint2 *>(o.out[2] + off) = make_uint2(pack2(l2[0], l2[1]), pack2(l2[2], l2[3]));
+    *reinterpret_cast<uint2 *>(o.out[0] + off) = make_uint2(h[0], h[1]);
+    *reinterpret_cast<uint2 *>(o.out[1] + off) = make_uint2(l[0], l[1]);
+    if (a.np == 3) *reinterpret_cast<uint2 *>(o.out[2] + off) = make_uint2(l2[0], l2[1]);
 }
 
+template <bool F16>
 __global__ void __launch_bounds__(256) split_vec_kernel(const __grid_constant__ SplitArgs a) {
     __shared__ float tile[64][65];
+    split_entry_guard(a.done, a.expect);
     int64_t b = blockIdx.x;
     const int w = b < a.op[0].tiles ? 0 : 1;
     if (w) b -= a.op[0].tiles;
@@ -210,7 +426,7 @@ __global__ void __launch_bounds__(256) split_vec_kernel(const __grid_constant__ 
                 for (int q = 0; q < 4; q++)
                     if (k + q < a.K) v[q] = src[q];
             }
-            split_store4(a, o, r, k, v);
+            split_store4<F16>(a, o, r, k, v);
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) ptx::pdl_wait();   // as split_kernel
         return;
@@ -239,7 +455,7 @@ __global__ void __launch_bounds__(256) split_vec_kernel(const __grid_constant__ 
         const int64_t r = r0 + rr;
         if (r >= o.rows) continue;
         const float v[4] = {tile[c4][rr], tile[c4 + 1][rr], tile[c4 + 2][rr], tile[c4 + 3][rr]};
-        split_store4(a, o, r, k0 + c4, v);
+        split_store4<F16>(a, o, r, k0 + c4, v);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) ptx::pdl_wait();   // as split_kernel
 }
@@ -248,21 +464,24 @@ __global__ void __launch_bounds__(256) split_vec_kernel(const __grid_constant__ 
 // Persistent: one CTA per SM walks the 128 x BN C tiles in a grouped order
 // (GROUP_M tile rows at a time, so neighbouring CTAs share A and B tiles in
 // L2).  K in blocks of 32 (one 64-byte swizzle atom), 4 shared-memory stages
-// of 48 KB holding NP BF16 pieces of the A and B tiles (NP = 2: hi, lo with
-// BN = 256; NP = 3: hi, mid, lo with BN = 128).  Two TMEM accumulators of BN
-// columns: the epilogue of tile i (warps 2-5) overlaps the MMAs of tile i+1
-// (warp 1).
+// holding NP 16-bit pieces of the A and B tiles (NP = 2: hi, lo with BN =
+// 256; NP = 3: hi, mid, lo with BN = 128).  Two TMEM accumulators: the
+// epilogue of tile (or accumulator chunk) i overlaps the MMAs of i+1.
 constexpr int BM = 128, BK = 32, STAGES = 4, GROUP_M = 8;
 constexpr int A_TILE = BM * BK * 2;            // 8 KB
-constexpr int EPI_BYTES = 4 * 32 * 33 * 4;     // per-warp 32 x 32 staging, padded
-constexpr int NT = 192;
+constexpr int EPI_BYTES = 4 * 32 * 33 * 4;     // four warps' 32 x 32 staging, padded
 
-template <int NP, int BN>
+// EW epilogue warps: 4 (one per TMEM lane quarter, all BN columns, C staged
+// through shared memory) or 8 (two per lane quarter, 128 columns each: the
+// wide folding form, C written from registers).
+template <int NP, int BN, int EW>
 struct TwoPass {
     static constexpr int B_TILE = BN * BK * 2;
     static constexpr int STAGE_BYTES = NP * A_TILE + NP * B_TILE;
-    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI_BYTES + 1024 /*align*/ + 256 /*barriers*/;
-    static constexpr uint32_t ACC_COLS = BN, TMEM_COLS = 2 * BN;
+    static constexpr int NT = 64 + 32 * EW;
+    static constexpr int EPI = EW == 4 ? EPI_BYTES : 0;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI + 1024 /*align*/ + 256 /*barriers*/ +
+                                      EW * 32 * 4 /*row scales*/;
 };
 
 // tensor maps of the A and B pieces (hi, lo[, lo2])
@@ -280,71 +499,36 @@ struct EpiParams {
     int tiles_m, tiles_n;
     int *err;
     int chunk_kb;    // k-blocks per accumulator chunk (folding form)
-    // Stream-K tail: tiles [0, dp_tiles) go whole to CTAs in turn; the K
-    // iterations of tiles [dp_tiles, tiles) are split evenly over the grid, so
-    // a tile there may be computed in two parts (by CTAs b and b + 1): each
-    // part's raw accumulator goes to sk_part[2b + half], and the second CTA to
-    // finish (sk_cnt[b]) adds the two in order and writes C.
-    int dp_tiles;
-    float *sk_part;
-    int *sk_cnt;
     // Half-tile tail: tiles [half_start, tiles) (a last wave at most half
     // full) run as two 128-column halves on different CTAs, so the wave takes
     // half a tile time.
     int half_start;
+    // CTAs of this stream's GEMMs that have finished (read by the next call's
+    // split pass, see split_entry_guard); null when not tracked
+    unsigned long long *done;
+    // FP16 form: largest |x| bit patterns of op(A)'s rows and op(B)'s columns
+    // (the scale of each line), and the operands, for the outputs recomputed
+    // as plain dot products
+    const unsigned *rowbits, *colbits;
+    const float *A, *B;
+    int64_t lda, ldb, K;
+    int ta, tb;
 };
 
-// Work items of one CTA: (tile, k-blocks [kb0, kb1), half: -1 whole tile,
-// 0 / 1 the left / right 128 columns).
-struct WorkIt {
-    int i;
-    int64_t pos, end;   // stream-K position / end in (tile - dp_tiles) * num_kb + kb
-};
-
-__device__ __forceinline__ bool next_item(const EpiParams &p, int num_tiles, WorkIt &w, int &tile, int &kb0,
-                                          int &kb1, int &half) {
+// Work item i of this CTA: a whole tile (half = -1) or the left / right 128
+// columns of a tail tile (half 0 / 1).
+__device__ __forceinline__ bool next_item(const EpiParams &p, int num_tiles, int &i, int &tile, int &half) {
+    const int t = blockIdx.x + i * gridDim.x;
+    i++;
     half = -1;
-    if (p.half_start < num_tiles) {   // whole tiles, then the tail in halves
-        const int t = blockIdx.x + w.i * gridDim.x;
-        w.i++;
-        kb0 = 0; kb1 = p.num_kb;
-        if (t < p.half_start) { tile = t; return true; }
-        const int h = t - p.half_start;
-        if (h >= 2 * (num_tiles - p.half_start)) return false;
-        tile = p.half_start + h / 2;
-        half = h & 1;
+    if (t < p.half_start) {
+        tile = t;
         return true;
     }
-    if (w.pos < 0) {
-        const int t = blockIdx.x + w.i * gridDim.x;
-        if (t < p.dp_tiles) {
-            tile = t; kb0 = 0; kb1 = p.num_kb; w.i++;
-            return true;
-        }
-        const int64_t W = (int64_t)(num_tiles - p.dp_tiles) * p.num_kb;
-        w.pos = W * blockIdx.x / gridDim.x;
-        w.end = W * (blockIdx.x + 1) / gridDim.x;
-    }
-    if (w.pos >= w.end) return false;
-    if (blockIdx.x & 1) {
-        // odd CTAs walk their range backwards, so both parts of every split
-        // tile are computed at the same time (by the end of two neighbours'
-        // walks or by their start) and share its operand tiles in L2
-        const int st = (int)((w.end - 1) / p.num_kb);
-        const int64_t t0 = (int64_t)st * p.num_kb;
-        const int64_t s0 = w.pos > t0 ? w.pos : t0;
-        kb0 = (int)(s0 - t0);
-        kb1 = (int)(w.end - t0);
-        tile = p.dp_tiles + st;
-        w.end = s0;
-        return true;
-    }
-    const int st = (int)(w.pos / p.num_kb);
-    kb0 = (int)(w.pos - (int64_t)st * p.num_kb);
-    const int64_t left = w.end - w.pos;
-    kb1 = left < p.num_kb - kb0 ? kb0 + (int)left : p.num_kb;
-    tile = p.dp_tiles + st;
-    w.pos += kb1 - kb0;
+    const int h = t - p.half_start;
+    if (h >= 2 * (num_tiles - p.half_start)) return false;
+    tile = p.half_start + h / 2;
+    half = h & 1;
     return true;
 }
 
@@ -358,32 +542,69 @@ __device__ __forceinline__ void tile_coords(int t, int tiles_m, int tiles_n, int
     tn = r / gm;
 }
 
+// Instruction descriptor of kind::f16 with FP16 (F16) or BF16 operands, FP32 accumulation.
+template <bool F16>
+__host__ __device__ constexpr uint32_t idesc_f32acc(int M, int N) {
+    return F16 ? (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24) : ptx::idesc_bf16_f32(M, N);
+}
+
+__device__ __forceinline__ bool reads_c(const EpiParams &p) {
+    return p.semantics == GB_SEM_ACCUM_SCALAR_BETA || (p.semantics == GB_SEM_BLAS && p.beta != 0.f);
+}
+
+// alpha/beta epilogue of one output from its product x (and C's old value
+// when reads_c): C = alpha x + beta C (BLAS), alpha x + beta, C + (alpha x + beta)
+__device__ __forceinline__ float epi_value(const EpiParams &p, float x, float cin) {
+    const float v = p.alpha * x;
+    if (p.semantics == GB_SEM_BLAS) return p.beta != 0.f ? fmaf(p.beta, cin, v) : v + 0.f;
+    if (p.semantics == GB_SEM_SCALAR_BETA) return v + p.beta;
+    return cin + (v + p.beta);
+}
+
+// The output (row, col) from a plain FP32 dot product (its row of op(A) or
+// column of op(B) holds an Inf or a NaN), written with the epilogue.
+__device__ __noinline__ void store_recomputed(const EpiParams &p, int64_t row, int64_t col) {
+    const float x = dot_f32_cold(p.A, p.lda, p.ta, row, p.B, p.ldb, p.tb, col, p.K);
+    float *c = p.C + row * p.ldc + col;
+    *c = epi_value(p, x, reads_c(p) ? *c : 0.f);
+}
+
 // FOLD: the tensor cores add each MMA into the FP32 accumulator with an
-// error of about one unit in the last place of the accumulator, so over a
-// long K the error grows with the number of MMAs and with the size of the
-// running sum.  With FOLD the accumulator is restarted every chunk_kb
-// k-blocks (chunk_kb * 32 values of K) and the epilogue warps add each chunk
-// into an FP32 running total held in registers (round-to-nearest), and the
-// most significant product hi*hi is accumulated apart from the small
-// cross products, so only the hi*hi MMAs add into a large accumulator.
-// TMEM: two chunk buffers of 256 columns (hi*hi at +0, the rest at +128),
-// BN = 128; the MMAs of chunk c+1 overlap the fold of chunk c.
-template <int NP, int BN, bool FOLD>
-__global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constant__ PieceMaps maps, EpiParams p) {
+// error of about one unit in the last place of the accumulator, biased like
+// a truncation, so over a long K the error grows with the number of MMAs and
+// with the size of the running sum.  With FOLD the accumulator is restarted
+// every chunk_kb k-blocks (chunk_kb * 32 values of K) and the epilogue warps
+// add each chunk into an FP32 running total held in registers
+// (round-to-nearest).  Two forms:
+//  - BN = 128, 4 epilogue warps (BF16X6): the most significant product hi*hi
+//    is accumulated apart from the cross products, so only the hi*hi MMAs add
+//    into a large accumulator; TMEM: two chunk buffers of 256 columns (hi*hi
+//    at +0, the rest at +128).
+//  - BN = 256, 8 epilogue warps (FP16X3, BF16X3 folded): all products in one
+//    accumulator of 256 columns, two chunk buffers; each epilogue warp keeps
+//    the totals of 32 rows x 128 columns and writes C from registers.
+// The MMAs of chunk c+1 overlap the fold of chunk c.
+// F16: FP16 pieces of scaled lines (FP16X3), the epilogue applies the scales.
+template <int NP, int BN, bool FOLD, bool F16, int EW>
+__global__ void __launch_bounds__(64 + 32 * EW, 1)
+    bf16x3_gemm_kernel(const __grid_constant__ PieceMaps maps, EpiParams p) {
     // the next call's split pass may start beside this grid (it writes the other workspace half)
     if (threadIdx.x == 0) ptx::pdl_launch_dependents();
-    using CF = TwoPass<NP, BN>;
-    static_assert(!FOLD || BN == 128, "the folding form keeps a 128-column total per thread");
+    using CF = TwoPass<NP, BN, EW>;
+    constexpr bool SEP = FOLD && EW == 4;   // hi*hi apart from the cross products
+    static_assert(!SEP || BN == 128, "the separated folding form keeps a 128-column total per thread");
+    static_assert(EW == 4 || (FOLD && BN == 256), "eight epilogue warps: the wide folding form");
     constexpr int B_TILE = CF::B_TILE, STAGE_BYTES = CF::STAGE_BYTES;
-    constexpr uint32_t ACC_COLS = FOLD ? 256 : CF::ACC_COLS, TMEM_COLS = FOLD ? 512 : CF::TMEM_COLS;
+    constexpr uint32_t ACC_COLS = SEP ? 256 : BN, TMEM_COLS = 2 * ACC_COLS;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     float *epi = reinterpret_cast<float *>(smem + STAGES * STAGE_BYTES);
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES + EPI_BYTES);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES + CF::EPI);
     uint64_t *empty = full + STAGES;
     uint64_t *acc_full = empty + STAGES;     // [2]
     uint64_t *acc_empty = acc_full + 2;      // [2]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+    int *row_scale = reinterpret_cast<int *>(smem + STAGES * STAGE_BYTES + CF::EPI + 256);   // [4][32]
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int num_tiles = p.tiles_m * p.tiles_n;
@@ -396,7 +617,7 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
         }
         for (int b = 0; b < 2; b++) {
             ptx::mbar_init(&acc_full[b], 1);
-            ptx::mbar_init(&acc_empty[b], 4);   // one arrive per epilogue warp
+            ptx::mbar_init(&acc_empty[b], EW);   // one arrive per epilogue warp
         }
         ptx::fence_mbar_init();
         for (int i = 0; i < NP; i++) {
@@ -414,14 +635,13 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
         if (lane == 0) {   // TMA producer
             int kbg = 0;   // running k-block counter across tiles (stage / phase)
             bool go = true;
-            WorkIt wi{0, -1, 0};
-            int t, kbA, kbB, half;
-            while (go && next_item(p, num_tiles, wi, t, kbA, kbB, half)) {
+            int it = 0, t, half;
+            while (go && next_item(p, num_tiles, it, t, half)) {
                 int tm, tn;
                 tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
                 const int m0 = tm * BM, n0 = tn * BN + (half > 0 ? BN / 2 : 0);
                 const uint32_t bytes = half < 0 ? STAGE_BYTES : NP * A_TILE + NP * (B_TILE / 2);
-                for (int kb = kbA; kb < kbB; kb++, kbg++) {
+                for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
                     const int s = kbg % STAGES;
                     if (kbg >= STAGES && !ptx::mbar_wait(&empty[s], ((kbg / STAGES) & 1) ^ 1, p.err, 1)) {
                         go = false;
@@ -440,16 +660,14 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
         }
     } else if (warp == 1) {
         if (lane == 0) {   // MMA issuer
-            constexpr uint32_t idesc = ptx::idesc_bf16_f32(BM, BN);
+            constexpr uint32_t idesc = idesc_f32acc<F16>(BM, BN);
+            constexpr uint32_t idesc_half = idesc_f32acc<F16>(BM, BN / 2);
             int kbg = 0, ch = 0;   // running k-block and accumulator-chunk counters
-            (void)B_TILE;
             bool go = true;
-            constexpr uint32_t idesc_half = ptx::idesc_bf16_f32(BM, BN / 2);
-            WorkIt wi{0, -1, 0};
-            int t, kbA, kbB, half;
-            while (go && next_item(p, num_tiles, wi, t, kbA, kbB, half)) {
+            int it = 0, t, half;
+            while (go && next_item(p, num_tiles, it, t, half)) {
                 const uint32_t id = half < 0 ? idesc : idesc_half;
-                const int nch = (kbB - kbA + chunk_kb - 1) / chunk_kb;
+                const int nch = (p.num_kb + chunk_kb - 1) / chunk_kb;
                 for (int c = 0; c < nch && go; c++, ch++) {
                     const int b = ch & 1;
                     if (ch >= 2 && !ptx::mbar_wait(&acc_empty[b], ((ch >> 1) & 1) ^ 1, p.err, 2)) {
@@ -458,9 +676,9 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                     }
                     ptx::tc_fence_after();
                     const uint32_t acc = tmem + (uint32_t)(b * ACC_COLS);
-                    const uint32_t acc_lo = FOLD ? acc + 128u : acc;   // cross products
-                    const int kbc = kbA + c * chunk_kb;
-                    const int kb1 = kbc + chunk_kb < kbB ? kbc + chunk_kb : kbB;
+                    const uint32_t acc_lo = SEP ? acc + 128u : acc;   // cross products
+                    const int kbc = c * chunk_kb;
+                    const int kb1 = kbc + chunk_kb < p.num_kb ? kbc + chunk_kb : p.num_kb;
                     for (int kb = kbc; kb < kb1; kb++, kbg++) {
                         const int s = kbg % STAGES;
                         if (!ptx::mbar_wait(&full[s], (kbg / STAGES) & 1, p.err, 3)) { go = false; break; }
@@ -475,14 +693,14 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                         const bool first = kb == kbc;
 #pragma unroll
                         for (int k = 0; k < BK / 16; k++) {
-                            // advance 16 BF16 = 32 bytes along K inside the 64-byte swizzle atom
+                            // advance 16 values = 32 bytes along K inside the 64-byte swizzle atom
                             const uint64_t dk = (uint64_t)((k * 32) >> 4);
                             // piece products (i, j) with i + j < NP, least significant first
 #pragma unroll
                             for (int d = NP - 1; d >= 0; d--)
 #pragma unroll
                                 for (int i = d; i >= 0; i--) {
-                                    const bool lead = FOLD ? (d == NP - 1 && i == d) || d == 0 : d == NP - 1 && i == d;
+                                    const bool lead = SEP ? (d == NP - 1 && i == d) || d == 0 : d == NP - 1 && i == d;
                                     ptx::umma_f16(d == 0 ? acc : acc_lo, ad[i] + dk, bd[d - i] + dk, id,
                                                   !(first && k == 0 && lead));
                                 }
@@ -493,31 +711,30 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                 }
             }
         }
-    } else {               // epilogue: warps 2..5 own TMEM lane quarters (warp % 4)
+    } else if constexpr (EW == 4) {   // epilogue: warps 2..5 own TMEM lane quarters (warp % 4)
         const int q = warp % 4;
         float *stage = epi + q * 32 * 33;
+        int *rs = row_scale + q * 32;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         int ch = 0;
         float total[FOLD ? BN : 1];
         bool go = true;
-        __shared__ int sk_last;
-        WorkIt wi{0, -1, 0};
-        int t, kbA, kbB, half;
-        while (go && next_item(p, num_tiles, wi, t, kbA, kbB, half)) {
+        int it = 0, t, half;
+        while (go && next_item(p, num_tiles, it, t, half)) {
             int tm, tn;
             tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
             const int64_t row0 = (int64_t)tm * BM + q * 32;
             const int64_t n0 = (int64_t)tn * BN + (half > 0 ? BN / 2 : 0);
             const int ncols = half < 0 ? BN : BN / 2;
-            // a stream-K part: raw accumulator to its slot, C written by the second finisher
-            const bool part = !FOLD && (kbA != 0 || kbB != p.num_kb);
-            const int sk_b = kbA == 0 ? (int)blockIdx.x : (int)blockIdx.x - 1;
-            float *slot = part ? p.sk_part + ((size_t)sk_b * 2 + (kbA == 0 ? 0 : 1)) * (BM * BN) : nullptr;
+            if (F16) {   // the scale of each of the warp's 32 rows, for the whole tile
+                rs[lane] = row0 + lane < p.M ? f16_line_scale(p.rowbits[row0 + lane]) : 0;
+                __syncwarp();
+            }
             uint32_t accb = 0;
             if (FOLD) {
 #pragma unroll
                 for (int j = 0; j < (FOLD ? BN : 1); j++) total[j] = 0.f;
-                for (int c = 0; c < (kbB - kbA + chunk_kb - 1) / chunk_kb; c++, ch++) {
+                for (int c = 0; c < (p.num_kb + chunk_kb - 1) / chunk_kb; c++, ch++) {
                     const int b = ch & 1;
                     if (!ptx::mbar_wait(&acc_full[b], (ch >> 1) & 1, p.err, 4)) { go = false; break; }
                     ptx::tc_fence_after();
@@ -543,6 +760,7 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                 ptx::tc_fence_after();
                 accb = (uint32_t)(b * ACC_COLS);
             }
+            bool nf = false;   // an output of this thread's columns waits for the recompute pass
 #pragma unroll
             for (int c = 0; c < BN; c += 32) {
                 if (c >= ncols) break;
@@ -559,19 +777,21 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                     for (int j = 0; j < 32; j++) stage[lane * 33 + j] = __uint_as_float(r[j]);
                 }
                 __syncwarp();
-                if (part) {   // raw values, tile-local layout [row][col]
-#pragma unroll
-                    for (int rr = 0; rr < 32; rr++) slot[(q * 32 + rr) * BN + c + lane] = stage[rr * 33 + lane];
-                    __syncwarp();
-                    continue;
-                }
                 const int64_t col = n0 + c + lane;
                 if (col < p.N) {
                     const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
-                    if (p.semantics == GB_SEM_SCALAR_BETA || (p.semantics == GB_SEM_BLAS && p.beta == 0.f)) {
+                    const int cs = F16 ? f16_line_scale(p.colbits[col]) : 0;
+                    if (!reads_c(p)) {
                         const float add = p.semantics == GB_SEM_SCALAR_BETA ? p.beta : 0.f;
-                        for (int rr = 0; rr < rows; rr++)
-                            p.C[(row0 + rr) * p.ldc + col] = p.alpha * stage[rr * 33 + lane] + add;
+                        for (int rr = 0; rr < rows; rr++) {
+                            float x = stage[rr * 33 + lane];
+                            if (F16) {
+                                const int sr = rs[rr];
+                                if (sr == kNonFiniteScale || cs == kNonFiniteScale) { nf = true; continue; }
+                                x = mul_pow2f(x, -(sr + cs));
+                            }
+                            p.C[(row0 + rr) * p.ldc + col] = p.alpha * x + add;
+                        }
                     } else {
                         float cin[32];
 #pragma unroll
@@ -580,9 +800,15 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
 #pragma unroll
                         for (int rr = 0; rr < 32; rr++) {
                             if (rr < rows) {
-                                float v = p.alpha * stage[rr * 33 + lane];
-                                v = p.semantics == GB_SEM_BLAS ? fmaf(p.beta, cin[rr], v) : cin[rr] + (v + p.beta);
-                                p.C[(row0 + rr) * p.ldc + col] = v;
+                                float x = stage[rr * 33 + lane];
+                                bool skip = false;
+                                if (F16) {
+                                    const int sr = rs[rr];
+                                    skip = sr == kNonFiniteScale || cs == kNonFiniteScale;
+                                    x = mul_pow2f(x, -(sr + cs));
+                                }
+                                if (skip) nf = true;
+                                else p.C[(row0 + rr) * p.ldc + col] = epi_value(p, x, cin[rr]);
                             }
                         }
                     }
@@ -595,44 +821,93 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
                 if (lane == 0) ptx::mbar_arrive(&acc_empty[ch & 1]);
                 ch++;
             }
-            if (part) {
-                __threadfence();                                  // this part is visible GPU-wide ...
-                asm volatile("bar.sync 1, 128;" ::: "memory");   // ... for all four epilogue warps
-                if (warp == 2 && lane == 0) {
-                    const int old = atomicAdd(&p.sk_cnt[sk_b], 1);
-                    if (old == 1) p.sk_cnt[sk_b] = 0;            // both parts done: reset for the next call
-                    sk_last = old == 1;
-                    __threadfence();
-                }
-                asm volatile("bar.sync 1, 128;" ::: "memory");
-                if (sk_last) {   // left part + right part, in that order, then the epilogue
-                    const float *p0 = p.sk_part + (size_t)sk_b * 2 * (BM * BN), *p1 = p0 + BM * BN;
+            if (F16 && __any_sync(0xffffffffu, nf)) {   // outputs whose line holds an Inf or a NaN
+                for (int c = 0; c < ncols; c += 32) {
+                    const int64_t col = n0 + c + lane;
+                    if (col >= p.N) continue;
+                    const int cs = f16_line_scale(p.colbits[col]);
                     const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
-                    const bool read_c = p.semantics == GB_SEM_ACCUM_SCALAR_BETA ||
-                                        (p.semantics == GB_SEM_BLAS && p.beta != 0.f);
-                    for (int c = 0; c < BN; c += 32) {
-                        const int64_t col = n0 + c + lane;
-                        if (col >= p.N) continue;
-                        // all 32 rows' loads in flight before any use
-                        float v[32], cin[32];
+                    for (int rr = 0; rr < rows; rr++)
+                        if (rs[rr] == kNonFiniteScale || cs == kNonFiniteScale) store_recomputed(p, row0 + rr, col);
+                }
+            }
+            if (F16) __syncwarp();   // rs is rewritten for the next tile
+        }
+    } else {   // EW == 8: two warps per TMEM lane quarter, 128 columns each
+        const int q = warp % 4, hc = (warp - 2) / 4;
+        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+        const bool vec = (p.ldc & 3) == 0 && ((uintptr_t)p.C & 15) == 0;
+        int ch = 0;
+        float total[128];
+        bool go = true;
+        int it = 0, t, half;
+        while (go && next_item(p, num_tiles, it, t, half)) {
+            int tm, tn;
+            tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+            const int64_t row = (int64_t)tm * BM + q * 32 + lane;
+            const int64_t c0 = (int64_t)tn * BN + hc * 128;
 #pragma unroll
-                        for (int rr = 0; rr < 32; rr++) {
-                            const int e = (q * 32 + rr) * BN + c + lane;
-                            v[rr] = rr < rows ? __ldcg(p0 + e) + __ldcg(p1 + e) : 0.f;
-                            cin[rr] = (read_c && rr < rows) ? p.C[(row0 + rr) * p.ldc + col] : 0.f;
-                        }
+            for (int j = 0; j < 128; j++) total[j] = 0.f;
+            for (int c = 0; c < (p.num_kb + chunk_kb - 1) / chunk_kb; c++, ch++) {
+                const int b = ch & 1;
+                if (!ptx::mbar_wait(&acc_full[b], (ch >> 1) & 1, p.err, 4)) { go = false; break; }
+                ptx::tc_fence_after();
 #pragma unroll
-                        for (int rr = 0; rr < 32; rr++) {
-                            if (rr >= rows) break;
-                            float x = p.alpha * v[rr];
-                            if (p.semantics == GB_SEM_BLAS) x = p.beta != 0.f ? fmaf(p.beta, cin[rr], x) : x;
-                            else if (p.semantics == GB_SEM_SCALAR_BETA) x = x + p.beta;
-                            else x = cin[rr] + (x + p.beta);
-                            p.C[(row0 + rr) * p.ldc + col] = x;
+                for (int g = 0; g < 4; g++) {
+                    uint32_t r[32];
+                    ptx::tmem_ld_32x32b_x32(tmem + (uint32_t)(b * ACC_COLS) + lane_off + (uint32_t)(hc * 128 + g * 32),
+                                            r);
+                    ptx::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; j++) total[g * 32 + j] += __uint_as_float(r[j]);
+                }
+                ptx::tc_fence_before();
+                __syncwarp();
+                if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
+            }
+            if (!go) break;
+            // this thread's row, 128 columns from c0, four at a time
+            bool nf = false;
+            const int sr = (F16 && row < p.M) ? f16_line_scale(p.rowbits[row]) : 0;
+            if (row < p.M) {
+                const bool rc = reads_c(p);
+                float *crow = p.C + row * p.ldc;
+#pragma unroll
+                for (int g = 0; g < 32; g++) {
+                    const int64_t col = c0 + 4 * g;
+                    if (col >= p.N) break;
+                    float x[4] = {total[4 * g], total[4 * g + 1], total[4 * g + 2], total[4 * g + 3]};
+                    bool skip[4] = {false, false, false, false};
+                    if (F16) {
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const int cs = col + j < p.N ? f16_line_scale(p.colbits[col + j]) : 0;
+                            skip[j] = sr == kNonFiniteScale || cs == kNonFiniteScale;
+                            x[j] = mul_pow2f(x[j], -(sr + cs));
                         }
                     }
+                    const bool any_skip = skip[0] | skip[1] | skip[2] | skip[3];
+                    nf |= any_skip;
+                    if (vec && col + 3 < p.N && !any_skip) {
+                        float4 cin = rc ? *reinterpret_cast<const float4 *>(crow + col) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        float4 v;
+                        v.x = epi_value(p, x[0], cin.x);
+                        v.y = epi_value(p, x[1], cin.y);
+                        v.z = epi_value(p, x[2], cin.z);
+                        v.w = epi_value(p, x[3], cin.w);
+                        *reinterpret_cast<float4 *>(crow + col) = v;
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 4; j++)
+                            if (col + j < p.N && !skip[j]) crow[col + j] = epi_value(p, x[j], rc ? crow[col + j] : 0.f);
+                    }
                 }
-                asm volatile("bar.sync 1, 128;" ::: "memory");   // sk_last is reused by the next part
+            }
+            if (F16 && __any_sync(0xffffffffu, nf) && row < p.M) {   // outputs whose line holds an Inf or a NaN
+                const int64_t c1 = c0 + 128 < p.N ? c0 + 128 : p.N;
+                for (int64_t col = c0; col < c1; col++)
+                    if (sr == kNonFiniteScale || f16_line_scale(p.colbits[col]) == kNonFiniteScale)
+                        store_recomputed(p, row, col);
             }
         }
     }
@@ -643,8 +918,8 @@ __global__ void __launch_bounds__(NT, 1) bf16x3_gemm_kernel(const __grid_constan
         ptx::tc_fence_after();
         ptx::tmem_dealloc(tmem, TMEM_COLS);
     }
+    if (threadIdx.x == 0 && p.done) atomicAdd(p.done, 1ull);   // last: this CTA is done
 }
-
 
 // ============================================================ fused split
 // The same 3xBF16 product without a separate split pass: TMA brings FP32
@@ -954,7 +1229,7 @@ gb_status launch(const GemmArgs &g, int *err) {
 }  // namespace fused
 }  // namespace
 
-static gb_status two_pass(const GemmArgs &g, int np, int fold_kb);
+static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16);
 
 // Accumulator chunk (k-blocks of 32) from the environment, for measurement.
 static int env_chunk(const char *name, int dflt) {
@@ -970,7 +1245,6 @@ gb_status launch_sgemm_bf16x3(const GemmArgs &g) {
         return set_status(GB_ERR_UNSUPPORTED, "bf16x3: dimension too large");
     {
         // fused split: FP32 TMA straight from A and B (16-byte aligned bases,
-        // row strides a multiple of 16 bytes)
         // row strides a multiple of 16 bytes).  Used for skinny products
         // (min(M, N) <= 64), where a separate split pass would double the
         // HBM traffic of the streamed operand; large square products keep the
@@ -989,118 +1263,208 @@ gb_status launch_sgemm_bf16x3(const GemmArgs &g) {
             return fused::launch<256>(g, e);
         }
     }
-    return two_pass(g, 2, env_chunk("GB_BF16X3_FOLD", 0));
+    return two_pass(g, 2, env_chunk("GB_BF16X3_FOLD", 0), false);
 }
 
 gb_status launch_sgemm_bf16x6(const GemmArgs &g) {
     if (g.M == 0 || g.N == 0) return ok();
     if (g.M > 0x7fffffff / 2 || g.N > 0x7fffffff / 2 || g.K > 0x7fffffff / 2)
         return set_status(GB_ERR_UNSUPPORTED, "bf16x6: dimension too large");
-    return two_pass(g, 3, env_chunk("GB_BF16X6_CHUNK", 8));
+    return two_pass(g, 3, env_chunk("GB_BF16X6_CHUNK", 8), false);
 }
 
-// Stream-K split of the last waves (tiles that do not fill the grid), or
-// none: dp_tiles = tiles.  Only when every CTA's share of the split range is
-// at least one whole tile, so a split tile has exactly two parts.
-// Off unless GB_BF16X3_SK=1: on this GPU the split measured slower than
-// whole tiles even where whole tiles waste most of a wave (4096^3, 512
-// tiles on 152 SMs: 0.344 vs 0.306 ms per call; 1152 x 4352 x 4096, 153
-// tiles: 0.187 vs 0.163 ms), the two parts of a tile fetching its operand
-// panels separately (L2 traffic +32 %, DRAM reads +60 %).
-static int stream_k_dp_tiles(int tiles, int grid, bool fold) {
-    const char *e = getenv("GB_BF16X3_SK");
-    if (fold || !(e && e[0] == '1') || grid <= 1) return tiles;
-    const int full = tiles / grid, rem = tiles % grid;
-    if (rem == 0 || full < 1) return tiles;
-    return (full - 1) * grid;
+gb_status launch_sgemm_fp16x3(const GemmArgs &g) {
+    if (g.M == 0 || g.N == 0) return ok();
+    if (g.M > 0x7fffffff / 2 || g.N > 0x7fffffff / 2 || g.K > 0x7fffffff / 2)
+        return set_status(GB_ERR_UNSUPPORTED, "fp16x3: dimension too large");
+    return two_pass(g, 2, env_chunk("GB_FP16X3_FOLD", 4), true);
 }
 
-template <int NP, int BN, bool FOLD>
-static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64_t kp, int *err, int fold_kb,
-                                 float *sk_part, int *sk_cnt) {
-    using CF = TwoPass<NP, BN>;
+// ------------------------------------------------------------ stream state
+// Per (device, stream): a counter of finished GEMM CTAs (a slot of a static
+// device array, so tracking needs no allocation), how many CTAs the stream's
+// GEMMs launched so far, the byte range of the last GEMM's C and the
+// workspace half its pieces are in.  A split pass is launched beside the
+// previous GEMM only when that GEMM was this library's, this call's A and B
+// do not overlap its C, and the two halves fit; split_entry_guard covers
+// work the caller queued in between.
+constexpr int kDoneSlots = 1024;
+static __device__ unsigned long long g_gemm_done[kDoneSlots];
+
+struct StreamState {
+    int dev;
+    void *stream;
+    int slot;                    // index into g_gemm_done, -1: none left
+    unsigned long long launched; // CTAs of this stream's GEMMs launched so far
+    bool valid;                  // the stream's last two-pass GEMM is known
+    uintptr_t c_lo, c_hi;        // its C
+    unsigned parity;             // its workspace half
+};
+static std::mutex g_tp_mu;
+static std::vector<StreamState> g_tp;
+static unsigned long long *g_done_base[64] = {nullptr};
+
+static StreamState &stream_state(int dev, void *stream) {
+    int used = 0;
+    for (auto &s : g_tp) {
+        if (s.dev == dev && s.stream == stream) return s;
+        if (s.dev == dev) used++;
+    }
+    g_tp.push_back(StreamState{dev, stream, used < kDoneSlots ? used : -1, 0ull, false, 0, 0, 0u});
+    return g_tp.back();
+}
+
+static unsigned long long *done_counter(int dev, int slot) {
+    if (slot < 0 || dev < 0 || dev >= 64) return nullptr;
+    if (!g_done_base[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_gemm_done) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        g_done_base[dev] = (unsigned long long *)p;
+    }
+    return g_done_base[dev] + slot;
+}
+
+// Bytes [lo, hi) spanned by a rows x cols operand stored with leading
+// dimension ld (transposed storage: cols x rows).
+static void span(const void *p, bool trans, int64_t rows, int64_t cols, int64_t ld, int64_t elem, uintptr_t &lo,
+                 uintptr_t &hi) {
+    const int64_t sr = trans ? cols : rows, sc = trans ? rows : cols;
+    lo = (uintptr_t)p;
+    hi = lo + (uintptr_t)(((sr - 1) * ld + sc) * elem);
+}
+
+template <int NP, int BN, bool FOLD, bool F16, int EW>
+static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64_t kp, const EpiParams &base,
+                                 int *grid_out) {
+    using CF = TwoPass<NP, BN, EW>;
     static std::atomic<uint64_t> attr{0};
     if (device_setup_needed(attr)) {
-        GB_CUDA_TRY(cudaFuncSetAttribute(bf16x3_gemm_kernel<NP, BN, FOLD>,
+        GB_CUDA_TRY(cudaFuncSetAttribute(bf16x3_gemm_kernel<NP, BN, FOLD, F16, EW>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, CF::SMEM_BYTES));
         device_setup_done(attr);
     }
     const int tiles_m = (int)ceil_div(g.M, BM), tiles_n = (int)ceil_div(g.N, BN);
     const int tiles = tiles_m * tiles_n;
     const int grid = tiles < sm_count() ? tiles : sm_count();
-    const int dp = sk_part ? stream_k_dp_tiles(tiles, grid, FOLD) : tiles;
-    if (dp < tiles) GB_CUDA_TRY(cudaMemsetAsync(sk_cnt, 0, (size_t)grid * sizeof(int), g.stream));
     // half-tile tail when the last wave is at most half full (whole tiles
     // would leave most of the GPU idle for a tile time); GB_BF16X3_HALF=0 off
     int half_start = tiles;
     {
         const char *e = getenv("GB_BF16X3_HALF");
         const int rem = tiles % grid;
-        if (!FOLD && BN == 256 && dp == tiles && !(e && e[0] == '0') && rem > 0 && 2 * rem <= grid)
-            half_start = tiles - rem;
+        if (!FOLD && BN == 256 && !(e && e[0] == '0') && rem > 0 && 2 * rem <= grid) half_start = tiles - rem;
     }
-    EpiParams p{(float *)g.C, g.M, g.N, g.ldc, (float)g.alpha, (float)g.beta, g.semantics, (int)(kp / BK),
-                tiles_m, tiles_n, err, FOLD ? fold_kb : 1, dp, sk_part, sk_cnt, half_start};
-    bf16x3_gemm_kernel<NP, BN, FOLD><<<grid, NT, CF::SMEM_BYTES, g.stream>>>(maps, p);
+    EpiParams p = base;
+    p.num_kb = (int)(kp / BK);
+    p.tiles_m = tiles_m;
+    p.tiles_n = tiles_n;
+    p.chunk_kb = FOLD ? p.chunk_kb : 1;
+    p.half_start = half_start;
+    bf16x3_gemm_kernel<NP, BN, FOLD, F16, EW><<<grid, CF::NT, CF::SMEM_BYTES, g.stream>>>(maps, p);
     GB_LAUNCH_CHECK("bf16x3_gemm_kernel");
+    *grid_out = grid;
     return ok();
 }
 
-// Split pass (NP BF16 pieces per operand, K-major) + MMA kernel; fold_kb > 0
-// selects the folding form with that accumulator chunk (in k-blocks of 32).
-static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
+template <bool F16>
+static gb_status gemm_launch(const GemmArgs &g, int np, int fold_kb, const PieceMaps &maps, int64_t kp,
+                             const EpiParams &p, int *grid) {
+    if constexpr (!F16) {   // three pieces are BF16 only
+        if (np == 3)
+            return fold_kb > 0 ? two_pass_launch<3, 128, true, false, 4>(g, maps, kp, p, grid)
+                               : two_pass_launch<3, 128, false, false, 4>(g, maps, kp, p, grid);
+    }
+    return fold_kb > 0 ? two_pass_launch<2, 256, true, F16, 8>(g, maps, kp, p, grid)
+                       : two_pass_launch<2, 256, false, F16, 4>(g, maps, kp, p, grid);
+}
+
+// Split pass (NP 16-bit pieces per operand, K-major) + MMA kernel; fold_kb >
+// 0 selects the folding form with that accumulator chunk (in k-blocks of 32);
+// f16: FP16 pieces of scaled lines (a max-exponent scan first).
+static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
+    if (f16 && np != 2) return set_status(GB_ERR_UNSUPPORTED, "fp16 pieces: two per value");
     const int64_t kp = ceil_div(g.K, 64) * 64;   // multiple of BK, zero-padded
     const size_t a_bytes = (size_t)g.M * kp * 2, b_bytes = (size_t)g.N * kp * 2;
-    // pieces, then the stream-K part slots (2 per CTA of 128 x 256 FP32) and counters
-    const size_t pieces = (np * (a_bytes + b_bytes) + 255) / 256 * 256;
-    const bool sk = np == 2 && fold_kb == 0;
-    const size_t sk_bytes = sk ? (size_t)sm_count() * 2 * BM * 256 * 4 + (size_t)sm_count() * 4 : 0;
-    // Two halves for the pieces, alternating per call on the stream: the split of a call then
-    // writes the half the previous call's GEMM is not reading, and is launched to run beside
-    // that GEMM (programmatic stream serialization; the GEMM triggers it at its start).  One
-    // half, launched in plain order, when the pieces are large or GB_BF16X3_PDL=0.
+    const size_t piece_bytes = (np * (a_bytes + b_bytes) + 255) / 256 * 256;
+    const size_t bits_bytes = f16 ? ((size_t)(g.M + g.N) * 4 + 255) / 256 * 256 : 0;
+    const size_t pieces = piece_bytes + bits_bytes;
+    // The buffer is [half 0 | half 1], the same for every call of any form (the halves move only
+    // when the buffer grows, which first drains its stream).  Calls alternate between the halves,
+    // so a split may run beside the previous GEMM; one half when two do not fit in 16 GiB.
     const char *pe = getenv("GB_BF16X3_PDL");
-    const bool pdl = !(pe && pe[0] == '0') && pieces <= (size_t(8) << 30);
-    const int halves = pdl ? 2 : 1;
-    unsigned seq = 0;
+    const bool pdl_env = !(pe && pe[0] == '0') && !f16;
+    const size_t want = pieces <= (size_t(8) << 30) ? 2 * pieces : pieces;
+    unsigned seq_unused = 0;
     size_t ws_size = 0;
-    // [half 0 | half 1 | stream-K slots]: the halves at fixed places in the buffer, whatever the
-    // size of this call and the last (the buffer only grows after its stream has drained)
-    const size_t tail = (sk_bytes + 4096 + 255) / 256 * 256;
-    uint8_t *ws = (uint8_t *)workspace(halves * pieces + tail + 512, g.stream, &seq, &ws_size);
+    uint8_t *ws = (uint8_t *)workspace(want, g.stream, &seq_unused, &ws_size);
     if (!ws) return (gb_status)gb_get_last_status();
-    const size_t half = (ws_size - tail) / 2 / 256 * 256;   // >= pieces
-    float *sk_part = sk ? (float *)(ws + ws_size - tail) : nullptr;
-    int *sk_cnt = sk ? (int *)(ws + ws_size - tail + (size_t)sm_count() * 2 * BM * 256 * 4) : nullptr;
-    uint8_t *pw = ws + (pdl ? (size_t)(seq & 1) * half : 0);
-    __nv_bfloat16 *ap[3], *bp[3];
-    for (int i = 0; i < np; i++) {
-        ap[i] = (__nv_bfloat16 *)(pw + i * a_bytes);
-        bp[i] = (__nv_bfloat16 *)(pw + np * a_bytes + i * b_bytes);
+    const size_t half = ws_size / 2 / 256 * 256;
+    const bool two_halves = half >= pieces;
+    int *err = error_word();
+    if (!err) return set_status(GB_ERR_OOM, "bf16x3: no device error word");
+    int dev = 0;
+    GB_CUDA_TRY(cudaGetDevice(&dev));
+    static std::atomic<uint64_t> carve{0};
+    if (device_setup_needed(carve)) {   // the GEMM's shared-memory configuration, so a split fits beside it
+        GB_CUDA_TRY(cudaFuncSetAttribute(split_vec_kernel<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        GB_CUDA_TRY(cudaFuncSetAttribute(split_kernel<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        device_setup_done(carve);
     }
+
+    // the stream's state and this call's launches as one step
+    std::lock_guard<std::mutex> lk(g_tp_mu);
+    StreamState &st = stream_state(dev, g.stream);
+    unsigned long long *done = done_counter(dev, st.slot);
+    uintptr_t alo, ahi, blo, bhi, clo, chi;
+    span(g.A, g.ta, g.M, g.K, g.lda, 4, alo, ahi);
+    span(g.B, g.tb, g.K, g.N, g.ldb, 4, blo, bhi);
+    span(g.C, false, g.M, g.N, g.ldc, 4, clo, chi);
+    const bool pdl = pdl_env && two_halves && done != nullptr && st.valid &&
+                     (ahi <= st.c_lo || alo >= st.c_hi) && (bhi <= st.c_lo || blo >= st.c_hi);
+    const unsigned parity = two_halves ? (st.parity ^ 1u) : 0u;
+    uint8_t *pw = ws + (size_t)parity * half;
+    uint16_t *ap[3], *bp[3];
+    for (int i = 0; i < np; i++) {
+        ap[i] = (uint16_t *)(pw + i * a_bytes);
+        bp[i] = (uint16_t *)(pw + np * a_bytes + i * b_bytes);
+    }
+    unsigned *bits = f16 ? (unsigned *)(pw + piece_bytes) : nullptr;   // op(A) rows, then op(B) columns
+    const unsigned long long *gdone = pdl ? done : nullptr;
+    const unsigned long long expect = st.launched;
+
     cudaLaunchAttribute pdl_attr[1];
     pdl_attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     pdl_attr[0].val.programmaticStreamSerializationAllowed = 1;
-    static std::atomic<uint64_t> carve{0};
-    if (pdl && device_setup_needed(carve)) {   // the GEMM's shared-memory configuration, so both fit on an SM
-        GB_CUDA_TRY(cudaFuncSetAttribute(split_vec_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-        GB_CUDA_TRY(cudaFuncSetAttribute(split_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-        device_setup_done(carve);
+    const bool vec = g.lda % 4 == 0 && g.ldb % 4 == 0 && (uintptr_t)g.A % 16 == 0 && (uintptr_t)g.B % 16 == 0;
+
+    if (f16) {   // largest |x| of every row of op(A) and column of op(B)
+        GB_CUDA_TRY(cudaMemsetAsync(bits, 0, (size_t)(g.M + g.N) * 4, g.stream));
+        ScanArgs sc;
+        memset(&sc, 0, sizeof(sc));
+        sc.K = g.K;
+        sc.vec = vec ? 1 : 0;
+        const int64_t tk = ceil_div(g.K, 64);
+        sc.op[0] = ScanOp{(const float *)g.A, g.lda, g.M, tk, ceil_div(g.M, 64) * tk, g.ta ? 1 : 0, bits};
+        sc.op[1] = ScanOp{(const float *)g.B, g.ldb, g.N, tk, ceil_div(g.N, 64) * tk, g.tb ? 0 : 1, bits + g.M};
+        const int64_t blocks = sc.op[0].tiles + sc.op[1].tiles;
+        if (blocks > 0x7fffffff) return set_status(GB_ERR_UNSUPPORTED, "fp16x3: operands too large");
+        maxbits_kernel<<<(unsigned)blocks, 256, 0, g.stream>>>(sc);
+        GB_LAUNCH_CHECK("fp16x3 scan");
     }
-    int *err = error_word();
-    if (!err) return set_status(GB_ERR_OOM, "bf16x3: no device error word");
 
     // split: op(A)(m, k) = ta ? A[k*lda + m] : A[m*lda + k]
     //        op(B)^T(n, k) = op(B)(k, n) = tb ? B[n*ldb + k] : B[k*ldb + n]
-    const bool vec = g.lda % 4 == 0 && g.ldb % 4 == 0 && (uintptr_t)g.A % 16 == 0 && (uintptr_t)g.B % 16 == 0;
     if (vec) {
         SplitArgs sa;
         memset(&sa, 0, sizeof(sa));
-        sa.K = g.K; sa.kp = kp; sa.np = np;
+        sa.K = g.K; sa.kp = kp; sa.np = np; sa.done = gdone; sa.expect = expect;
         sa.op[0] = SplitOp{(const float *)g.A, g.lda, g.M, kp / 64, ceil_div(g.M, 64) * (kp / 64), g.ta ? 1 : 0,
-                           {ap[0], ap[1], np == 3 ? ap[2] : nullptr}};
+                           {ap[0], ap[1], np == 3 ? ap[2] : nullptr}, bits};
         sa.op[1] = SplitOp{(const float *)g.B, g.ldb, g.N, kp / 64, ceil_div(g.N, 64) * (kp / 64), g.tb ? 0 : 1,
-                           {bp[0], bp[1], np == 3 ? bp[2] : nullptr}};
+                           {bp[0], bp[1], np == 3 ? bp[2] : nullptr}, f16 ? bits + g.M : nullptr};
         const int64_t blocks = sa.op[0].tiles + sa.op[1].tiles;
         if (blocks > 0x7fffffff) return set_status(GB_ERR_UNSUPPORTED, "bf16x3: operands too large");
         cudaLaunchConfig_t cfg = {};
@@ -1109,7 +1473,8 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
         cfg.stream = g.stream;
         cfg.attrs = pdl_attr;
         cfg.numAttrs = pdl ? 1 : 0;
-        GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_vec_kernel, sa));
+        if (f16) GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_vec_kernel<true>, sa));
+        else GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_vec_kernel<false>, sa));
         GB_LAUNCH_CHECK("bf16x3 split");
     } else {
         dim3 sgA((unsigned)ceil_div(kp, 32), (unsigned)ceil_div(g.M, 32));
@@ -1121,29 +1486,59 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb) {
         cfg.stream = g.stream;
         cfg.attrs = pdl_attr;
         cfg.numAttrs = pdl ? 1 : 0;
-        GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_kernel, (const float *)g.A, g.lda, g.ta ? 1 : 0, g.M, g.K, kp,
-                                       ap[0], ap[1], np == 3 ? ap[2] : (__nv_bfloat16 *)nullptr));
+        const unsigned *mb = bits;
+        if (f16)
+            GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_kernel<true>, (const float *)g.A, g.lda, g.ta ? 1 : 0, g.M, g.K,
+                                           kp, ap[0], ap[1], (uint16_t *)nullptr, mb, gdone, expect));
+        else
+            GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_kernel<false>, (const float *)g.A, g.lda, g.ta ? 1 : 0, g.M,
+                                           g.K, kp, ap[0], ap[1], np == 3 ? ap[2] : (uint16_t *)nullptr, mb, gdone,
+                                           expect));
         GB_LAUNCH_CHECK("bf16x3 split A");
-        split_kernel<<<sgB, 256, 0, g.stream>>>((const float *)g.B, g.ldb, g.tb ? 0 : 1, g.N, g.K, kp, bp[0], bp[1],
-                                                np == 3 ? bp[2] : nullptr);
+        const unsigned *mbB = f16 ? bits + g.M : nullptr;
+        if (f16)
+            split_kernel<true><<<sgB, 256, 0, g.stream>>>((const float *)g.B, g.ldb, g.tb ? 0 : 1, g.N, g.K, kp, bp[0],
+                                                          bp[1], nullptr, mbB, nullptr, 0ull);
+        else
+            split_kernel<false><<<sgB, 256, 0, g.stream>>>((const float *)g.B, g.ldb, g.tb ? 0 : 1, g.N, g.K, kp,
+                                                           bp[0], bp[1], np == 3 ? bp[2] : nullptr, nullptr, nullptr,
+                                                           0ull);
         GB_LAUNCH_CHECK("bf16x3 split B");
     }
 
-    const int bn = (np == 3 || fold_kb > 0) ? 128 : 256;
+    const int bn = np == 3 ? 128 : 256;
     PieceMaps maps;
     memset(&maps, 0, sizeof(maps));
     bool okm = true;
-    for (int i = 0; i < np; i++) {
+    for (int i = 0; i < np; i++) {   // 2-byte elements, copied as they are (BF16 or FP16)
         okm = okm && make_tmap_bf16(&maps.a[i], ap[i], kp, g.M, kp * 2, BK, BM, 64);
         okm = okm && make_tmap_bf16(&maps.b[i], bp[i], kp, g.N, kp * 2, BK, bn, 64);
         okm = okm && make_tmap_bf16(&maps.bh[i], bp[i], kp, g.N, kp * 2, BK, bn / 2, 64);
     }
     if (!okm) return set_status(GB_ERR_CUDA, "bf16x3: cuTensorMapEncodeTiled failed");
-    if (np == 3)
-        return fold_kb > 0 ? two_pass_launch<3, 128, true>(g, maps, kp, err, fold_kb, nullptr, nullptr)
-                           : two_pass_launch<3, 128, false>(g, maps, kp, err, 0, nullptr, nullptr);
-    return fold_kb > 0 ? two_pass_launch<2, 128, true>(g, maps, kp, err, fold_kb, nullptr, nullptr)
-                       : two_pass_launch<2, 256, false>(g, maps, kp, err, 0, sk_part, sk_cnt);
+    EpiParams p;
+    memset(&p, 0, sizeof(p));
+    p.C = (float *)g.C; p.M = g.M; p.N = g.N; p.ldc = g.ldc;
+    p.alpha = (float)g.alpha; p.beta = (float)g.beta; p.semantics = g.semantics;
+    p.err = err;
+    p.chunk_kb = fold_kb;
+    p.done = done;
+    if (f16) {
+        p.rowbits = bits; p.colbits = bits + g.M;
+        p.A = (const float *)g.A; p.B = (const float *)g.B;
+        p.lda = g.lda; p.ldb = g.ldb; p.K = g.K;
+        p.ta = g.ta ? 1 : 0; p.tb = g.tb ? 1 : 0;
+    }
+    int grid = 0;
+    gb_status s = f16 ? gemm_launch<true>(g, np, fold_kb, maps, kp, p, &grid)
+                      : gemm_launch<false>(g, np, fold_kb, maps, kp, p, &grid);
+    if (s != GB_OK) return s;
+    st.launched += (unsigned long long)grid;
+    st.valid = done != nullptr;
+    st.c_lo = clo;
+    st.c_hi = chi;
+    st.parity = parity;
+    return ok();
 }
 
 }  // namespace gb

@@ -18,7 +18,8 @@
 // every partial sum of a 1024-long K chunk is an integer of magnitude at most
 // 1024*128^2 = 2^24: exact.  Eight bits per slice (balanced digits keep the
 // products within 2^14 although they carry a full byte) give FP64-level
-// results with 7 slices, 28 slice products.  Chunk sums are added exactly in int32 registers (up to 127 chunks),
+// results with 7 slices (28 slice products) and no worse than native FP64
+// with 8 (36, the default).  Chunk sums are added exactly in int32 registers (up to 127 chunks),
 // and FP64 appears only in the per-pair scaled sum kept in TMEM and in the
 // final 2^(e_i+f_j), alpha, beta epilogue.  (sm_103a has no kind::i8 MMA, so
 // the INT8 products are carried in BF16; products and sums stay exact.)
@@ -47,10 +48,11 @@ int ozaki_pick_slices(double target_err, int64_t K) {
     // Each input is truncated at 2^(1-8s) of its row (column) maximum, so a
     // product term errs by at most ~2^(2-8s) |a||b|; FP64's own rounding is
     // u = 2^-53 per term, and both grow like sqrt(K) over a dot product.
-    // target_err 0 (FP64-equivalent): 2^(2-8s) <= u/2, s = 7 (measured on
-    // 8192^3 with entries u*2^e, e in [-20, 20]: 7.56e-18 vs native 7.51e-18).
+    // target_err 0 (FP64-equivalent): no worse than native FP64, s = 8
+    // (measured on 8192^3 with entries u*2^e, e in [-20, 20]: 8.3e-19 against
+    // native 7.5e-18; s = 7 measured 7.56e-18, a little worse than native).
     // A target: the smallest s with 2^(2-8s) sqrt(K) * 4 <= target.
-    if (target_err <= 0) return 7;
+    if (target_err <= 0) return 8;
     double logk = 0;
     for (int64_t k = K; k > 1; k >>= 1) logk += 0.5;
     for (int s = 2; s <= 9; s++)

@@ -22,8 +22,9 @@ INCLUDE_DIR = os.path.join(_REPO, "include")
 # gb_status
 OK, ERR_INVALID_ARG, ERR_UNSUPPORTED, ERR_OOM, ERR_DEVICE_TIMEOUT, ERR_CUDA, ERR_NO_DEVICE = range(7)
 # gb_algo
-ALGO_AUTO, ALGO_ORDERED, ALGO_SIMT, ALGO_DMMA, ALGO_BF16X3, ALGO_OZAKI, ALGO_SKINNY, ALGO_BF16X6 = range(8)
-ALGO_NAMES = {0: "auto", 1: "ordered", 2: "simt", 3: "dmma", 4: "bf16x3", 5: "ozaki", 6: "skinny", 7: "bf16x6"}
+ALGO_AUTO, ALGO_ORDERED, ALGO_SIMT, ALGO_DMMA, ALGO_BF16X3, ALGO_OZAKI, ALGO_SKINNY, ALGO_BF16X6, ALGO_FP16X3 = range(9)
+ALGO_NAMES = {0: "auto", 1: "ordered", 2: "simt", 3: "dmma", 4: "bf16x3", 5: "ozaki", 6: "skinny", 7: "bf16x6",
+              8: "fp16x3"}
 # gb_semantics
 SEM_BLAS, SEM_SCALAR_BETA, SEM_ACCUM_SCALAR_BETA = range(3)
 # gb_stencil_order

@@ -96,8 +96,12 @@ typedef enum gb_algo {
     GB_ALGO_BF16X3 = 4,   /* SGEMM as hi*hi+hi*lo+lo*hi BF16 on tcgen05, FP32 acc */
     GB_ALGO_OZAKI = 5,    /* DGEMM from exact integer slices on tensor cores    */
     GB_ALGO_SKINNY = 6,   /* tiny M (shortA) / tiny N (thinB) streaming kernels */
-    GB_ALGO_BF16X6 = 7    /* SGEMM from 3 BF16 pieces (6 products) on tcgen05:
+    GB_ALGO_BF16X6 = 7,   /* SGEMM from 3 BF16 pieces (6 products) on tcgen05:
                              FP32-level error at half the BF16X3 rate        */
+    GB_ALGO_FP16X3 = 8    /* SGEMM from 2 FP16 pieces of power-of-two scaled
+                             rows of op(A) / columns of op(B) (3 products,
+                             folded accumulation) on tcgen05: FP32-level
+                             error                                            */
 } gb_algo;
 
 typedef enum gb_semantics {
@@ -123,8 +127,8 @@ typedef struct gb_gemm_opts {
                               instead of op(A) (sgemm V1.3.x)                  */
     int32_t ozaki_slices;  /* OZAKI: 8-bit (balanced) slices per operand
                               (2..9), 0 -> the fewest meeting target_err      */
-    double  target_err;    /* OZAKI: normwise error target, 0 -> FP64 level
-                              (7 slices)                                      */
+    double  target_err;    /* OZAKI: normwise error target, 0 -> no worse
+                              than native FP64 (8 slices)                     */
     int32_t reserved[4];
 } gb_gemm_opts;
 
@@ -137,7 +141,9 @@ void gb_gemm_opts_init(gb_gemm_opts *opts);
  * (K == 0 still applies beta).  opts may be NULL.
  * Stream-ordered: work queued after a call sees its C.  Two BF16X3 / BF16X6
  * calls back to back on one stream may overlap the second's operand split
- * with the first's GEMM (never its GEMM with the first's).  FP64 through the
+ * with the first's GEMM (never its GEMM with the first's) when the second's
+ * A and B do not overlap the first's C; work queued on the stream between
+ * the two calls is waited for before the split reads A and B.  FP64 through the
  * digit forms (OZAKI, FP64 SKINNY): an output whose row of op(A) or column of
  * op(B) holds an Inf or a NaN is computed as a plain FP64 dot product, so
  * they propagate as in IEEE arithmetic. */

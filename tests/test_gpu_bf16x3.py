@@ -10,6 +10,8 @@
 """
 
 SPLIT_ERR = 3 * 2.0 ** -17
+# FP16X3 error at K = 4096 relative to plain FFMA on the same inputs (at most)
+FP16X3_VS_SIMT = 1.0
 import numpy as np
 import pytest
 
@@ -232,35 +234,6 @@ def test_bf16x6_error_tracks_simt(torch):
 
 
 @pytest.mark.parametrize("mode", MODES)
-@pytest.mark.parametrize("M,N,K", [(4096, 4096, 320), (2048, 4096, 96), (4000, 3900, 1000)])
-def test_bf16x3_stream_k_tail_exact(torch, mode, M, N, K):
-    """Tile counts that leave a partial last wave, with the stream-K tail
-    switched on (GB_BF16X3_SK=1): the tail tiles are split in K over two CTAs
-    and summed by the second finisher.  Small integers keep every partial sum
-    exact, so the result must equal the exact product."""
-    import os
-    import gbblas
-    os.environ["GB_BF16X3_SK"] = "1"
-    ta, tb = mode
-    ar, ac = op_shape(ta, M, K)
-    br, bc = op_shape(tb, K, N)
-    A, B = _ints(ar, ac, 31), _ints(br, bc, 32)
-    C0 = _ints(M, N, 33)
-    opA = A.T if ta == "T" else A
-    opB = B.T if tb == "T" else B
-    want = (opA.astype(np.float64) @ opB.astype(np.float64) - 2.0 * C0).astype(np.float32)
-    try:
-        for _ in range(2):   # twice: the part counters must be back at zero
-            dC = dev(C0)
-            gbblas.sgemm(ta, tb, M, N, K, 1.0, dev(A), ac, dev(B), bc, -2.0, dC, N, algo=gbblas.ALGO_BF16X3)
-            got = host(dC)
-            bad = np.argwhere(got != want)
-            assert bad.size == 0, (mode, bad[:5])
-    finally:
-        os.environ.pop("GB_BF16X3_SK", None)
-
-
-@pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("M,N,K", [(4096, 4096, 96), (1152, 4352, 64), (300, 700, 128)])
 def test_bf16x3_half_tile_tail_exact(torch, mode, M, N, K):
     """A last wave at most half full runs as 128-column half tiles (N = 128
@@ -334,3 +307,269 @@ def test_back_to_back_calls_of_mixed_sizes(torch):
         finally:
             os.environ.pop("GB_BF16X3_PDL", None)
     assert outs[0] == outs[1]
+
+
+def _pdl_both(fn):
+    """fn() run with the split passes allowed beside the previous GEMM and
+    with every launch in plain stream order (GB_BF16X3_PDL=0)."""
+    import os
+    outs = []
+    for pdl in ("1", "0"):
+        os.environ["GB_BF16X3_PDL"] = pdl
+        try:
+            outs.append(fn())
+        finally:
+            os.environ.pop("GB_BF16X3_PDL", None)
+    return outs
+
+
+def test_back_to_back_chain_reads_previous_result(torch):
+    """C1 = A B, then C2 = C1 D, then C3 = E C2 with no host synchronisation:
+    each call's operands are the previous call's result, so no split may read
+    them before the GEMM that writes them has finished.  Same bits as the
+    calls in plain order."""
+    import gbblas
+    M = N = K = 1536
+    A = dev(oracle.fill(M, K, 901, dtype=np.float32))
+    D = dev(oracle.fill(K, N, 902, dtype=np.float32))
+    E = dev(oracle.fill(M, K, 903, dtype=np.float32))
+
+    def run():
+        C1 = dev(np.zeros((M, N), np.float32))
+        C2 = dev(np.zeros((M, N), np.float32))
+        C3 = dev(np.zeros((M, N), np.float32))
+        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, D, N, 0.0, C1, N, algo=gbblas.ALGO_BF16X3)
+        gbblas.sgemm("N", "N", M, N, K, 0.5, C1, N, D, N, 0.0, C2, N, algo=gbblas.ALGO_BF16X3)
+        gbblas.sgemm("N", "T", M, N, K, 0.25, E, K, C2, N, 0.0, C3, N, algo=gbblas.ALGO_BF16X3)
+        return host(C3).tobytes()
+
+    a, b = _pdl_both(run)
+    assert a == b
+
+
+def test_back_to_back_alternating_forms(torch):
+    """BF16X3, BF16X6 and FP16X3 calls alternating on one stream with no host
+    synchronisation: every two-pass call places its pieces in the same two
+    workspace halves, whatever the form of the previous call.  Same bits as
+    the calls in plain order."""
+    import gbblas
+    shapes = [(1536, 1280, 1024), (640, 768, 512), (2048, 1024, 768)]
+    ops = [(dev(oracle.fill(M, K, 920 + i, dtype=np.float32)), dev(oracle.fill(K, N, 930 + i, dtype=np.float32)))
+           for i, (M, N, K) in enumerate(shapes)]
+    algos = [gbblas.ALGO_BF16X3, gbblas.ALGO_BF16X6, gbblas.ALGO_FP16X3]
+
+    def run():
+        Cs = [dev(oracle.fill(M, N, 940 + i, dtype=np.float32)) for i, (M, N, K) in enumerate(shapes)]
+        for rep in range(3):
+            for i, (M, N, K) in enumerate(shapes):
+                A, B = ops[i]
+                gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B, N, 1.0, Cs[i], N, algo=algos[(i + rep) % 3])
+        return [host(c).tobytes() for c in Cs]
+
+    a, b = _pdl_both(run)
+    assert a == b
+
+
+def test_back_to_back_with_caller_work_in_between(torch):
+    """A torch kernel on the same stream rewrites the next call's B between
+    two calls: the next call's split starts only after that kernel and reads
+    the new B.  Same bits as the calls in plain order."""
+    import gbblas
+    tc = torch
+    M = N = K = 1024
+    A = dev(oracle.fill(M, K, 950, dtype=np.float32))
+    B0 = dev(oracle.fill(K, N, 951, dtype=np.float32))
+    B1src = dev(oracle.fill(K, N, 952, dtype=np.float32))
+
+    def run():
+        B1 = tc.zeros_like(B1src)
+        C0 = dev(np.zeros((M, N), np.float32))
+        C1 = dev(np.zeros((M, N), np.float32))
+        tc.cuda.synchronize()
+        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B0, N, 0.0, C0, N, algo=gbblas.ALGO_BF16X3)
+        B1.copy_(B1src)          # torch's current stream is the legacy default stream gbblas uses
+        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B1, N, 0.0, C1, N, algo=gbblas.ALGO_BF16X3)
+        return host(C0).tobytes() + host(C1).tobytes()
+
+    a, b = _pdl_both(run)
+    assert a == b
+
+
+# ---------------------------------------------------------------- FP16X3
+# Two FP16 pieces (11 + 11 significand bits) of every value after its row of
+# op(A) / column of op(B) is scaled by a power of two that puts the line's
+# largest magnitude in [2^14, 2^15); the three products hi*hi + hi*lo + lo*hi,
+# accumulated in chunks of 128 k that are summed in registers.  The dropped
+# lo*lo term and the residue are ~2^-22 of a product, so the error is that of
+# FP32 accumulation.
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (130, 300, 70), (7, 9, 5), (1030, 2050, 96), (2048, 4096, 64)])
+def test_fp16x3_exact_on_integers(torch, mode, M, N, K):
+    import gbblas
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A, B = _ints(ar, ac, 21), _ints(br, bc, 22)
+    C0 = _ints(M, N, 23)
+    opA = A.T if ta == "T" else A
+    opB = B.T if tb == "T" else B
+    want = (2.0 * (opA.astype(np.float64) @ opB.astype(np.float64)) + 1.0 * C0).astype(np.float32)
+    dC = dev(C0)
+    gbblas.sgemm(ta, tb, M, N, K, 2.0, dev(A), ac, dev(B), bc, 1.0, dC, N, algo=gbblas.ALGO_FP16X3)
+    got = host(dC)
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (mode, bad[:5])
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_fp16x3_exact_across_exponent_range(torch, mode):
+    """Rows of op(A) and columns of op(B) scaled by powers of two from 2^-146
+    (FP32 subnormals) to 2^60: each line gets its own scale, so small-integer
+    products stay exact and land at the right exponent."""
+    import gbblas
+    ta, tb = mode
+    M, N, K = 160, 144, 96
+    rng = np.random.default_rng(24)
+    ea = rng.choice([-146, -100, -60, -20, 0, 30, 60], size=M)
+    fb = rng.choice([-60, -20, 0, 10, 50], size=N)
+    opA = (rng.integers(-8, 9, size=(M, K)) * np.exp2(ea)[:, None]).astype(np.float64)
+    opB = (rng.integers(-8, 9, size=(K, N)) * np.exp2(fb)[None, :]).astype(np.float64)
+    want = (opA @ opB).astype(np.float32)          # every sum exact (|int sum| < 2^13)
+    assert np.array_equal(opA.astype(np.float32).astype(np.float64), opA)
+    A = np.ascontiguousarray(opA.T if ta == "T" else opA).astype(np.float32)
+    B = np.ascontiguousarray(opB.T if tb == "T" else opB).astype(np.float32)
+    dC = dev(np.zeros((M, N), np.float32))
+    gbblas.sgemm(ta, tb, M, N, K, 1.0, dev(A), A.shape[1], dev(B), B.shape[1], 0.0, dC, N,
+                 algo=gbblas.ALGO_FP16X3)
+    got = host(dC)
+    bad = np.argwhere(got != want)
+    assert bad.size == 0, (mode, bad[:5], got[tuple(bad[0])] if bad.size else None)
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("M,N,K,pad", [(384, 512, 1040, 16), (333, 257, 515, 3), (1, 1, 1, 0), (129, 1000, 4096, 8),
+                                       (64, 64, 3, 1)])
+def test_fp16x3_normwise_fp32_level(torch, mode, M, N, K, pad):
+    import gbblas
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A = oracle.fill(ar, ac, 71, dtype=np.float32, ld=ac + pad)
+    B = oracle.fill(br, bc, 72, dtype=np.float32, ld=bc + pad)
+    C0 = oracle.fill(M, N, 73, dtype=np.float32, ld=N + pad)
+    dC = dev(C0)
+    gbblas.sgemm(ta, tb, M, N, K, 1.5, dev(A), ac + pad, dev(B), bc + pad, -0.5, dC, N + pad,
+                 algo=gbblas.ALGO_FP16X3)
+    got = host(dC)
+    rows = np.arange(0, M, max(1, M // 97))
+    cols = np.arange(0, N, max(1, N // 97))
+    err, _ = oracle.normwise_error(got, ta, tb, M, N, K, 1.5, A, ac + pad, B, bc + pad, -0.5, C0, N + pad,
+                                   rows, cols)
+    assert err <= (2 * K + 4) * 2.0 ** -24, err
+    if pad:
+        assert np.array_equal(got[:, N:], C0[:, N:])
+
+
+def test_fp16x3_error_tracks_simt(torch):
+    """At K = 4096 the FP16 three-product result is as accurate as plain
+    FFMA, and an order of magnitude better than BF16X3."""
+    import gbblas
+    M = N = 512
+    K = 4096
+    A = oracle.fill(M, K, 81, dtype=np.float32)
+    B = oracle.fill(K, N, 82, dtype=np.float32)
+    C0 = np.zeros((M, N), np.float32)
+    rows = np.arange(0, M, 8)
+    cols = np.arange(0, N, 8)
+    errs = {}
+    for name, algo in (("simt", gbblas.ALGO_SIMT), ("x3", gbblas.ALGO_BF16X3), ("f16", gbblas.ALGO_FP16X3)):
+        dC = dev(C0)
+        gbblas.sgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=algo)
+        errs[name], _ = oracle.normwise_error(host(dC), "N", "N", M, N, K, 1.0, A, K, B, N, 0.0, C0, N, rows, cols)
+    assert errs["f16"] <= errs["simt"] * FP16X3_VS_SIMT, errs
+    assert errs["f16"] * 4 <= errs["x3"], errs
+
+
+@pytest.mark.parametrize("mode", ["NN", "TT"])
+def test_fp16x3_inf_nan_propagate(torch, mode):
+    """A row of op(A) holding +Inf, one holding NaN and a column of op(B)
+    holding -Inf: those outputs are plain FP32 dot products, so NaN and
+    +-Inf appear exactly where IEEE arithmetic puts them; the rest is
+    unaffected."""
+    import gbblas
+    ta, tb = mode
+    M, N, K = 300, 280, 200
+    opA = oracle.fill(M, K, 91, dtype=np.float32)
+    opB = oracle.fill(K, N, 92, dtype=np.float32)
+    opA[3, 17] = np.inf
+    opA[7, 40] = np.nan
+    opB[55, 5] = -np.inf
+    opB[:, 9] = 0.0
+    opB[60, 9] = np.inf      # column 9: Inf times the zeros of op(A)'s row 11
+    opA[11, :] = 0.0
+    opA[11, 60] = 1.0
+    A = np.ascontiguousarray(opA.T if ta == "T" else opA)
+    B = np.ascontiguousarray(opB.T if tb == "T" else opB)
+    dC = dev(np.zeros((M, N), np.float32))
+    gbblas.sgemm(ta, tb, M, N, K, 1.0, dev(A), A.shape[1], dev(B), B.shape[1], 0.0, dC, N,
+                 algo=gbblas.ALGO_FP16X3)
+    got = host(dC)
+    a64, b64 = opA.astype(np.float64), opB.astype(np.float64)
+    want = np.empty((M, N))
+    with np.errstate(invalid="ignore", over="ignore"):
+        for i in range(M):   # every product formed (a BLAS may skip zeros and lose Inf * 0 = NaN)
+            want[i] = (a64[i][:, None] * b64).sum(axis=0)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    assert np.array_equal(np.isposinf(got), np.isposinf(want))
+    assert np.array_equal(np.isneginf(got), np.isneginf(want))
+    fin = np.isfinite(want)
+    assert np.max(np.abs(got[fin] - want[fin])) <= 2 * K * 2.0 ** -24 * np.max(np.abs(want[fin]))
+
+
+@pytest.mark.parametrize("chunk", ["0", "2", "16"])
+def test_fp16x3_accumulation_chunks(torch, chunk):
+    """Other accumulator chunks (0: one accumulator over all of K, no
+    folding): exact on integers, within 2*K*u32 on U[-1,1]."""
+    import os
+    import gbblas
+    os.environ["GB_FP16X3_FOLD"] = chunk
+    try:
+        M, N, K = 700, 520, 2000
+        A, B = _ints(M, K, 25), _ints(K, N, 26)
+        want = (A.astype(np.float64) @ B.astype(np.float64)).astype(np.float32)
+        dC = dev(np.zeros((M, N), np.float32))
+        gbblas.sgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=gbblas.ALGO_FP16X3)
+        assert np.array_equal(host(dC), want)
+        A = oracle.fill(M, K, 27, dtype=np.float32)
+        B = oracle.fill(N, K, 28, dtype=np.float32)
+        dC = dev(np.zeros((M, N), np.float32))
+        gbblas.sgemm("N", "T", M, N, K, 1.0, dev(A), K, dev(B), K, 0.0, dC, N, algo=gbblas.ALGO_FP16X3)
+        err, _ = oracle.normwise_error(host(dC), "N", "T", M, N, K, 1.0, A, K, B, K, 0.0, None, N,
+                                       np.arange(0, M, 7), np.arange(0, N, 7))
+        assert err <= 2 * K * 2.0 ** -24, err
+    finally:
+        os.environ.pop("GB_FP16X3_FOLD", None)
+
+
+def test_bf16x3_folded_wide_form_exact(torch):
+    """BF16X3 through the folding form with eight epilogue warps
+    (GB_BF16X3_FOLD): exact on integers in all four modes."""
+    import os
+    import gbblas
+    os.environ["GB_BF16X3_FOLD"] = "4"
+    try:
+        for mode in MODES:
+            ta, tb = mode
+            M, N, K = 1030, 700, 600
+            ar, ac = op_shape(ta, M, K)
+            br, bc = op_shape(tb, K, N)
+            A, B, C0 = _ints(ar, ac, 31), _ints(br, bc, 32), _ints(M, N, 33)
+            opA = A.T if ta == "T" else A
+            opB = B.T if tb == "T" else B
+            want = (opA.astype(np.float64) @ opB.astype(np.float64) - 0.5 * C0).astype(np.float32)
+            dC = dev(C0)
+            gbblas.sgemm(ta, tb, M, N, K, 1.0, dev(A), ac, dev(B), bc, -0.5, dC, N, algo=gbblas.ALGO_BF16X3)
+            assert np.array_equal(host(dC), want), mode
+    finally:
+        os.environ.pop("GB_BF16X3_FOLD", None)

@@ -30,7 +30,7 @@ def test_bounded_wait_gives_up_and_the_device_stays_usable(torch):
     M, N, K = 512, 384, 256
     A = rng.integers(-8, 9, size=(M, K)).astype(np.float32)
     B = rng.integers(-8, 9, size=(K, N)).astype(np.float32)
-    for algo in (gbblas.ALGO_BF16X3, gbblas.ALGO_BF16X6):
+    for algo in (gbblas.ALGO_BF16X3, gbblas.ALGO_BF16X6, gbblas.ALGO_FP16X3):
         dC = dev(np.zeros((M, N), np.float32))
         gbblas.sgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=algo)
         assert L.gb_sync(None) == gbblas.OK

@@ -152,8 +152,9 @@ def test_sgemm_ordered_scalar_beta_bit_exact(torch, mode):
 
 
 @pytest.mark.parametrize("mode", MODES)
-def test_sgemm_simt_4096_ld4112_normwise(torch, mode):
-    """SGEMM BLAS semantics, alpha=1.5 beta=-0.5, padded leading dimensions."""
+def test_sgemm_simt_384x320x1040_padded_ld_normwise(torch, mode):
+    """SGEMM BLAS semantics, alpha=1.5 beta=-0.5, leading dimensions padded by
+    16 (the 4096^3 ld-4112 configuration itself: test_gpu_configs_full.py)."""
     import gbblas
     ta, tb = mode
     M, N, K = 384, 320, 1040
