@@ -284,8 +284,9 @@ def cpu_sgemm_sample(max_seconds=10.0):
         if secs * 3 > max_seconds or rows >= 256:
             break
         rows *= 2
-    return (flops / secs / 1e12, nt, "%d of %d rows of C per mode, 4 modes, K=%d: oracle port of the reference "
-            "host loop sgemm_demo.c:214-242, gcc -O2 -fopenmp, %d threads" % (rows, M, K, nt))
+    return (flops / secs / 1e12, nt, "sampled rate (not the full problem): %d of %d rows of C per mode, 4 modes, "
+            "K=%d: oracle port of the reference host loop sgemm_demo.c:214-242, gcc -O2 -fopenmp, %d threads"
+            % (rows, M, K, nt))
 
 
 def cpu_dgemm_sample(max_seconds=10.0):
@@ -305,8 +306,9 @@ def cpu_dgemm_sample(max_seconds=10.0):
         if secs * 3 > max_seconds or rows >= 64:
             break
         rows *= 2
-    return (2.0 * rows * n * n / secs / 1e12, nt, "%d of 8192 rows of C, NN, K=8192: oracle port of "
-            "dgemm_demo.c:233-252, %d threads (rate extrapolated to the full problem)" % (rows, nt))
+    return (2.0 * rows * n * n / secs / 1e12, nt, "sampled rate (not the full problem): %d of 8192 rows of C, NN, "
+            "K=8192: oracle port of dgemm_demo.c:233-252, %d threads (rate extrapolated to the full problem)"
+            % (rows, nt))
 
 
 def cpu_bw_sample(kind, bits, max_seconds=8.0):

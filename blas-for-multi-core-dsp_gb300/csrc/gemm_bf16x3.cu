@@ -471,17 +471,18 @@ constexpr int BM = 128, BK = 32, STAGES = 4, GROUP_M = 8;
 constexpr int A_TILE = BM * BK * 2;            // 8 KB
 constexpr int EPI_BYTES = 4 * 32 * 33 * 4;     // four warps' 32 x 32 staging, padded
 
-// EW epilogue warps: 4 (one per TMEM lane quarter, all BN columns, C staged
-// through shared memory) or 8 (two per lane quarter, 128 columns each: the
-// wide folding form, C written from registers).
+// EW epilogue warps: 4 (one per TMEM lane quarter, all BN columns) or 8 (two
+// per lane quarter, 128 columns each: the wide folding form); both stage C
+// through shared memory so that loads and stores of C are coalesced.
 template <int NP, int BN, int EW>
 struct TwoPass {
     static constexpr int B_TILE = BN * BK * 2;
     static constexpr int STAGE_BYTES = NP * A_TILE + NP * B_TILE;
     static constexpr int NT = 64 + 32 * EW;
-    static constexpr int EPI = EW == 4 ? EPI_BYTES : 0;
-    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI + 1024 /*align*/ + 256 /*barriers*/ +
-                                      EW * 32 * 4 /*row scales*/;
+    // C staging: 4 warps x 32 x 32 (padded 33), or 8 warps x 32 x 16 (padded 17)
+    static constexpr int EPI = EW == 4 ? EPI_BYTES : 8 * 32 * 17 * 4;
+    static constexpr int SCALES = EW == 8 ? 8 * (128 + 32) * 4 : 0;   // FP16 column and row scales per warp
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + EPI + 1024 /*align*/ + 256 /*barriers*/ + SCALES;
 };
 
 // tensor maps of the A and B pieces (hi, lo[, lo2])
@@ -582,7 +583,8 @@ __device__ __noinline__ void store_recomputed(const EpiParams &p, int64_t row, i
 //    at +0, the rest at +128).
 //  - BN = 256, 8 epilogue warps (FP16X3, BF16X3 folded): all products in one
 //    accumulator of 256 columns, two chunk buffers; each epilogue warp keeps
-//    the totals of 32 rows x 128 columns and writes C from registers.
+//    the totals of 32 rows x 128 columns and writes C through shared memory
+//    16 columns at a time.
 // The MMAs of chunk c+1 overlap the fold of chunk c.
 // F16: FP16 pieces of scaled lines (FP16X3), the epilogue applies the scales.
 template <int NP, int BN, bool FOLD, bool F16, int EW>
@@ -594,6 +596,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
     constexpr bool SEP = FOLD && EW == 4;   // hi*hi apart from the cross products
     static_assert(!SEP || BN == 128, "the separated folding form keeps a 128-column total per thread");
     static_assert(EW == 4 || (FOLD && BN == 256), "eight epilogue warps: the wide folding form");
+    static_assert(!F16 || EW == 8, "FP16 pieces: the wide folding form");
     constexpr int B_TILE = CF::B_TILE, STAGE_BYTES = CF::STAGE_BYTES;
     constexpr uint32_t ACC_COLS = SEP ? 256 : BN, TMEM_COLS = 2 * ACC_COLS;
     extern __shared__ uint8_t smem_raw[];
@@ -604,7 +607,8 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
     uint64_t *acc_full = empty + STAGES;     // [2]
     uint64_t *acc_empty = acc_full + 2;      // [2]
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
-    int *row_scale = reinterpret_cast<int *>(smem + STAGES * STAGE_BYTES + CF::EPI + 256);   // [4][32]
+    int *col_scale = reinterpret_cast<int *>(smem + STAGES * STAGE_BYTES + CF::EPI + 256);   // [8][128]
+    int *row_scale = col_scale + 8 * 128;                                                     // [8][32]
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int num_tiles = p.tiles_m * p.tiles_n;
@@ -714,7 +718,6 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
     } else if constexpr (EW == 4) {   // epilogue: warps 2..5 own TMEM lane quarters (warp % 4)
         const int q = warp % 4;
         float *stage = epi + q * 32 * 33;
-        int *rs = row_scale + q * 32;
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
         int ch = 0;
         float total[FOLD ? BN : 1];
@@ -726,10 +729,6 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
             const int64_t row0 = (int64_t)tm * BM + q * 32;
             const int64_t n0 = (int64_t)tn * BN + (half > 0 ? BN / 2 : 0);
             const int ncols = half < 0 ? BN : BN / 2;
-            if (F16) {   // the scale of each of the warp's 32 rows, for the whole tile
-                rs[lane] = row0 + lane < p.M ? f16_line_scale(p.rowbits[row0 + lane]) : 0;
-                __syncwarp();
-            }
             uint32_t accb = 0;
             if (FOLD) {
 #pragma unroll
@@ -760,7 +759,6 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 ptx::tc_fence_after();
                 accb = (uint32_t)(b * ACC_COLS);
             }
-            bool nf = false;   // an output of this thread's columns waits for the recompute pass
 #pragma unroll
             for (int c = 0; c < BN; c += 32) {
                 if (c >= ncols) break;
@@ -780,37 +778,18 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 const int64_t col = n0 + c + lane;
                 if (col < p.N) {
                     const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
-                    const int cs = F16 ? f16_line_scale(p.colbits[col]) : 0;
                     if (!reads_c(p)) {
                         const float add = p.semantics == GB_SEM_SCALAR_BETA ? p.beta : 0.f;
-                        for (int rr = 0; rr < rows; rr++) {
-                            float x = stage[rr * 33 + lane];
-                            if (F16) {
-                                const int sr = rs[rr];
-                                if (sr == kNonFiniteScale || cs == kNonFiniteScale) { nf = true; continue; }
-                                x = mul_pow2f(x, -(sr + cs));
-                            }
-                            p.C[(row0 + rr) * p.ldc + col] = p.alpha * x + add;
-                        }
+                        for (int rr = 0; rr < rows; rr++)
+                            p.C[(row0 + rr) * p.ldc + col] = p.alpha * stage[rr * 33 + lane] + add;
                     } else {
                         float cin[32];
 #pragma unroll
                         for (int rr = 0; rr < 32; rr++)
                             cin[rr] = rr < rows ? p.C[(row0 + rr) * p.ldc + col] : 0.f;
 #pragma unroll
-                        for (int rr = 0; rr < 32; rr++) {
-                            if (rr < rows) {
-                                float x = stage[rr * 33 + lane];
-                                bool skip = false;
-                                if (F16) {
-                                    const int sr = rs[rr];
-                                    skip = sr == kNonFiniteScale || cs == kNonFiniteScale;
-                                    x = mul_pow2f(x, -(sr + cs));
-                                }
-                                if (skip) nf = true;
-                                else p.C[(row0 + rr) * p.ldc + col] = epi_value(p, x, cin[rr]);
-                            }
-                        }
+                        for (int rr = 0; rr < 32; rr++)
+                            if (rr < rows) p.C[(row0 + rr) * p.ldc + col] = epi_value(p, stage[rr * 33 + lane], cin[rr]);
                     }
                 }
                 __syncwarp();
@@ -821,22 +800,15 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 if (lane == 0) ptx::mbar_arrive(&acc_empty[ch & 1]);
                 ch++;
             }
-            if (F16 && __any_sync(0xffffffffu, nf)) {   // outputs whose line holds an Inf or a NaN
-                for (int c = 0; c < ncols; c += 32) {
-                    const int64_t col = n0 + c + lane;
-                    if (col >= p.N) continue;
-                    const int cs = f16_line_scale(p.colbits[col]);
-                    const int rows = (p.M - row0) < 32 ? (int)(p.M - row0) : 32;
-                    for (int rr = 0; rr < rows; rr++)
-                        if (rs[rr] == kNonFiniteScale || cs == kNonFiniteScale) store_recomputed(p, row0 + rr, col);
-                }
-            }
-            if (F16) __syncwarp();   // rs is rewritten for the next tile
         }
     } else {   // EW == 8: two warps per TMEM lane quarter, 128 columns each
-        const int q = warp % 4, hc = (warp - 2) / 4;
+        const int q = warp % 4, hc = (warp - 2) / 4, wi = warp - 2;
+        int *cs_w = col_scale + wi * 128;   // F16: the scales of this warp's 128 columns ...
+        int *rs_w = row_scale + wi * 32;    // ... and 32 rows
+        float *stg = epi + wi * 32 * 17;    // 32 rows x 16 columns, padded
         const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        const bool vec = (p.ldc & 3) == 0 && ((uintptr_t)p.C & 15) == 0;
+        const bool rc = reads_c(p);
+        const int cl = lane & 15, rh = lane >> 4;   // this lane's column and row parity when storing
         int ch = 0;
         float total[128];
         bool go = true;
@@ -844,19 +816,33 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         while (go && next_item(p, num_tiles, it, t, half)) {
             int tm, tn;
             tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-            const int64_t row = (int64_t)tm * BM + q * 32 + lane;
+            const int64_t row0 = (int64_t)tm * BM + q * 32;
             const int64_t c0 = (int64_t)tn * BN + hc * 128;
+            if (F16) {   // the scales of the warp's rows and columns, once per tile
+                unsigned cb[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int64_t col = c0 + lane + 32 * j;
+                    cb[j] = col < p.N ? p.colbits[col] : 0u;
+                }
+                const unsigned rb = row0 + lane < p.M ? p.rowbits[row0 + lane] : 0u;
+                __syncwarp();   // the previous tile's reads of the scales are done
+#pragma unroll
+                for (int j = 0; j < 4; j++) cs_w[lane + 32 * j] = f16_line_scale(cb[j]);
+                rs_w[lane] = f16_line_scale(rb);
+                __syncwarp();
+            }
 #pragma unroll
             for (int j = 0; j < 128; j++) total[j] = 0.f;
             for (int c = 0; c < (p.num_kb + chunk_kb - 1) / chunk_kb; c++, ch++) {
                 const int b = ch & 1;
                 if (!ptx::mbar_wait(&acc_full[b], (ch >> 1) & 1, p.err, 4)) { go = false; break; }
                 ptx::tc_fence_after();
+                const uint32_t a0 = tmem + (uint32_t)(b * ACC_COLS) + lane_off + (uint32_t)(hc * 128);
 #pragma unroll
-                for (int g = 0; g < 4; g++) {
+                for (int g = 0; g < 4; g++) {   // 32 columns per load (128 totals + 32 in flight: 168 registers)
                     uint32_t r[32];
-                    ptx::tmem_ld_32x32b_x32(tmem + (uint32_t)(b * ACC_COLS) + lane_off + (uint32_t)(hc * 128 + g * 32),
-                                            r);
+                    ptx::tmem_ld_32x32b_x32(a0 + (uint32_t)(g * 32), r);
                     ptx::tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 32; j++) total[g * 32 + j] += __uint_as_float(r[j]);
@@ -866,48 +852,52 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
             }
             if (!go) break;
-            // this thread's row, 128 columns from c0, four at a time
+            // C in passes of 16 columns through shared memory: lane l holds row l's totals; after
+            // the transpose lane l takes column l % 16 of rows l / 16, l / 16 + 2, ..., so each
+            // load / store instruction covers two 64-byte row segments
             bool nf = false;
-            const int sr = (F16 && row < p.M) ? f16_line_scale(p.rowbits[row]) : 0;
-            if (row < p.M) {
-                const bool rc = reads_c(p);
-                float *crow = p.C + row * p.ldc;
+            const int64_t rows_left = p.M - row0;
 #pragma unroll
-                for (int g = 0; g < 32; g++) {
-                    const int64_t col = c0 + 4 * g;
-                    if (col >= p.N) break;
-                    float x[4] = {total[4 * g], total[4 * g + 1], total[4 * g + 2], total[4 * g + 3]};
-                    bool skip[4] = {false, false, false, false};
+            for (int ps = 0; ps < 8; ps++) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) stg[lane * 17 + j] = total[16 * ps + j];
+                __syncwarp();
+                const int64_t col = c0 + 16 * ps + cl;
+                const bool colok = col < p.N;
+                const int cs = F16 ? cs_w[16 * ps + cl] : 0;
+                float *cp = p.C + (row0 + rh) * p.ldc + col;
+                float cin[16];
+#pragma unroll
+                for (int i = 0; i < 16; i++)
+                    cin[i] = (rc && colok && 2 * i + rh < rows_left) ? cp[(int64_t)(2 * i) * p.ldc] : 0.f;
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    const int rr = 2 * i + rh;
+                    float x = stg[rr * 17 + cl];
+                    bool skip = false;
                     if (F16) {
-#pragma unroll
-                        for (int j = 0; j < 4; j++) {
-                            const int cs = col + j < p.N ? f16_line_scale(p.colbits[col + j]) : 0;
-                            skip[j] = sr == kNonFiniteScale || cs == kNonFiniteScale;
-                            x[j] = mul_pow2f(x[j], -(sr + cs));
-                        }
+                        const int sr = rs_w[rr];
+                        skip = sr == kNonFiniteScale || cs == kNonFiniteScale;
+                        x = mul_pow2f(x, -(sr + cs));
                     }
-                    const bool any_skip = skip[0] | skip[1] | skip[2] | skip[3];
-                    nf |= any_skip;
-                    if (vec && col + 3 < p.N && !any_skip) {
-                        float4 cin = rc ? *reinterpret_cast<const float4 *>(crow + col) : make_float4(0.f, 0.f, 0.f, 0.f);
-                        float4 v;
-                        v.x = epi_value(p, x[0], cin.x);
-                        v.y = epi_value(p, x[1], cin.y);
-                        v.z = epi_value(p, x[2], cin.z);
-                        v.w = epi_value(p, x[3], cin.w);
-                        *reinterpret_cast<float4 *>(crow + col) = v;
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 4; j++)
-                            if (col + j < p.N && !skip[j]) crow[col + j] = epi_value(p, x[j], rc ? crow[col + j] : 0.f);
+                    if (colok && rr < rows_left) {
+                        if (skip) nf = true;
+                        else cp[(int64_t)(2 * i) * p.ldc] = epi_value(p, x, cin[i]);
                     }
                 }
+                __syncwarp();
             }
-            if (F16 && __any_sync(0xffffffffu, nf) && row < p.M) {   // outputs whose line holds an Inf or a NaN
-                const int64_t c1 = c0 + 128 < p.N ? c0 + 128 : p.N;
-                for (int64_t col = c0; col < c1; col++)
-                    if (sr == kNonFiniteScale || f16_line_scale(p.colbits[col]) == kNonFiniteScale)
-                        store_recomputed(p, row, col);
+            if (F16 && __any_sync(0xffffffffu, nf)) {   // outputs whose line holds an Inf or a NaN
+                for (int ps = 0; ps < 8; ps++) {
+                    const int64_t col = c0 + 16 * ps + cl;
+                    if (col >= p.N) continue;
+                    const int cs = cs_w[16 * ps + cl];
+                    for (int i = 0; i < 16; i++) {
+                        const int rr = 2 * i + rh;
+                        if (row0 + rr < p.M && (rs_w[rr] == kNonFiniteScale || cs == kNonFiniteScale))
+                            store_recomputed(p, row0 + rr, col);
+                    }
+                }
             }
         }
     }
@@ -1361,7 +1351,7 @@ static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64
     p.num_kb = (int)(kp / BK);
     p.tiles_m = tiles_m;
     p.tiles_n = tiles_n;
-    p.chunk_kb = FOLD ? p.chunk_kb : 1;
+    p.chunk_kb = FOLD ? (p.chunk_kb > 0 ? p.chunk_kb : p.num_kb) : 1;
     p.half_start = half_start;
     bf16x3_gemm_kernel<NP, BN, FOLD, F16, EW><<<grid, CF::NT, CF::SMEM_BYTES, g.stream>>>(maps, p);
     GB_LAUNCH_CHECK("bf16x3_gemm_kernel");
@@ -1377,8 +1367,12 @@ static gb_status gemm_launch(const GemmArgs &g, int np, int fold_kb, const Piece
             return fold_kb > 0 ? two_pass_launch<3, 128, true, false, 4>(g, maps, kp, p, grid)
                                : two_pass_launch<3, 128, false, false, 4>(g, maps, kp, p, grid);
     }
-    return fold_kb > 0 ? two_pass_launch<2, 256, true, F16, 8>(g, maps, kp, p, grid)
-                       : two_pass_launch<2, 256, false, F16, 4>(g, maps, kp, p, grid);
+    if constexpr (F16) {   // always the wide folding form (fold_kb 0: one chunk over all of K)
+        return two_pass_launch<2, 256, true, true, 8>(g, maps, kp, p, grid);
+    } else {
+        return fold_kb > 0 ? two_pass_launch<2, 256, true, false, 8>(g, maps, kp, p, grid)
+                           : two_pass_launch<2, 256, false, false, 4>(g, maps, kp, p, grid);
+    }
 }
 
 // Split pass (NP 16-bit pieces per operand, K-major) + MMA kernel; fold_kb >
