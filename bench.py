@@ -76,8 +76,44 @@ def profile_traffic(name):
     return None
 
 
-FP32_SIMT_PEAK = 152 * 128 * 2 * 2.07e9 / 1e12       # nominal FFMA TFLOP/s
-FP64_PEAK = 1.25                                      # nominal FP64 TFLOP/s (GB300)
+
+
+class Cublas:
+    """cuBLAS through ctypes, for yardsticks printed beside the library's own
+    numbers (context only: never the measured product).  Row-major GEMMs are
+    issued as the column-major C^T = op(B)^T op(A)^T."""
+    R32, R64 = 0, 1                                   # cudaDataType
+    COMPUTE = {"32F": 68, "32F_EMULATED_16BFX9": 78, "64F": 70, "64F_EMULATED_FIXEDPOINT": 79}
+    EAGER = 2                                         # cublasEmulationStrategy_t
+
+    def __init__(self, stream):
+        import glob
+        paths = sorted(glob.glob("/usr/local/cuda/lib64/libcublas.so*"))
+        if not paths:
+            raise OSError("no libcublas.so")
+        self.L = ctypes.CDLL(paths[0])
+        self.h = ctypes.c_void_p()
+        if self.L.cublasCreate_v2(ctypes.byref(self.h)) != 0:
+            raise OSError("cublasCreate failed")
+        self.L.cublasSetStream_v2(self.h, ctypes.c_void_p(stream))
+        f = self.L.cublasGemmEx
+        f.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                      ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                      ctypes.c_int]
+
+    def gemm(self, ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, bits, compute):
+        emulated = "EMULATED" in compute
+        if hasattr(self.L, "cublasSetEmulationStrategy"):
+            self.L.cublasSetEmulationStrategy(self.h, self.EAGER if emulated else 0)
+        ct = ctypes.c_double if bits == 64 else ctypes.c_float
+        al, be = ct(alpha), ct(beta)
+        dt = self.R64 if bits == 64 else self.R32
+        rc = self.L.cublasGemmEx(self.h, 1 if tb == "T" else 0, 1 if ta == "T" else 0, N, M, K,
+                                 ctypes.addressof(al), B.data_ptr(), dt, ldb, A.data_ptr(), dt, lda,
+                                 ctypes.addressof(be), C.data_ptr(), dt, ldc, self.COMPUTE[compute], -1)
+        if rc != 0:
+            raise RuntimeError("cublasGemmEx(%s) status %d" % (compute, rc))
 
 
 class ClockSampler:
@@ -192,6 +228,9 @@ class Ctx:
         self.dev = torch.device("cuda", self.local)
         self.stream = torch.cuda.current_stream(self.dev)
         self.peaks, self.peak_src = measured_peaks()
+        # scalar FMA rooflines, measured on this GPU (FFMA and DFMA chains on every SM)
+        self.fma_peak = {32: gbblas.fma_peak(32, self.stream.cuda_stream),
+                         64: gbblas.fma_peak(64, self.stream.cuda_stream)}
 
     def event(self):
         return self.torch.cuda.Event(enable_timing=True)
@@ -418,6 +457,40 @@ def run_sgemm(ctx):
         return 4 * len(MODES) * flops / (s0.elapsed_time(s1) * 1e-3) / 1e12
 
     compare = {an + "_tflops": rate(ids[an]) for an in ("simt", "bf16x3", "bf16x6", "fp16x3")}
+    # cuBLAS on the same inputs (yardsticks, not the product): native FP32 and its emulated
+    # BF16x9 form, rate and error on the same subgrid
+    try:
+        cb = Cublas(ctx.stream.cuda_stream)
+        for name, compute in (("cublas_sgemm", "32F"), ("cublas_bf16x9", "32F_EMULATED_16BFX9")):
+            def cgemm(mode, Cx, compute=compute):
+                A, B = ops(mode)
+                cb.gemm(mode[0], mode[1], M, N, K, ALPHA, A, LD, B, LD, BETA, Cx, LD, 32, compute)
+            if "simt" in errors:
+                worst = 0.0
+                for mode in MODES:
+                    Cw = C0.clone()
+                    cgemm(mode, Cw)
+                    A = hb["A_T" if mode[0] == "T" else "A_N"]
+                    B = hb["B_T" if mode[1] == "T" else "B_N"]
+                    e, _ = oracle.normwise_error(Cw.cpu().numpy(), mode[0], mode[1], M, N, K, ALPHA, A, LD, B, LD,
+                                                 BETA, c0, LD, rows, cols)
+                    worst = max(worst, e)
+                errors[name] = worst
+            Cw = C0.clone()
+            for mode in MODES:
+                cgemm(mode, Cw)
+            s0, s1 = ctx.event(), ctx.event()
+            s0.record(ctx.stream)
+            for _ in range(4):
+                for mode in MODES:
+                    cgemm(mode, Cw)
+            s1.record(ctx.stream)
+            torch.cuda.synchronize()
+            compare[name + "_tflops"] = 4 * len(MODES) * flops / (s0.elapsed_time(s1) * 1e-3) / 1e12
+        compare["cublas_note"] = ("cuBLAS yardsticks on the same inputs: CUBLAS_COMPUTE_32F and "
+                                  "CUBLAS_COMPUTE_32F_EMULATED_16BFX9 (emulation strategy eager)")
+    except Exception as e:
+        compare["cublas_error"] = repr(e)
     # the headline form: the fastest emulated form whose measured error is no worse than plain
     # FFMA's on the same subgrid (matched error); --algo names one instead
     if args.algo != "best":
@@ -513,8 +586,8 @@ def run_sgemm(ctx):
                           else "split + MMA kernels")}
         kname = "sgemm_%s_4096" % algo_name
     else:
-        roof = {"bound": "fp32-simt", "achieved": kernel_tflops, "peak": FP32_SIMT_PEAK, "unit": "TFLOP/s",
-                "peak_note": "nominal FFMA peak 152 SMs x 128 lanes x 2 x 2.07 GHz (no measured FP32 peak)"}
+        roof = {"bound": "fp32-simt", "achieved": kernel_tflops, "peak": ctx.fma_peak[32], "unit": "TFLOP/s",
+                "peak_note": "FFMA peak measured on this GPU (gb_measure_fma_peak)"}
         kname = "sgemm_simt_4096"
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["traffic"] = profile_traffic(kname)
@@ -603,6 +676,26 @@ def run_dgemm(ctx):
             e, mr = err_of(mode, Cw)
             res[mode] = {"tflops": flops / (a.elapsed_time(b) * 1e-3) / 1e12, "normwise": e, "max_rel": mr}
         study["native_fp64"] = res
+        try:   # cuBLAS yardsticks (not the product): native DGEMM and its fixed-point emulation
+            cb = Cublas(ctx.stream.cuda_stream)
+            for name, compute in (("cublas_dgemm", "64F"), ("cublas_fixedpoint", "64F_EMULATED_FIXEDPOINT")):
+                res = {}
+                for mode in modes:
+                    A = bufs["AT" if mode[0] == "T" else "A"]
+                    B = bufs["BT" if mode[1] == "T" else "B"]
+                    Cw = C0.clone()
+                    cb.gemm(mode[0], mode[1], n, n, n, 1.0, A, n, B, n, 1.0, Cw, n, 64, compute)
+                    Cw2 = C0.clone()
+                    a, b = ctx.event(), ctx.event()
+                    a.record(ctx.stream)
+                    cb.gemm(mode[0], mode[1], n, n, n, 1.0, A, n, B, n, 1.0, Cw2, n, 64, compute)
+                    b.record(ctx.stream)
+                    torch.cuda.synchronize()
+                    e, mr = err_of(mode, Cw2)
+                    res[mode] = {"tflops": flops / (a.elapsed_time(b) * 1e-3) / 1e12, "normwise": e, "max_rel": mr}
+                study[name] = res
+        except Exception as e:
+            study["cublas_error"] = repr(e)
         study["subgrid"] = "seeded %d x %d rows/cols, Dot2 oracle" % (sub, sub)
         if slices == 0:   # fewest slices whose error is no worse than native FP64's in both modes
             for s in (4, 5, 6, 7, 8, 9):
@@ -725,11 +818,12 @@ def run_skinny(ctx):
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
     value = aggregate(ctx.world, args.steps, len(MODES) * nbytes_alg, ms) / 1e9
     tflops = flops / (kms * 1e-3) / 1e12
-    cpeak = FP64_PEAK if bits == 64 else FP32_SIMT_PEAK
+    cpeak = ctx.fma_peak[bits]
     roof = bw_roof(ctx, nbytes_alg / (kms * 1e-3) / 1e9, None, "%s_%s_n%d" % (args.workload, "f%d" % bits, small),
                    {"compute_tflops": tflops, "compute_peak_tflops": cpeak,
                     "compute_frac": tflops / cpeak, "kernel_ms": kms, "kernel_ms_by_mode": ctx.per_mode_ms(MODES),
-                    "peak_note_compute": "nominal %s peak" % ("FP64" if bits == 64 else "FP32 FFMA")})
+                    "peak_note_compute": "%s peak measured on this GPU (gb_measure_fma_peak)"
+                                         % ("DFMA" if bits == 64 else "FFMA")})
     hostbufs = {m: (ops[m][0].cpu().pin_memory(), ops[m][2].cpu().pin_memory()) for m in MODES}
     hostC = C.cpu().pin_memory()
 
@@ -853,7 +947,8 @@ def run_jacobi(ctx):
              "fp_tflops": gflops, "note": "achieved = algorithmic bytes (2*M*N*s per sweep) / time; temporal "
              "blocking lets it exceed the HBM peak (DRAM bytes in profiles/)"}
     if bits == 64:
-        extra.update({"compute_bound": "fp64", "compute_peak_tflops": FP64_PEAK, "compute_frac": gflops / FP64_PEAK})
+        extra.update({"compute_bound": "fp64", "compute_peak_tflops": ctx.fma_peak[64],
+                      "compute_frac": gflops / ctx.fma_peak[64], "compute_peak_note": "DFMA peak measured on this GPU"})
     roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "%s_f%d_8192" % ("stencil9" if nine else "jacobi", bits),
                    extra)
     hA = A0.cpu().pin_memory()

@@ -173,6 +173,60 @@ __global__ void bounded_wait_selftest_kernel(int *err, uint64_t limit_ns) {
     ptx::mbar_wait_limit(&bar, 0, err, 99, limit_ns);
 }
 
+// ------------------------------------------------------------ FMA peak
+// Eight independent FMA chains per thread, 16 steps each per iteration, on
+// every SM: the scalar FP32 (FFMA) or FP64 (DFMA) throughput of this GPU,
+// the roofline of the plain SIMT kernels.  x -> x*a + b with a = 1 - 2^-20,
+// b = 2^-20 keeps every chain near 1; the sum is stored only if it takes an
+// impossible value, so the chains are not removed.
+static __device__ float g_fma_sink32;
+static __device__ double g_fma_sink64;
+
+template <typename T>
+__global__ void __launch_bounds__(256) fma_peak_kernel(int iters, T a, T b) {
+    T x[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) x[j] = (T)1 + (T)(threadIdx.x + j) * (T)1e-7;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int s = 0; s < 16; s++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) x[j] = fma(x[j], a, b);
+    }
+    T sum = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) sum += x[j];
+    if (sum == (T)-12345) {
+        if (sizeof(T) == 8) g_fma_sink64 = (double)sum;
+        else g_fma_sink32 = (float)sum;
+    }
+}
+
+template <typename T>
+static gb_status fma_peak(double *tflops, void *stream) {
+    cudaStream_t st = as_stream(stream);
+    const int blocks = sm_count() * 8, threads = 256;
+    const int iters = sizeof(T) == 8 ? 256 : 4096;
+    cudaEvent_t e0, e1;
+    GB_CUDA_TRY(cudaEventCreate(&e0));
+    GB_CUDA_TRY(cudaEventCreate(&e1));
+    const T a = (T)1 - (T)(1.0 / 1048576.0), b = (T)(1.0 / 1048576.0);
+    fma_peak_kernel<T><<<blocks, threads, 0, st>>>(iters / 8, a, b);   // warm-up
+    GB_LAUNCH_CHECK("fma_peak_kernel");
+    GB_CUDA_TRY(cudaEventRecord(e0, st));
+    fma_peak_kernel<T><<<blocks, threads, 0, st>>>(iters, a, b);
+    GB_LAUNCH_CHECK("fma_peak_kernel");
+    GB_CUDA_TRY(cudaEventRecord(e1, st));
+    GB_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    GB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    return ok();
+}
+
 // -------------------------------------------------------------- generator
 template <typename T>
 __global__ void fill_kernel(T *X, int64_t rows, int64_t cols, int64_t ld, uint64_t seed, int kind) {
@@ -323,6 +377,12 @@ gb_status gb_selftest_bounded_wait(uint64_t limit_ns, void *stream) {
     bounded_wait_selftest_kernel<<<1, 32, 0, as_stream(stream)>>>(err, limit_ns);
     GB_LAUNCH_CHECK("bounded_wait_selftest_kernel");
     return ok();
+}
+
+gb_status gb_measure_fma_peak(int dtype_bits, double *tflops, void *stream) {
+    GB_CHECK_ARG(dtype_bits == 32 || dtype_bits == 64, "gb_measure_fma_peak: dtype_bits must be 32 or 64");
+    GB_CHECK_ARG(tflops != nullptr, "gb_measure_fma_peak: null out-pointer");
+    return dtype_bits == 64 ? fma_peak<double>(tflops, stream) : fma_peak<float>(tflops, stream);
 }
 
 gb_status gb_fill_f64(double *X, int64_t rows, int64_t cols, int64_t ld, uint64_t seed, int kind, void *stream) {

@@ -1408,10 +1408,16 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
         device_setup_done(carve);
     }
 
+    // Launches captured into a graph run whenever the graph is replayed, so the host cannot
+    // count their CTAs: a captured call neither tracks nor overlaps.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    GB_CUDA_TRY(cudaStreamIsCapturing(g.stream, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+
     // the stream's state and this call's launches as one step
     std::lock_guard<std::mutex> lk(g_tp_mu);
     StreamState &st = stream_state(dev, g.stream);
-    unsigned long long *done = done_counter(dev, st.slot);
+    unsigned long long *done = capturing ? nullptr : done_counter(dev, st.slot);
     uintptr_t alo, ahi, blo, bhi, clo, chi;
     span(g.A, g.ta, g.M, g.K, g.lda, 4, alo, ahi);
     span(g.B, g.tb, g.K, g.N, g.ldb, 4, blo, bhi);
@@ -1527,7 +1533,7 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
     gb_status s = f16 ? gemm_launch<true>(g, np, fold_kb, maps, kp, p, &grid)
                       : gemm_launch<false>(g, np, fold_kb, maps, kp, p, &grid);
     if (s != GB_OK) return s;
-    st.launched += (unsigned long long)grid;
+    if (done) st.launched += (unsigned long long)grid;
     st.valid = done != nullptr;
     st.c_lo = clo;
     st.c_hi = chi;

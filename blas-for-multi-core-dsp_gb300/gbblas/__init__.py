@@ -124,6 +124,7 @@ _SIGS = {
     "gb_ref_set_stream": ([_vp], None),
     "gb_workspace_reserve": ([ctypes.c_size_t, _vp], _int),
     "gb_selftest_bounded_wait": ([ctypes.c_uint64, _vp], _int),
+    "gb_measure_fma_peak": ([_int, ctypes.POINTER(ctypes.c_double), _vp], _int),
     "gb_gemm_batch": ([ctypes.POINTER(GemmDesc), _int, _vp], _int),
     "gb_server_config_init": ([ctypes.POINTER(ServerConfig)], None),
     "gb_server_create": ([ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)], _int),
@@ -207,6 +208,13 @@ def launch_count():
 
 def arch():
     return lib().gb_device_arch()
+
+
+def fma_peak(bits, stream=None):
+    """Measured scalar FMA throughput (TFLOP/s) of the device: FFMA (32) or DFMA (64)."""
+    v = ctypes.c_double()
+    _check(lib().gb_measure_fma_peak(bits, ctypes.byref(v), _stream(stream)), "gb_measure_fma_peak")
+    return v.value
 
 
 def sync(stream=None):

@@ -66,7 +66,10 @@ gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int kind, void *st
 /* The library keeps one grow-only scratch buffer per (device, stream) for
  * split-K partials and split / sliced GEMM operands.  Growing it
  * synchronises that stream; reserve the largest size up front to keep
- * cudaMalloc off the call path of later calls on `stream`. */
+ * cudaMalloc off the call path of later calls on `stream`.  Calls captured
+ * into a CUDA graph refer to the buffer as it was at capture: reserve it
+ * before capturing, and do not let later calls on that stream grow it while
+ * the graph is still replayed (growing frees the old buffer). */
 gb_status gb_workspace_reserve(size_t bytes, void *stream);
 
 /* Self-test of the bounded device waits (no reference counterpart; the
@@ -79,6 +82,12 @@ gb_status gb_workspace_reserve(size_t bytes, void *stream);
  * GB_ERR_DEVICE_TIMEOUT, the one after that GB_OK, and the device stays
  * usable. */
 gb_status gb_selftest_bounded_wait(uint64_t limit_ns, void *stream);
+
+/* Scalar FMA throughput of the current device (no reference counterpart): a
+ * short kernel of independent FFMA (dtype_bits 32) or DFMA (64) chains on
+ * every SM, timed with CUDA events on `stream`; *tflops = 2 x FMAs / time.
+ * The roofline of the plain SIMT / DFMA kernels.  Synchronises `stream`. */
+gb_status gb_measure_fma_peak(int dtype_bits, double *tflops, void *stream);
 
 /* ------------------------------------------------------------ inputs */
 /* Seeded counter-based generator (bit-identical to the oracle's): element

@@ -573,3 +573,39 @@ def test_bf16x3_folded_wide_form_exact(torch):
             assert np.array_equal(host(dC), want), mode
     finally:
         os.environ.pop("GB_BF16X3_FOLD", None)
+
+
+@pytest.mark.parametrize("algo_name", ["BF16X3", "FP16X3"])
+def test_two_pass_captured_in_cuda_graph(torch, algo_name):
+    """A call captured into a CUDA graph (workspace reserved first) replays
+    to the same bits as the eager call, also with eager calls of other shapes
+    on the same stream between the replays."""
+    import gbblas
+    algo = getattr(gbblas, "ALGO_" + algo_name)
+    tc = torch
+    s = tc.cuda.Stream()
+    M, N, K = 1024, 768, 1536
+    A = dev(oracle.fill(M, K, 960, dtype=np.float32))
+    B = dev(oracle.fill(K, N, 961, dtype=np.float32))
+    A2 = dev(oracle.fill(512, 640, 962, dtype=np.float32))
+    B2 = dev(oracle.fill(640, 384, 963, dtype=np.float32))
+    assert gbblas.lib().gb_workspace_reserve(256 << 20, s.cuda_stream) == gbblas.OK
+    C_ref = tc.zeros((M, N), dtype=tc.float32, device="cuda:0")
+    C2_ref = tc.zeros((512, 384), dtype=tc.float32, device="cuda:0")
+    with tc.cuda.stream(s):
+        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B, N, 0.0, C_ref, N, algo=algo, stream=s)
+        gbblas.sgemm("N", "N", 512, 384, 640, 1.0, A2, 640, B2, 384, 0.0, C2_ref, 384, algo=algo, stream=s)
+    s.synchronize()
+    C = tc.zeros_like(C_ref)
+    g = tc.cuda.CUDAGraph()
+    with tc.cuda.graph(g, stream=s):
+        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B, N, 0.0, C, N, algo=algo, stream=s)
+    C2 = tc.zeros_like(C2_ref)
+    with tc.cuda.stream(s):
+        for _ in range(3):
+            C.zero_()
+            g.replay()
+            gbblas.sgemm("N", "N", 512, 384, 640, 1.0, A2, 640, B2, 384, 0.0, C2, 384, algo=algo, stream=s)
+    s.synchronize()
+    assert tc.equal(C, C_ref)
+    assert tc.equal(C2, C2_ref)
