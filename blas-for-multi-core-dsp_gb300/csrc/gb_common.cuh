@@ -151,6 +151,8 @@ struct GemmArgs {
     double alpha, beta;
     int semantics;   // gb_semantics
     int k_block, k_slab, alpha_on_b;
+    int accum_k;     // tensor-core SGEMM forms: accumulator chunk in K (0 default, < 0 none)
+    int split_k;     // skinny: split-K override (0: the planner's)
     cudaStream_t stream;
 };
 

@@ -96,6 +96,8 @@ gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alph
     g.alpha = (double)alpha; g.beta = (double)beta;
     g.semantics = o.semantics;
     g.k_block = o.k_block; g.k_slab = o.k_slab; g.alpha_on_b = o.alpha_on_b;
+    GB_CHECK_ARG(o.split_k >= 0 && o.split_k <= 64, "%s: split_k %d not in 0..64", fn, o.split_k);
+    g.accum_k = o.accum_k; g.split_k = o.split_k;
     g.stream = as_stream(o.stream);
 
     int algo = o.algo;

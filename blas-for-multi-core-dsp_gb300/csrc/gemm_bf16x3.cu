@@ -1221,9 +1221,13 @@ gb_status launch(const GemmArgs &g, int *err) {
 
 static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16);
 
-// Accumulator chunk (k-blocks of 32) from the environment, for measurement.
-static int env_chunk(const char *name, int dflt) {
-    const char *v = getenv(name);
+// Accumulator chunk in k-blocks of 32 (0: one accumulator over all of K):
+// the call's accum_k (values of K, < 0 none), else the environment variable
+// (k-blocks, for measurement), else the form's default.
+static int chunk_kb(const GemmArgs &g, const char *env, int dflt) {
+    if (g.accum_k < 0) return 0;
+    if (g.accum_k > 0) return (int)((g.accum_k + 31) / 32);
+    const char *v = getenv(env);
     if (!v || !*v) return dflt;
     const int c = atoi(v);
     return c < 0 ? 0 : c;
@@ -1253,21 +1257,21 @@ gb_status launch_sgemm_bf16x3(const GemmArgs &g) {
             return fused::launch<256>(g, e);
         }
     }
-    return two_pass(g, 2, env_chunk("GB_BF16X3_FOLD", 0), false);
+    return two_pass(g, 2, chunk_kb(g, "GB_BF16X3_FOLD", 0), false);
 }
 
 gb_status launch_sgemm_bf16x6(const GemmArgs &g) {
     if (g.M == 0 || g.N == 0) return ok();
     if (g.M > 0x7fffffff / 2 || g.N > 0x7fffffff / 2 || g.K > 0x7fffffff / 2)
         return set_status(GB_ERR_UNSUPPORTED, "bf16x6: dimension too large");
-    return two_pass(g, 3, env_chunk("GB_BF16X6_CHUNK", 8), false);
+    return two_pass(g, 3, chunk_kb(g, "GB_BF16X6_CHUNK", 8), false);
 }
 
 gb_status launch_sgemm_fp16x3(const GemmArgs &g) {
     if (g.M == 0 || g.N == 0) return ok();
     if (g.M > 0x7fffffff / 2 || g.N > 0x7fffffff / 2 || g.K > 0x7fffffff / 2)
         return set_status(GB_ERR_UNSUPPORTED, "fp16x3: dimension too large");
-    return two_pass(g, 2, env_chunk("GB_FP16X3_FOLD", 4), true);
+    return two_pass(g, 2, chunk_kb(g, "GB_FP16X3_FOLD", 4), true);
 }
 
 // ------------------------------------------------------------ stream state

@@ -50,7 +50,7 @@ struct TuneKey {
     }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, int> g_tune;
+std::map<TuneKey, gb_tune_choice> g_tune;
 
 int lg(int64_t x) {   // bucket: round(log2(x)) (0 for x <= 1)
     if (x <= 1) return 0;
@@ -62,10 +62,12 @@ TuneKey key_of(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
 }
 }  // namespace
 
-int tuned_algo(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
+bool tuned_choice(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K, gb_tune_choice *out) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tune.find(key_of(bits, ta, tb, M, N, K));
-    return it == g_tune.end() ? -1 : it->second;
+    if (it == g_tune.end()) return false;
+    *out = it->second;
+    return true;
 }
 
 // ------------------------------------------------------------------- server
@@ -181,9 +183,13 @@ gb_status launch_one(Server *s, const gb_request &r, cudaStream_t st) {
         o.stream = st;
         o.semantics = r.semantics;
         o.algo = r.algo;
-        if (o.algo == GB_ALGO_AUTO) {
-            int t = tuned_algo(r.dtype_bits, is_trans(r.transA), is_trans(r.transB), r.M, r.N, r.K);
-            if (t >= 0) o.algo = t;
+        gb_tune_choice t;
+        if (o.algo == GB_ALGO_AUTO && tuned_choice(r.dtype_bits, is_trans(r.transA), is_trans(r.transB), r.M, r.N,
+                                                   r.K, &t)) {
+            o.algo = t.algo;
+            o.accum_k = t.accum_k;
+            o.split_k = t.split_k;
+            o.ozaki_slices = t.ozaki_slices;
         }
         if (r.dtype_bits == 64)
             return gb_dgemm(r.transA, r.transB, r.M, r.N, r.K, r.alpha, (const double *)r.A, r.lda,
@@ -453,21 +459,87 @@ void gb_server_destroy(gb_server *sv) {
 gb_status gb_autotune_set(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K, int algo) {
     GB_CHECK_ARG(dtype_bits == 32 || dtype_bits == 64, "gb_autotune_set: dtype_bits");
     GB_CHECK_ARG(gb::is_mode(transA) && gb::is_mode(transB), "gb_autotune_set: mode");
-    GB_CHECK_ARG(algo >= GB_ALGO_AUTO && algo <= GB_ALGO_SKINNY, "gb_autotune_set: algo");
+    GB_CHECK_ARG(algo >= GB_ALGO_AUTO && algo <= GB_ALGO_FP16X3, "gb_autotune_set: algo");
+    gb_tune_choice c;
+    memset(&c, 0, sizeof(c));
+    c.algo = algo;
     std::lock_guard<std::mutex> lk(gb::g_tune_mu);
-    gb::g_tune[gb::key_of(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K)] = algo;
+    gb::g_tune[gb::key_of(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K)] = c;
+    return gb::ok();
+}
+
+gb_status gb_autotune_lookup(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
+                             gb_tune_choice *out) {
+    GB_CHECK_ARG(out != nullptr, "gb_autotune_lookup: null out-pointer");
+    if (!gb::tuned_choice(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K, out))
+        return gb::set_status(GB_ERR_INVALID_ARG, "gb_autotune_lookup: no choice for this bucket");
     return gb::ok();
 }
 
 int gb_autotune_get(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K) {
-    return gb::tuned_algo(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K);
+    gb_tune_choice c;
+    return gb::tuned_choice(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K, &c) ? c.algo : -1;
 }
 
-gb_status gb_autotune_gemm(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K, int *best,
-                           double *best_ms) {
-    GB_CHECK_ARG(dtype_bits == 32 || dtype_bits == 64, "gb_autotune_gemm: dtype_bits");
-    GB_CHECK_ARG(gb::is_mode(transA) && gb::is_mode(transB), "gb_autotune_gemm: mode");
-    GB_CHECK_ARG(M > 0 && N > 0 && K > 0, "gb_autotune_gemm: dimensions must be positive");
+namespace gb {
+namespace {
+
+// One candidate: algorithm and knobs (as in gb_gemm_opts).
+gb_status run_candidate(int bits, char ta, char tb, int64_t M, int64_t N, int64_t K, const void *A, int64_t lda,
+                        const void *B, int64_t ldb, void *C, const gb_tune_choice &c, void *stream) {
+    gb_gemm_opts o;
+    gb_gemm_opts_init(&o);
+    o.stream = stream;
+    o.algo = c.algo;
+    o.accum_k = c.accum_k;
+    o.split_k = c.split_k;
+    o.ozaki_slices = c.ozaki_slices;
+    return bits == 64 ? gb_dgemm(ta, tb, M, N, K, 1.0, (const double *)A, lda, (const double *)B, ldb, 0.0,
+                                 (double *)C, N, &o)
+                      : gb_sgemm(ta, tb, M, N, K, 1.0f, (const float *)A, lda, (const float *)B, ldb, 0.0f,
+                                 (float *)C, N, &o);
+}
+
+std::vector<gb_tune_choice> candidates(int bits, int64_t M, int64_t N, int64_t K, double target_err) {
+    std::vector<gb_tune_choice> v;
+    auto add = [&](int algo, int accum, int split, int slices) {
+        gb_tune_choice c;
+        memset(&c, 0, sizeof(c));
+        c.algo = algo; c.accum_k = accum; c.split_k = split; c.ozaki_slices = slices;
+        v.push_back(c);
+    };
+    const int64_t small = M < N ? M : N;
+    if (bits == 32) {
+        add(GB_ALGO_SIMT, 0, 0, 0);
+        if (K >= 64) add(GB_ALGO_BF16X3, 0, 0, 0);   // its split floor meets 2*K*u32 from K ~ 12: keep a margin
+        add(GB_ALGO_FP16X3, 128, 0, 0);
+        add(GB_ALGO_FP16X3, 256, 0, 0);
+        add(GB_ALGO_BF16X6, 0, 0, 0);
+    } else {
+        add(GB_ALGO_ORDERED, 0, 0, 0);
+        add(GB_ALGO_DMMA, 0, 0, 0);
+        const int s = ozaki_pick_slices(target_err, K);
+        add(GB_ALGO_OZAKI, 0, 0, s);
+        if (s < 9) add(GB_ALGO_OZAKI, 0, 0, s + 1);
+    }
+    if (small <= 64) {
+        add(GB_ALGO_SKINNY, 0, 0, 0);
+        for (int sp : {1, 4, 16}) add(GB_ALGO_SKINNY, 0, sp, 0);
+    }
+    return v;
+}
+
+}  // namespace
+}  // namespace gb
+
+gb_status gb_autotune_gemm_ex(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
+                              double target_err, int reps, void *stream, gb_tune_choice *best) {
+    GB_CHECK_ARG(dtype_bits == 32 || dtype_bits == 64, "gb_autotune_gemm_ex: dtype_bits");
+    GB_CHECK_ARG(gb::is_mode(transA) && gb::is_mode(transB), "gb_autotune_gemm_ex: mode");
+    GB_CHECK_ARG(M > 0 && N > 0 && K > 0, "gb_autotune_gemm_ex: dimensions must be positive");
+    GB_CHECK_ARG(target_err >= 0.0, "gb_autotune_gemm_ex: negative target_err");
+    GB_CHECK_ARG(reps == 0 || (reps >= 5 && reps <= 1000), "gb_autotune_gemm_ex: reps must be 0 or 5..1000");
+    if (reps == 0) reps = 5;
     const bool ta = gb::is_trans(transA), tb = gb::is_trans(transB);
     const int64_t es = dtype_bits / 8;
     const int64_t lda = ta ? M : K, ldb = tb ? K : N;
@@ -477,61 +549,65 @@ gb_status gb_autotune_gemm(int dtype_bits, char transA, char transB, int64_t M, 
     if ((st = gb_malloc(&B, (size_t)(K * N * es))) != GB_OK) { gb_free(A); return st; }
     if ((st = gb_malloc(&C, (size_t)(M * N * es))) != GB_OK) { gb_free(A); gb_free(B); return st; }
     if (dtype_bits == 64) {
-        gb_fill_f64((double *)A, ta ? K : M, lda, lda, 1, 0, nullptr);
-        gb_fill_f64((double *)B, tb ? N : K, ldb, ldb, 2, 0, nullptr);
+        gb_fill_f64((double *)A, ta ? K : M, lda, lda, 1, 0, stream);
+        gb_fill_f64((double *)B, tb ? N : K, ldb, ldb, 2, 0, stream);
     } else {
-        gb_fill_f32((float *)A, ta ? K : M, lda, lda, 1, 0, nullptr);
-        gb_fill_f32((float *)B, tb ? N : K, ldb, ldb, 2, 0, nullptr);
+        gb_fill_f32((float *)A, ta ? K : M, lda, lda, 1, 0, stream);
+        gb_fill_f32((float *)B, tb ? N : K, ldb, ldb, 2, 0, stream);
     }
-    std::vector<int> cands;
-    const int64_t small = M < N ? M : N;
-    if (dtype_bits == 32) {
-        cands = {GB_ALGO_SIMT};
-        if (K >= 64) cands.push_back(GB_ALGO_BF16X3);   // meets 2*K*u only from K ~ 12; keep a margin
-    } else {
-        cands = {GB_ALGO_ORDERED, GB_ALGO_OZAKI};
-    }
-    if (small <= 64) cands.push_back(GB_ALGO_SKINNY);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    int arg = cands[0];
-    float bestt = 1e30f;
-    for (int a : cands) {
-        gb_gemm_opts o;
-        gb_gemm_opts_init(&o);
-        o.algo = a;
-        float tsum = 0;
-        bool okrun = true;
-        for (int rep = 0; rep < 3 && okrun; rep++) {
-            cudaEventRecord(e0, nullptr);
-            gb_status r = dtype_bits == 64
-                              ? gb_dgemm(transA, transB, M, N, K, 1.0, (const double *)A, lda, (const double *)B, ldb,
-                                         0.0, (double *)C, N, &o)
-                              : gb_sgemm(transA, transB, M, N, K, 1.0f, (const float *)A, lda, (const float *)B, ldb,
-                                         0.0f, (float *)C, N, &o);
-            cudaEventRecord(e1, nullptr);
-            cudaEventSynchronize(e1);
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (r != GB_OK) okrun = false;
-            else if (rep > 0) tsum += ms;   // first run warms up
+    const std::vector<gb_tune_choice> cands = gb::candidates(dtype_bits, M, N, K, target_err);
+    std::vector<cudaEvent_t> ev(2 * (size_t)reps);
+    for (auto &e : ev) cudaEventCreate(&e);
+    gb_tune_choice arg = cands[0];
+    arg.ms = 1e30;
+    for (const gb_tune_choice &c0 : cands) {
+        gb_tune_choice c = c0;
+        bool okrun = gb::run_candidate(dtype_bits, transA, transB, M, N, K, A, lda, B, ldb, C, c, stream) == GB_OK;
+        double med = 0;
+        for (int attempt = 0; attempt < 2 && okrun; attempt++) {
+            for (int r = 0; r < reps && okrun; r++) {
+                cudaEventRecord(ev[2 * r], gb::as_stream(stream));
+                okrun = gb::run_candidate(dtype_bits, transA, transB, M, N, K, A, lda, B, ldb, C, c, stream) == GB_OK;
+                cudaEventRecord(ev[2 * r + 1], gb::as_stream(stream));
+            }
+            if (!okrun || cudaStreamSynchronize(gb::as_stream(stream)) != cudaSuccess) {
+                cudaGetLastError();
+                okrun = false;
+                break;
+            }
+            std::vector<float> t((size_t)reps);
+            for (int r = 0; r < reps; r++) cudaEventElapsedTime(&t[r], ev[2 * r], ev[2 * r + 1]);
+            std::sort(t.begin(), t.end());
+            med = t[reps / 2];
+            if (t[reps - 1] <= 1.3f * t[0]) break;   // steady: keep it; else measure once more
         }
-        if (okrun && tsum / 2 < bestt) {
-            bestt = tsum / 2;
-            arg = a;
+        gb_clear_last_status();
+        if (okrun && med < arg.ms) {
+            arg = c;
+            arg.ms = med;
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    for (auto &e : ev) cudaEventDestroy(e);
     gb_free(A);
     gb_free(B);
     gb_free(C);
-    gb_status sync = gb_sync(nullptr);
-    if (sync != GB_OK) return sync;
-    gb_autotune_set(dtype_bits, transA, transB, M, N, K, arg);
+    st = gb_sync(stream);
+    if (st != GB_OK) return st;
+    {
+        std::lock_guard<std::mutex> lk(gb::g_tune_mu);
+        gb::g_tune[gb::key_of(dtype_bits, ta, tb, M, N, K)] = arg;
+    }
     if (best) *best = arg;
-    if (best_ms) *best_ms = bestt;
+    return gb::ok();
+}
+
+gb_status gb_autotune_gemm(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K, int *best,
+                           double *best_ms) {
+    gb_tune_choice c;
+    gb_status st = gb_autotune_gemm_ex(dtype_bits, transA, transB, M, N, K, 0.0, 5, nullptr, &c);
+    if (st != GB_OK) return st;
+    if (best) *best = c.algo;
+    if (best_ms) *best_ms = c.ms;
     return gb::ok();
 }
 
@@ -540,10 +616,11 @@ gb_status gb_autotune_save(const char *path) {
     FILE *f = fopen(path, "w");
     if (!f) return gb::set_status(GB_ERR_INVALID_ARG, "gb_autotune_save: cannot open %s", path);
     std::lock_guard<std::mutex> lk(gb::g_tune_mu);
-    fprintf(f, "# bits ta tb log2M log2N log2K algo\n");
+    fprintf(f, "# bits ta tb log2M log2N log2K algo accum_k split_k slices ms\n");
     for (auto &kv : gb::g_tune)
-        fprintf(f, "%d %d %d %d %d %d %d\n", kv.first.bits, kv.first.ta, kv.first.tb, kv.first.lm, kv.first.ln,
-                kv.first.lk, kv.second);
+        fprintf(f, "%d %d %d %d %d %d %d %d %d %d %.6g\n", kv.first.bits, kv.first.ta, kv.first.tb, kv.first.lm,
+                kv.first.ln, kv.first.lk, kv.second.algo, kv.second.accum_k, kv.second.split_k,
+                kv.second.ozaki_slices, kv.second.ms);
     fclose(f);
     return gb::ok();
 }
@@ -557,10 +634,13 @@ gb_status gb_autotune_load(const char *path) {
     while (fgets(line, sizeof(line), f)) {
         if (line[0] == '#') continue;
         gb::TuneKey k;
-        int a;
-        if (sscanf(line, "%d %d %d %d %d %d %d", &k.bits, &k.ta, &k.tb, &k.lm, &k.ln, &k.lk, &a) == 7 &&
-            a >= GB_ALGO_AUTO && a <= GB_ALGO_SKINNY)
-            gb::g_tune[k] = a;
+        gb_tune_choice c;
+        memset(&c, 0, sizeof(c));
+        const int n = sscanf(line, "%d %d %d %d %d %d %d %d %d %d %lf", &k.bits, &k.ta, &k.tb, &k.lm, &k.ln, &k.lk,
+                             &c.algo, &c.accum_k, &c.split_k, &c.ozaki_slices, &c.ms);
+        if ((n == 7 || n >= 10) && c.algo >= GB_ALGO_AUTO && c.algo <= GB_ALGO_FP16X3 && c.split_k >= 0 &&
+            c.split_k <= 64 && c.ozaki_slices >= 0 && c.ozaki_slices <= 9)
+            gb::g_tune[k] = c;
     }
     fclose(f);
     return gb::ok();

@@ -44,6 +44,7 @@ struct SkParams {
     double alpha, beta;
     int semantics;
     int splits; int64_t kchunk;           // split-K
+    int want_splits;                      // requested split count (0: the planner's choice)
     void *part;                           // splits x rows x NB partials (split-K only)
     void *wpieces;                        // BF16 pieces of W (tensor-core form only)
 };
@@ -622,6 +623,7 @@ gb_status make_plan(SkParams &p, Plan &pl, bool allow_tc = true) {
         const int64_t nst = thin_tc_stages(p.K, classes);
         int splits = 1;
         while (pl.rtiles * splits < 4 * (int64_t)sm_count() && nst / (splits * 2) >= 8 && splits < 64) splits *= 2;
+        if (p.want_splits > 0) splits = p.want_splits;
         const int64_t cst = ceil_div(nst, splits);
         p.kchunk = cst * 64;
         p.splits = (int)ceil_div(nst, cst);
@@ -642,6 +644,7 @@ gb_status make_plan(SkParams &p, Plan &pl, bool allow_tc = true) {
         // split K until there are ~6 units per SM (tail balance of the persistent grid)
         int splits = 1;
         while (pl.rtiles * splits < 6 * (int64_t)sm_count() && nkb / (splits * 2) >= 16 && splits < 64) splits *= 2;
+        if (p.want_splits > 0) splits = p.want_splits;
         const int64_t ckb = ceil_div(nkb, splits);
         p.kchunk = ckb * thin::BK;
         p.splits = (int)ceil_div(nkb, ckb);
@@ -659,6 +662,7 @@ gb_status make_plan(SkParams &p, Plan &pl, bool allow_tc = true) {
     const int64_t target = 2 * (int64_t)sm_count();
     int splits = 1;
     while (pl.rtiles * splits < target && p.K / (splits * 2) >= 256 && splits < 64) splits *= 2;
+    if (p.want_splits > 0) splits = p.want_splits;
     p.kchunk = ceil_div(ceil_div(p.K, splits), gran) * gran;
     p.splits = (int)ceil_div(p.K, p.kchunk);
     if (p.splits < 1) p.splits = 1;
@@ -854,6 +858,7 @@ gb_status dispatch(const GemmArgs &g) {
     SkParams p{};
     set_roles(p, g.ta, g.tb, g.M, g.N, g.A, g.lda, g.B, g.ldb, g.ldc);
     p.K = g.K; p.C = g.C; p.alpha = g.alpha; p.beta = g.beta; p.semantics = g.semantics;
+    p.want_splits = g.split_k;
     if (p.n > 64) return set_status(GB_ERR_UNSUPPORTED, "skinny: small dimension %lld > 64",
                                     (long long)(g.M < g.N ? g.M : g.N));
     if (sizeof(T) == 8 && thin_oz_eligible(p.tx, p.ldx, p.X, p.rows, p.K)) {
@@ -862,6 +867,7 @@ gb_status dispatch(const GemmArgs &g) {
         const int64_t rtiles = ceil_div(p.rows, 128), nchunks = ceil_div(p.K, 512);
         int splits = 1;
         while (rtiles * splits < 4 * (int64_t)sm_count() && nchunks / (splits * 2) >= 2 && splits < 64) splits *= 2;
+        if (g.split_k > 0) splits = g.split_k;
         const int64_t cpc = ceil_div(nchunks, splits);
         splits = (int)ceil_div(nchunks, cpc);
         void *ws = workspace(thin_oz_workspace_bytes(p.rows, p.K, p.n, splits), g.stream);

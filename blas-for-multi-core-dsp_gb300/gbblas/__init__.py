@@ -46,7 +46,12 @@ class GemmOpts(ctypes.Structure):
     _fields_ = [("stream", ctypes.c_void_p), ("algo", ctypes.c_int32), ("semantics", ctypes.c_int32),
                 ("k_block", ctypes.c_int32), ("k_slab", ctypes.c_int32), ("alpha_on_b", ctypes.c_int32),
                 ("ozaki_slices", ctypes.c_int32), ("target_err", ctypes.c_double),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("accum_k", ctypes.c_int32), ("split_k", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+
+
+class TuneChoice(ctypes.Structure):
+    _fields_ = [("algo", ctypes.c_int32), ("accum_k", ctypes.c_int32), ("split_k", ctypes.c_int32),
+                ("ozaki_slices", ctypes.c_int32), ("ms", ctypes.c_double)]
 
 
 class GemmDesc(ctypes.Structure):
@@ -136,6 +141,9 @@ _SIGS = {
     "gb_autotune_gemm": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, ctypes.POINTER(_int),
                           ctypes.POINTER(_dbl)], _int),
     "gb_autotune_set": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, _int], _int),
+    "gb_autotune_gemm_ex": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, _dbl, _int, _vp,
+                             ctypes.POINTER(TuneChoice)], _int),
+    "gb_autotune_lookup": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, ctypes.POINTER(TuneChoice)], _int),
     "gb_autotune_get": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64], _int),
     "gb_autotune_save": ([ctypes.c_char_p], _int),
     "gb_autotune_load": ([ctypes.c_char_p], _int),
@@ -222,7 +230,7 @@ def sync(stream=None):
 
 
 def opts(algo=ALGO_AUTO, semantics=SEM_BLAS, stream=None, k_block=0, k_slab=0, alpha_on_b=0,
-         ozaki_slices=0, target_err=0.0):
+         ozaki_slices=0, target_err=0.0, accum_k=0, split_k=0):
     o = GemmOpts()
     lib().gb_gemm_opts_init(ctypes.byref(o))
     o.stream = _stream(stream)
@@ -233,6 +241,8 @@ def opts(algo=ALGO_AUTO, semantics=SEM_BLAS, stream=None, k_block=0, k_slab=0, a
     o.alpha_on_b = alpha_on_b
     o.ozaki_slices = ozaki_slices
     o.target_err = target_err
+    o.accum_k = accum_k
+    o.split_k = split_k
     return o
 
 
@@ -392,3 +402,19 @@ def autotune_gemm(bits, ta, tb, M, N, K):
     _check(lib().gb_autotune_gemm(bits, ta.encode(), tb.encode(), M, N, K, ctypes.byref(best), ctypes.byref(ms)),
            "gb_autotune_gemm")
     return best.value, ms.value
+
+
+def autotune_gemm_ex(bits, ta, tb, M, N, K, target_err=0.0, reps=5, stream=None):
+    """Search the candidates for the shape; returns the chosen TuneChoice as a dict."""
+    c = TuneChoice()
+    _check(lib().gb_autotune_gemm_ex(bits, ta.encode(), tb.encode(), M, N, K, target_err, reps, _stream(stream),
+                                     ctypes.byref(c)), "gb_autotune_gemm_ex")
+    return {name: getattr(c, name) for name, _ in TuneChoice._fields_}
+
+
+def autotune_lookup(bits, ta, tb, M, N, K):
+    """The bucket's TuneChoice as a dict, or None."""
+    c = TuneChoice()
+    if lib().gb_autotune_lookup(bits, ta.encode(), tb.encode(), M, N, K, ctypes.byref(c)) != OK:
+        return None
+    return {name: getattr(c, name) for name, _ in TuneChoice._fields_}

@@ -138,7 +138,14 @@ typedef struct gb_gemm_opts {
                               (2..9), 0 -> the fewest meeting target_err      */
     double  target_err;    /* OZAKI: normwise error target, 0 -> no worse
                               than native FP64 (8 slices)                     */
-    int32_t reserved[4];
+    int32_t accum_k;       /* BF16X3 / BF16X6 / FP16X3: restart the tensor-
+                              memory accumulator every accum_k values of K
+                              (rounded up to 32) and sum the parts in FP32
+                              registers; 0 -> the form's default (FP16X3 128,
+                              BF16X6 256, BF16X3 never); < 0 -> never         */
+    int32_t split_k;       /* SKINNY: number of K ranges computed apart and
+                              summed (split-K); 0 -> the planner's choice     */
+    int32_t reserved[2];
 } gb_gemm_opts;
 
 /* Fill *opts with defaults (AUTO, BLAS, NULL stream). */
@@ -341,15 +348,45 @@ gb_status gb_server_drain(gb_server *s, double timeout_s);
 gb_status gb_server_get_stats(gb_server *s, gb_server_stats *out);
 void      gb_server_destroy(gb_server *s);
 
-/* Autotuner: time the candidate algorithms for a GEMM shape on scratch
- * operands and record the fastest for its (dtype, modes, log2 M, log2 N,
- * log2 K) bucket; GB_ALGO_AUTO requests through the server use the table.
- * FP32 candidates: SIMT, BF16X3 (K >= 64), SKINNY (min(M,N) <= 64); FP64:
- * ORDERED, OZAKI (slices for FP64-level error), SKINNY. */
+/* Autotuner.  No reference counterpart; the reference's tuning surface is
+ * its per-mode blocking constants (sgemm_release_V1.3.2/device_code/
+ * sgemm_kernel.c:2480-2493, the K_A / K_G table of
+ * dgemm_release_V1.1/readme.txt:17-24, the r6c96 / r6c128 switch at
+ * sgemm_kernel.c:14-15).  A choice is an algorithm and its knobs; the table
+ * keeps one per (dtype, modes, log2 M, log2 N, log2 K) bucket, and
+ * GB_ALGO_AUTO requests through the server use it. */
+typedef struct gb_tune_choice {
+    int32_t algo;          /* gb_algo                                         */
+    int32_t accum_k;       /* as gb_gemm_opts.accum_k                         */
+    int32_t split_k;       /* as gb_gemm_opts.split_k                         */
+    int32_t ozaki_slices;  /* as gb_gemm_opts.ozaki_slices                    */
+    double  ms;            /* median time of one call when it was measured    */
+} gb_tune_choice;
+
+/* Time every candidate for the shape on scratch operands (U[-1,1]) on
+ * `stream` -- one warm-up call, then `reps` (>= 5; 0 -> 5) timed calls,
+ * median taken, measured again when the spread of a candidate exceeds 30 % --
+ * and record the fastest.  Candidates: FP32: SIMT, BF16X3 (K >= 64), FP16X3
+ * with accumulator chunks of 128 and 256, BF16X6, and SKINNY (min(M, N) <=
+ * 64) with the planner's split-K and 1, 4 and 16 splits; FP64: ORDERED,
+ * DMMA, OZAKI with the fewest slices for `target_err` (0: no worse than
+ * native FP64) and one more, SKINNY (min(M, N) <= 64).  Every FP32 candidate
+ * meets the 2*K*u32 normwise bound; OZAKI meets target_err.  Synchronises
+ * `stream`. */
+gb_status gb_autotune_gemm_ex(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
+                              double target_err, int reps, void *stream, gb_tune_choice *best);
+/* The same with reps 5, target_err 0, the legacy default stream. */
 gb_status gb_autotune_gemm(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
                            int *best_algo, double *best_ms);
+/* Set a bucket's algorithm (knobs at their defaults) / read the full choice
+ * of a bucket (returns GB_ERR_INVALID_ARG when the bucket has none). */
 gb_status gb_autotune_set(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K, int algo);
+gb_status gb_autotune_lookup(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
+                             gb_tune_choice *out);
+/* The bucket's algorithm, -1 when the table has none. */
 int       gb_autotune_get(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K);
+/* Text file, one bucket per line: bits ta tb log2M log2N log2K algo accum_k split_k slices ms
+ * (files with only the first seven columns load too). */
 gb_status gb_autotune_save(const char *path);
 gb_status gb_autotune_load(const char *path);
 

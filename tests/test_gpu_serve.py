@@ -183,10 +183,91 @@ def test_server_results_same_alone_and_in_mix(torch, grouped, graphs, streams):
 def test_autotune_picks_a_working_algorithm(torch):
     import gbblas
     best, ms = gbblas.autotune_gemm(32, "N", "N", 1024, 1024, 1024)
-    assert best in (gbblas.ALGO_SIMT, gbblas.ALGO_BF16X3) and ms > 0
+    assert best in (gbblas.ALGO_SIMT, gbblas.ALGO_BF16X3, gbblas.ALGO_FP16X3, gbblas.ALGO_BF16X6) and ms > 0
     assert gbblas.lib().gb_autotune_get(32, b"N", b"N", 1024, 1024, 1024) == best
     best64, _ = gbblas.autotune_gemm(64, "N", "N", 600, 600, 600)
-    assert best64 in (gbblas.ALGO_ORDERED, gbblas.ALGO_OZAKI)
+    assert best64 in (gbblas.ALGO_ORDERED, gbblas.ALGO_OZAKI, gbblas.ALGO_DMMA)
+
+
+@pytest.mark.parametrize("bits,mode,M,N,K,target", [(32, "NT", 2048, 1536, 1024, 0.0), (64, "NN", 1024, 768, 2048, 1e-12),
+                                                     (64, "TN", 1024, 1024, 1024, 0.0), (32, "TN", 16, 30000, 4096, 0.0),
+                                                     (64, "NN", 40000, 24, 2048, 0.0)])
+def test_autotune_ex_choice_runs_within_its_bound(torch, bits, mode, M, N, K, target):
+    """The tuner's choice (algorithm and knobs) is stored for the bucket, was
+    timed on the stream given, and computes the product within 2*K*u (or the
+    Ozaki target) when run through the server on fresh inputs."""
+    import gbblas
+    tc = torch
+    s = tc.cuda.Stream()
+    ta, tb = mode
+    c = gbblas.autotune_gemm_ex(bits, ta, tb, M, N, K, target_err=target, reps=5, stream=s)
+    assert c["ms"] > 0
+    assert gbblas.autotune_lookup(bits, ta, tb, M, N, K) == c
+    dtype = np.float64 if bits == 64 else np.float32
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A = oracle.fill(ar, ac, 201, dtype=dtype)
+    B = oracle.fill(br, bc, 202, dtype=dtype)
+    C0 = oracle.fill(M, N, 203, dtype=dtype)
+    dA, dB, dC = dev(A), dev(B), dev(C0)
+    with gbblas.Server(streams=2) as srv:
+        srv.submit(gbblas.request(gbblas.OP_GEMM, bits, M, N, K, dA, ac, dB, bc, dC, N, ta=ta, tb=tb, alpha=0.5,
+                                  beta=-1.0, tag=1))
+        srv.drain(60.0)
+    rows = np.arange(0, M, max(1, M // 64))
+    cols = np.arange(0, N, max(1, N // 64))
+    err, _ = oracle.normwise_error(host(dC), ta, tb, M, N, K, 0.5, A, ac, B, bc, -1.0, C0, N, rows, cols)
+    u = 2.0 ** -53 if bits == 64 else 2.0 ** -24
+    bound = target if (bits == 64 and target > 0 and c["algo"] == gbblas.ALGO_OZAKI) else 2 * K * u
+    assert err <= bound, (c, err)
+
+
+@pytest.mark.parametrize("split", [1, 3, 16])
+@pytest.mark.parametrize("bits", [32, 64])
+def test_skinny_split_k_override(torch, split, bits):
+    """split_k overrides the planner's split-K: every count gives the product
+    within 2*K*u (thinB and shortA)."""
+    import gbblas
+    dtype = np.float64 if bits == 64 else np.float32
+    u = 2.0 ** -53 if bits == 64 else 2.0 ** -24
+    for M, N, mode in ((6000, 12, "NN"), (24, 5000, "TT")):
+        K = 9000
+        ta, tb = mode
+        ar, ac = op_shape(ta, M, K)
+        br, bc = op_shape(tb, K, N)
+        A = oracle.fill(ar, ac, 211, dtype=dtype)
+        B = oracle.fill(br, bc, 212, dtype=dtype)
+        C0 = oracle.fill(M, N, 213, dtype=dtype)
+        dC = dev(C0)
+        gbblas.gemm(ta, tb, M, N, K, 1.0, dev(A), ac, dev(B), bc, 0.5, dC, N, bits, algo=gbblas.ALGO_SKINNY,
+                    split_k=split)
+        rows = np.arange(0, M, max(1, M // 50))
+        cols = np.arange(0, N, max(1, N // 50))
+        err, _ = oracle.normwise_error(host(dC), ta, tb, M, N, K, 1.0, A, ac, B, bc, 0.5, C0, N, rows, cols)
+        assert err <= 2 * K * u, (mode, split, err)
+
+
+@pytest.mark.parametrize("algo_name,accum", [("FP16X3", 32), ("FP16X3", 512), ("FP16X3", -1), ("BF16X3", 256),
+                                             ("BF16X6", -1), ("BF16X6", 128)])
+def test_accum_k_knob(torch, algo_name, accum):
+    """accum_k sets the accumulator chunk of the tensor-core SGEMM forms: exact
+    on small integers, within 2*K*u32 on U[-1,1]."""
+    import gbblas
+    algo = getattr(gbblas, "ALGO_" + algo_name)
+    M, N, K = 640, 520, 1500
+    rng = np.random.default_rng(214)
+    A = rng.integers(-8, 9, size=(M, K)).astype(np.float32)
+    B = rng.integers(-8, 9, size=(K, N)).astype(np.float32)
+    dC = dev(np.zeros((M, N), np.float32))
+    gbblas.sgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=algo, accum_k=accum)
+    assert np.array_equal(host(dC), (A.astype(np.float64) @ B.astype(np.float64)).astype(np.float32))
+    A = oracle.fill(M, K, 215, dtype=np.float32)
+    B = oracle.fill(K, N, 216, dtype=np.float32)
+    dC = dev(np.zeros((M, N), np.float32))
+    gbblas.sgemm("N", "N", M, N, K, 1.0, dev(A), K, dev(B), N, 0.0, dC, N, algo=algo, accum_k=accum)
+    err, _ = oracle.normwise_error(host(dC), "N", "N", M, N, K, 1.0, A, K, B, N, 0.0, None, N,
+                                   np.arange(0, M, 5), np.arange(0, N, 5))
+    assert err <= 2 * K * 2.0 ** -24 + (3 * 2.0 ** -17 if algo_name == "BF16X3" else 0), err
 
 
 def test_strided_batched_matches_single_calls(torch):

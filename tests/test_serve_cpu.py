@@ -90,6 +90,35 @@ def test_autotune_table_roundtrip(L, tmp_path):
     assert L.gb_autotune_set(32, b"N", b"T", 1, 1, 1, 99) == gbblas.ERR_INVALID_ARG
 
 
+def test_autotune_choice_file_keeps_knobs(L, tmp_path):
+    """A saved choice carries its knobs (accumulator chunk, split-K, slices);
+    a file with only the seven legacy columns still loads."""
+    path = tmp_path / "tune.txt"
+    path.write_text("# bits ta tb log2M log2N log2K algo accum_k split_k slices ms\n"
+                    "32 0 1 12 12 12 8 256 0 0 0.41\n"
+                    "64 0 0 10 10 12 5 0 0 7 1.5\n"
+                    "32 1 0 4 18 12 6 0 16 0 0.2\n"
+                    "64 1 1 11 11 11 3\n")
+    assert L.gb_autotune_load(str(path).encode()) == gbblas.OK
+    c = gbblas.autotune_lookup(32, "N", "T", 4096, 4096, 4096)
+    assert c["algo"] == gbblas.ALGO_FP16X3 and c["accum_k"] == 256 and abs(c["ms"] - 0.41) < 1e-9
+    c = gbblas.autotune_lookup(64, "N", "N", 1024, 1024, 4096)
+    assert c["algo"] == gbblas.ALGO_OZAKI and c["ozaki_slices"] == 7
+    c = gbblas.autotune_lookup(32, "T", "N", 16, 262144, 4096)
+    assert c["algo"] == gbblas.ALGO_SKINNY and c["split_k"] == 16
+    assert gbblas.autotune_lookup(64, "T", "T", 2048, 2048, 2048)["algo"] == gbblas.ALGO_DMMA
+    assert gbblas.autotune_lookup(64, "T", "T", 7, 7, 7) is None
+    out = tmp_path / "again.txt"
+    assert L.gb_autotune_save(str(out).encode()) == gbblas.OK
+    assert "32 1 0 4 18 12 6 0 16 0" in out.read_text()
+
+
+def test_gemm_rejects_bad_split_k(L):
+    o = gbblas.opts(algo=gbblas.ALGO_SKINNY, split_k=65)
+    st = L.gb_sgemm(b"N", b"N", 100, 8, 100, 1.0, 16, 100, 32, 8, 0.0, 48, 8, ctypes.byref(o))
+    assert st == gbblas.ERR_INVALID_ARG
+
+
 def test_gemm_batch_rejects_bad_descriptors(L):
     d = gbblas.gemm_desc("N", "N", 8, 8, 8, 1.0, 16, 4, 32, 8, 0.0, 48, 8, 32)   # lda < K
     arr = (gbblas.GemmDesc * 1)(d)
