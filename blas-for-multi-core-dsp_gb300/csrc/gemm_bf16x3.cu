@@ -151,22 +151,21 @@ __device__ __forceinline__ float scale_line(float x, int s) {
     return s > 127 ? (x * pow2f(127)) * pow2f(s - 127) : x * pow2f(s);
 }
 
-// x * 2^k for |k| <= 378: one exact multiply in the normal range, else
-// factors applied largest first (only a result outside the normal range rounds)
+// x * 2^k, branch-free, as two factors in the normal range applied largest
+// first: exact while the result is normal, and for k in [-252, 254] the
+// product of the factors is 2^k; the epilogue's k lies in [-326, 226] and
+// below -252 the result underflows to zero either way (|x| < 2^62).
 __device__ __forceinline__ float mul_pow2f(float x, int k) {
-    if (k >= -126 && k <= 127) return x * pow2f(k);
     const int a = max(-126, min(127, k));
-    k -= a;
-    const int b = max(-126, min(127, k));
-    k -= b;
-    return x * pow2f(a) * pow2f(b) * pow2f(max(-126, min(127, k)));
+    const int b = max(-126, min(127, k - a));
+    return x * pow2f(a) * pow2f(b);
 }
 
 // Plain FP32 dot product of row i of op(A) and column j of op(B), in k order:
 // the outputs whose line holds an Inf or a NaN, so that those propagate as
 // IEEE arithmetic has them.
-__device__ __noinline__ float dot_f32_cold(const float *A, int64_t lda, int ta, int64_t i, const float *B, int64_t ldb,
-                                           int tb, int64_t j, int64_t K) {
+__device__ __forceinline__ float dot_f32_cold(const float *A, int64_t lda, int ta, int64_t i, const float *B,
+                                              int64_t ldb, int tb, int64_t j, int64_t K) {
     float s = 0.f;
     for (int64_t k = 0; k < K; k++) {
         const float a = ta ? A[k * lda + i] : A[i * lda + k];
@@ -564,7 +563,7 @@ __device__ __forceinline__ float epi_value(const EpiParams &p, float x, float ci
 
 // The output (row, col) from a plain FP32 dot product (its row of op(A) or
 // column of op(B) holds an Inf or a NaN), written with the epilogue.
-__device__ __noinline__ void store_recomputed(const EpiParams &p, int64_t row, int64_t col) {
+__device__ __forceinline__ void store_recomputed(const EpiParams &p, int64_t row, int64_t col) {
     const float x = dot_f32_cold(p.A, p.lda, p.ta, row, p.B, p.ldb, p.tb, col, p.K);
     float *c = p.C + row * p.ldc + col;
     *c = epi_value(p, x, reads_c(p) ? *c : 0.f);
@@ -802,23 +801,19 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
             }
         }
     } else {   // EW == 8: two warps per TMEM lane quarter, 128 columns each
-        const int q = warp % 4, hc = (warp - 2) / 4, wi = warp - 2;
-        int *cs_w = col_scale + wi * 128;   // F16: the scales of this warp's 128 columns ...
-        int *rs_w = row_scale + wi * 32;    // ... and 32 rows
-        float *stg = epi + wi * 32 * 17;    // 32 rows x 16 columns, padded
-        const uint32_t lane_off = (uint32_t)(q * 32) << 16;
-        const bool rc = reads_c(p);
-        const int cl = lane & 15, rh = lane >> 4;   // this lane's column and row parity when storing
+        // Registers: the 128 running totals and 16 columns in flight leave ~24 of the 168 for
+        // everything else, so only the tile index and chunk counter stay live across the fold;
+        // coordinates and pointers are recomputed after it.
         int ch = 0;
         float total[128];
         bool go = true;
         int it = 0, t, half;
         while (go && next_item(p, num_tiles, it, t, half)) {
-            int tm, tn;
-            tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
-            const int64_t row0 = (int64_t)tm * BM + q * 32;
-            const int64_t c0 = (int64_t)tn * BN + hc * 128;
             if (F16) {   // the scales of the warp's rows and columns, once per tile
+                int tm, tn;
+                tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+                const int64_t row0 = (int64_t)tm * BM + (warp % 4) * 32;
+                const int64_t c0 = (int64_t)tn * BN + ((warp - 2) / 4) * 128;
                 unsigned cb[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
@@ -826,32 +821,45 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                     cb[j] = col < p.N ? p.colbits[col] : 0u;
                 }
                 const unsigned rb = row0 + lane < p.M ? p.rowbits[row0 + lane] : 0u;
+                int *cs_w = col_scale + (warp - 2) * 128;
                 __syncwarp();   // the previous tile's reads of the scales are done
 #pragma unroll
                 for (int j = 0; j < 4; j++) cs_w[lane + 32 * j] = f16_line_scale(cb[j]);
-                rs_w[lane] = f16_line_scale(rb);
+                row_scale[(warp - 2) * 32 + lane] = f16_line_scale(rb);
                 __syncwarp();
             }
 #pragma unroll
             for (int j = 0; j < 128; j++) total[j] = 0.f;
-            for (int c = 0; c < (p.num_kb + chunk_kb - 1) / chunk_kb; c++, ch++) {
+            const int nch = (p.num_kb + chunk_kb - 1) / chunk_kb;
+            for (int c = 0; c < nch; c++, ch++) {
                 const int b = ch & 1;
                 if (!ptx::mbar_wait(&acc_full[b], (ch >> 1) & 1, p.err, 4)) { go = false; break; }
                 ptx::tc_fence_after();
-                const uint32_t a0 = tmem + (uint32_t)(b * ACC_COLS) + lane_off + (uint32_t)(hc * 128);
+                const uint32_t a0 = tmem + (uint32_t)(b * ACC_COLS) + ((uint32_t)((warp % 4) * 32) << 16) +
+                                    (uint32_t)(((warp - 2) / 4) * 128);
 #pragma unroll
-                for (int g = 0; g < 4; g++) {   // 32 columns per load (128 totals + 32 in flight: 168 registers)
-                    uint32_t r[32];
-                    ptx::tmem_ld_32x32b_x32(a0 + (uint32_t)(g * 32), r);
+                for (int g = 0; g < 8; g++) {   // 16 columns per load
+                    uint32_t r[16];
+                    ptx::tmem_ld_32x32b_x16(a0 + (uint32_t)(g * 16), r);
                     ptx::tmem_ld_wait();
 #pragma unroll
-                    for (int j = 0; j < 32; j++) total[g * 32 + j] += __uint_as_float(r[j]);
+                    for (int j = 0; j < 16; j++) total[g * 16 + j] += __uint_as_float(r[j]);
                 }
                 ptx::tc_fence_before();
                 __syncwarp();
                 if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
             }
             if (!go) break;
+            int tm, tn;
+            tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+            const int wi = warp - 2;
+            const int64_t row0 = (int64_t)tm * BM + (warp % 4) * 32;
+            const int64_t c0 = (int64_t)tn * BN + (wi / 4) * 128;
+            const int *cs_w = col_scale + wi * 128;
+            const int *rs_w = row_scale + wi * 32;
+            float *stg = epi + wi * 32 * 17;
+            const bool rc = reads_c(p);
+            const int cl = lane & 15, rh = lane >> 4;   // this lane's column and row parity when storing
             // C in passes of 16 columns through shared memory: lane l holds row l's totals; after
             // the transpose lane l takes column l % 16 of rows l / 16, l / 16 + 2, ..., so each
             // load / store instruction covers two 64-byte row segments
@@ -866,23 +874,26 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 const bool colok = col < p.N;
                 const int cs = F16 ? cs_w[16 * ps + cl] : 0;
                 float *cp = p.C + (row0 + rh) * p.ldc + col;
-                float cin[16];
 #pragma unroll
-                for (int i = 0; i < 16; i++)
-                    cin[i] = (rc && colok && 2 * i + rh < rows_left) ? cp[(int64_t)(2 * i) * p.ldc] : 0.f;
+                for (int i8 = 0; i8 < 16; i8 += 8) {   // C loads eight at a time
+                    float cin[8];
 #pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    const int rr = 2 * i + rh;
-                    float x = stg[rr * 17 + cl];
-                    bool skip = false;
-                    if (F16) {
-                        const int sr = rs_w[rr];
-                        skip = sr == kNonFiniteScale || cs == kNonFiniteScale;
-                        x = mul_pow2f(x, -(sr + cs));
-                    }
-                    if (colok && rr < rows_left) {
-                        if (skip) nf = true;
-                        else cp[(int64_t)(2 * i) * p.ldc] = epi_value(p, x, cin[i]);
+                    for (int i = i8; i < i8 + 8; i++)
+                        cin[i - i8] = (rc && colok && 2 * i + rh < rows_left) ? cp[(int64_t)(2 * i) * p.ldc] : 0.f;
+#pragma unroll
+                    for (int i = i8; i < i8 + 8; i++) {
+                        const int rr = 2 * i + rh;
+                        float x = stg[rr * 17 + cl];
+                        bool skip = false;
+                        if (F16) {
+                            const int sr = rs_w[rr];
+                            skip = sr == kNonFiniteScale || cs == kNonFiniteScale;
+                            x = mul_pow2f(x, -(sr + cs));
+                        }
+                        if (colok && rr < rows_left) {
+                            if (skip) nf = true;
+                            else cp[(int64_t)(2 * i) * p.ldc] = epi_value(p, x, cin[i - i8]);
+                        }
                     }
                 }
                 __syncwarp();
