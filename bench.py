@@ -1102,6 +1102,8 @@ def run_serve(ctx):
                 "mean_ms": st["mean_s"] * 1e3, "req_per_s": st["req_per_s"], "completed": st["completed"],
                 "submitted": st["submitted"], "failed": st["failed"], "launches": st["launches"],
                 "grouped_launches": st["grouped_launches"], "grouped_requests": st["grouped_requests"],
+                "graph_launches": st["graph_launches"], "graph_instantiations": st["graph_instantiations"],
+                "graph_fraction": st["graph_launches"] / st["launches"] if st["launches"] else 0.0,
                 "drained": drained, "submit_lag_s": lag, "submit_span_s": submit_end}
 
     l0 = gb.launch_count()

@@ -195,6 +195,7 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
 
 gb_status launch_skinny_f32(const GemmArgs &g);
 gb_status launch_skinny_f64(const GemmArgs &g);
+size_t skinny_workspace_bytes(const GemmArgs &g, int bits);   // what launch_skinny_* takes; launches nothing
 // C = beta*C (beta==0: C = 0) or C = C + beta (scalar) epilogue-only path (K == 0)
 gb_status launch_gemm_k0_f32(const GemmArgs &g);
 gb_status launch_gemm_k0_f64(const GemmArgs &g);

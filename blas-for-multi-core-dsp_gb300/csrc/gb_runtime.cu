@@ -114,6 +114,14 @@ void *workspace(size_t bytes, void *stream) {
     for (auto &e : g_ws)
         if (e.dev == dev && e.stream == stream) w = &e;
     if (w && w->size >= bytes) return w->ptr;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(as_stream(stream), &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone) {
+        // growing would synchronise and free under the capture: the caller reserves first
+        set_status(GB_ERR_INVALID_ARG, "workspace: %zu bytes not reserved before the stream capture began (%zu held)",
+                   bytes, w ? w->size : (size_t)0);
+        return nullptr;
+    }
+    cudaGetLastError();
     if (w && w->ptr) {
         // the old buffer may still be read by work queued on its stream
         cudaStreamSynchronize(as_stream(stream));

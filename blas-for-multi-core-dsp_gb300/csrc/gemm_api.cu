@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include "gb_common.cuh"
+#include "gb_internal.h"
 
 namespace gb {
 namespace {
@@ -136,6 +137,42 @@ gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alph
 }
 
 }  // namespace
+
+int resolve_algo(int bits, int algo, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
+    return algo == GB_ALGO_AUTO ? pick(bits, ta, tb, M, N, K) : algo;
+}
+
+size_t gemm_workspace_bound(int bits, int algo, bool ta, bool tb, int64_t M, int64_t N, int64_t K, const void *A,
+                            int64_t lda, const void *B, int64_t ldb, int slices, int split_k) {
+    algo = resolve_algo(bits, algo, ta, tb, M, N, K);
+    if (M <= 0 || N <= 0 || K <= 0) return 0;
+    switch (algo) {
+        case GB_ALGO_BF16X3:
+        case GB_ALGO_BF16X6:
+        case GB_ALGO_FP16X3: {   // two halves of pieces (up to three 16-bit pieces per operand) + line maxima
+            const int64_t kp = ceil_div(K, 64) * 64;
+            return 2 * ((size_t)3 * (M + N) * kp * 2 + (size_t)(M + N) * 4 + 1024) + 4096;
+        }
+        case GB_ALGO_SKINNY: {   // the skinny plan's own figure
+            GemmArgs g;
+            g.ta = ta; g.tb = tb; g.M = M; g.N = N; g.K = K;
+            g.A = A; g.lda = lda; g.B = B; g.ldb = ldb; g.C = nullptr; g.ldc = N;
+            g.split_k = split_k;
+            return skinny_workspace_bytes(g, bits);
+        }
+        case GB_ALGO_OZAKI: {   // slices of both operands (K cut into chunks past 4 GiB) + exponents
+            const int s = slices > 0 ? slices : ozaki_pick_slices(0.0, K);
+            const int64_t kp = ceil_div(K, 64) * 64, mp = ceil_div(M, 128) * 128, np = ceil_div(N, 128) * 128;
+            double v = (double)s * (double)(mp + np) * (double)kp * 2.0;
+            const double cap = 4.0 * (1ull << 30) + (double)s * (mp + np) * 1024 * 2.0;
+            if (v > cap) v = cap;
+            return (size_t)v + (size_t)(mp + np) * 4 + 8192;
+        }
+        default:
+            return 0;
+    }
+}
+
 }  // namespace gb
 
 extern "C" {

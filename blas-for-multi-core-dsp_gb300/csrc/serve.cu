@@ -22,11 +22,13 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
 #include <map>
 #include <mutex>
+#include <set>
 #include <thread>
 #include <tuple>
 #include <vector>
@@ -81,6 +83,16 @@ struct Pending {
 
 struct Batch;   // completion context of one launch
 
+// Bucket of a one-launch request's graph: requests of one bucket usually launch the same kernels,
+// so the cached executable graph is updated in place (cudaGraphExecUpdate) instead of rebuilt.
+struct GKey {
+    int op, bits, ta, tb, algo, lm, ln, lk, li;
+    bool operator<(const GKey &o) const {
+        return std::tie(op, bits, ta, tb, algo, lm, ln, lk, li) <
+               std::tie(o.op, o.bits, o.ta, o.tb, o.algo, o.lm, o.ln, o.lk, o.li);
+    }
+};
+
 }  // namespace
 
 struct Server {
@@ -96,6 +108,10 @@ struct Server {
     std::vector<uint64_t> done_tags;
     std::vector<double> done_lat;
     std::vector<cudaStream_t> streams;
+    std::vector<size_t> ws_reserved;                          // workspace reserved per stream
+    std::vector<std::map<GKey, cudaGraphExec_t>> execs;       // one-launch graphs per stream
+    std::set<GKey> seen;                                      // buckets that ran once without a graph
+    std::atomic<int64_t> graph_launches{0}, graph_instantiations{0};
     size_t rr = 0;
     GroupRunner *grouped = nullptr;
     std::thread dispatcher;
@@ -208,6 +224,84 @@ gb_status launch_one(Server *s, const gb_request &r, cudaStream_t st) {
     return gb_stencil2d_f32(r.M, r.N, (float *)r.A, (float *)r.C, r.iters, r.order, st);
 }
 
+// A one-launch request through a CUDA graph: its launches are captured on the stream (after the
+// stream's workspace has been grown to the request's bound, since a capture cannot allocate) and
+// replayed by the bucket's executable graph, updated in place when the launches match.  Anything
+// that cannot be captured runs as plain launches.
+gb_status launch_request(Server *s, const gb_request &r, size_t si, bool *graphed) {
+    cudaStream_t st = s->streams[si];
+    *graphed = false;
+    if (!s->cfg.use_graphs) return launch_one(s, r, st);
+    int algo = r.algo, slices = 0, split_k = 0;
+    const bool ta = is_trans(r.transA), tb = is_trans(r.transB);
+    if (r.op == GB_OP_GEMM) {
+        gb_tune_choice t;
+        if (algo == GB_ALGO_AUTO && tuned_choice(r.dtype_bits, ta, tb, r.M, r.N, r.K, &t)) {
+            algo = t.algo;
+            slices = t.ozaki_slices;
+            split_k = t.split_k;
+        }
+        algo = resolve_algo(r.dtype_bits, algo, ta, tb, r.M, r.N, r.K);
+    }
+    const GKey key{r.op, r.dtype_bits, ta ? 1 : 0, tb ? 1 : 0, algo, lg(r.M), lg(r.N), lg(r.K), lg(r.iters)};
+    // The first request of a bucket runs as plain launches: it loads the kernels and sets their
+    // attributes outside any capture, and a shape seen once builds no graph.
+    if (s->seen.insert(key).second) return launch_one(s, r, st);
+    const size_t need =
+        r.op == GB_OP_GEMM ? gemm_workspace_bound(r.dtype_bits, algo, ta, tb, r.M, r.N, r.K, r.A, r.lda, r.B, r.ldb,
+                                                  slices, split_k)
+                           : 0;
+    if (need > s->ws_reserved[si]) {
+        const size_t want = std::max(need, 2 * s->ws_reserved[si]);
+        if (gb_workspace_reserve(want, st) != GB_OK) {
+            gb_clear_last_status();
+            return launch_one(s, r, st);
+        }
+        s->ws_reserved[si] = want;
+    }
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return launch_one(s, r, st);
+    }
+    const gb_status rc = launch_one(s, r, st);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (rc != GB_OK || ce != cudaSuccess || g == nullptr) {   // not capturable: plain launches
+        cudaGetLastError();
+        gb_clear_last_status();
+        if (g) cudaGraphDestroy(g);
+        return launch_one(s, r, st);
+    }
+    auto &cache = s->execs[si];
+    cudaGraphExec_t ex = nullptr;
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(it->second, g, &info) == cudaSuccess) {
+            ex = it->second;
+        } else {   // other launches than the cached graph's: build a new one
+            cudaGetLastError();
+            cudaGraphExecDestroy(it->second);
+            cache.erase(it);
+        }
+    }
+    if (!ex) {
+        if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphDestroy(g);
+            return launch_one(s, r, st);
+        }
+        cache[key] = ex;
+        s->graph_instantiations++;
+    }
+    cudaGraphDestroy(g);
+    const cudaError_t le = cudaGraphLaunch(ex, st);
+    if (le != cudaSuccess) return cuda_status(le, "server: cudaGraphLaunch");
+    *graphed = true;
+    s->graph_launches++;
+    return GB_OK;
+}
+
 void dispatcher_main(Server *s) {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
@@ -247,9 +341,11 @@ void dispatcher_main(Server *s) {
                 group_reqs.push_back(p);
                 continue;
             }
-            cudaStream_t st = s->streams[s->rr++ % s->streams.size()];
+            const size_t si = s->rr++ % s->streams.size();
+            cudaStream_t st = s->streams[si];
             Batch *b = new Batch{s, {{p.r.tag, p.t_submit}}, p.bytes};
-            gb_status rc = s->cfg.dry_run ? GB_OK : launch_one(s, p.r, st);
+            bool graphed = false;
+            gb_status rc = s->cfg.dry_run ? GB_OK : launch_request(s, p.r, si, &graphed);
             if (rc != GB_OK) {
                 std::lock_guard<std::mutex> g(s->mu);
                 s->failed++;
@@ -279,6 +375,7 @@ void dispatcher_main(Server *s) {
             else cudaLaunchHostFunc(st, on_done, b);
             std::lock_guard<std::mutex> g(s->mu);
             s->launches++;
+            if (rc == GB_OK && s->cfg.use_graphs && !s->cfg.dry_run) s->graph_launches++;
             s->grouped_launches++;
             s->grouped_requests += (int64_t)group.size();
         }
@@ -336,6 +433,8 @@ gb_status gb_server_create(const gb_server_config *cfg, gb_server **out) {
                 return gb::cuda_status(e, "gb_server_create: stream");
             }
             s->streams.push_back(st);
+            s->ws_reserved.push_back(c.workspace_bytes);
+            s->execs.emplace_back();
             if (c.workspace_bytes) {
                 gb_status r = gb_workspace_reserve(c.workspace_bytes, st);
                 if (r != GB_OK) {
@@ -348,6 +447,8 @@ gb_status gb_server_create(const gb_server_config *cfg, gb_server **out) {
         s->grouped = gb::group_runner_create(2 * c.streams, c.max_batch);
     } else {
         s->streams.push_back(nullptr);
+        s->ws_reserved.push_back(0);
+        s->execs.emplace_back();
     }
     s->dispatcher = std::thread(gb::dispatcher_main, s);
     *out = reinterpret_cast<gb_server *>(s);
@@ -428,6 +529,8 @@ gb_status gb_server_get_stats(gb_server *sv, gb_server_stats *out) {
     out->launches = s->launches;
     out->grouped_launches = s->grouped_launches;
     out->grouped_requests = s->grouped_requests;
+    out->graph_launches = s->graph_launches.load();
+    out->graph_instantiations = s->graph_instantiations.load();
     out->p50_s = gb::percentile(s->latencies, 0.50);
     out->p99_s = gb::percentile(s->latencies, 0.99);
     out->mean_s = 0;
@@ -449,6 +552,8 @@ void gb_server_destroy(gb_server *sv) {
     if (s->dispatcher.joinable()) s->dispatcher.join();
     if (!s->cfg.dry_run) {
         for (auto st : s->streams) cudaStreamSynchronize(st);
+        for (auto &cache : s->execs)
+            for (auto &kv : cache) cudaGraphExecDestroy(kv.second);
         gb::group_runner_destroy(s->grouped);
         for (auto st : s->streams) cudaStreamDestroy(st);
     }

@@ -852,8 +852,20 @@ void set_roles(SkParams &p, bool ta, bool tb, int64_t M, int64_t N, const void *
     }
 }
 
+// The workspace run<T, NB> takes for the plan of p (bytes; 0 when the plan fails).
+template <typename T, int NB>
+size_t plan_bytes(SkParams p) {
+    Plan pl;
+    if (make_plan<T, NB>(p, pl) != GB_OK) return 0;
+    if (!pl.part_bytes && !pl.w_bytes) return 0;
+    return (pl.part_bytes + 255) / 256 * 256 + pl.w_bytes;
+}
+
+// need == nullptr: run the product.  Otherwise: store the workspace the run
+// would take in *need and launch nothing.
 template <typename T>
-gb_status dispatch(const GemmArgs &g) {
+gb_status dispatch(const GemmArgs &g, size_t *need = nullptr) {
+    if (need) *need = 0;
     if (g.M == 0 || g.N == 0) return ok();
     SkParams p{};
     set_roles(p, g.ta, g.tb, g.M, g.N, g.A, g.lda, g.B, g.ldb, g.ldc);
@@ -870,11 +882,20 @@ gb_status dispatch(const GemmArgs &g) {
         if (g.split_k > 0) splits = g.split_k;
         const int64_t cpc = ceil_div(nchunks, splits);
         splits = (int)ceil_div(nchunks, cpc);
+        if (need) {
+            *need = thin_oz_workspace_bytes(p.rows, p.K, p.n, splits);
+            return ok();
+        }
         void *ws = workspace(thin_oz_workspace_bytes(p.rows, p.K, p.n, splits), g.stream);
         if (!ws) return (gb_status)gb_get_last_status();
         return launch_thin_oz(p.rows, p.K, (const double *)p.X, p.ldx, p.tx, (const double *)p.W, p.ldw, p.tw, p.n,
                               (double *)p.C, p.cs_r, p.cs_c, p.alpha, p.beta, p.semantics, splits, cpc * 512, ws,
                               g.stream);
+    }
+    if (need) {
+        *need = p.n <= 8 ? plan_bytes<T, 8>(p) : p.n <= 16 ? plan_bytes<T, 16>(p)
+              : p.n <= 32 ? plan_bytes<T, 32>(p) : plan_bytes<T, 64>(p);
+        return ok();
     }
     if (p.n <= 8) return run<T, 8>(p, g.stream);
     if (p.n <= 16) return run<T, 16>(p, g.stream);
@@ -886,6 +907,12 @@ gb_status dispatch(const GemmArgs &g) {
 
 gb_status launch_skinny_f32(const GemmArgs &g) { return dispatch<float>(g); }
 gb_status launch_skinny_f64(const GemmArgs &g) { return dispatch<double>(g); }
+
+size_t skinny_workspace_bytes(const GemmArgs &g, int bits) {
+    size_t need = 0;
+    const gb_status st = bits == 64 ? dispatch<double>(g, &need) : dispatch<float>(g, &need);
+    return st == GB_OK ? need : 0;
+}
 
 }  // namespace gb
 

@@ -290,7 +290,8 @@ gb_status gb_stencil9_f64(int64_t M, int64_t N, double *A, double *B, int iters,
  * (FIFO; a request larger than the whole budget is rejected with
  * GB_ERR_OOM), small GEMMs admitted together run in one grouped launch
  * (replayed from CUDA graphs), the rest run one launch each with the
- * algorithm the autotune table picks, over a pool of streams.  Latency is
+ * algorithm the autotune table picks (captured into a CUDA graph per
+ * bucket and replayed), over a pool of streams.  Latency is
  * measured from submit to the completion callback on the stream.  No
  * reference counterpart (the reference host runs one kernel at a time). */
 typedef enum gb_op { GB_OP_GEMM = 0, GB_OP_TRANSPOSE = 1, GB_OP_STENCIL = 2 } gb_op;
@@ -322,7 +323,11 @@ typedef struct gb_server_config {
     int32_t  streams;           /* device streams (default 4)                         */
     int32_t  max_batch;         /* GEMMs per grouped launch (default 256)             */
     int32_t  max_inflight;      /* requests in flight at once (default 2^20)          */
-    int32_t  use_graphs;        /* replay grouped launches from CUDA graphs (1)       */
+    int32_t  use_graphs;        /* replay launches from CUDA graphs (1): grouped
+                                   launches per slot, one-launch requests per
+                                   (op, dtype, modes, algorithm, log2 sizes) bucket,
+                                   the stream's workspace grown to the request's
+                                   bound before each capture                         */
     int32_t  use_grouped;       /* group small GEMMs (1); 0 = one launch per request  */
     int32_t  dry_run;           /* admission and bookkeeping only, no device work     */
 } gb_server_config;
@@ -332,6 +337,8 @@ typedef struct gb_server_stats {
     uint64_t inflight_bytes;
     int64_t  launches, grouped_launches, grouped_requests;
     double   p50_s, p99_s, mean_s, req_per_s;
+    int64_t  graph_launches;        /* launches that replayed a CUDA graph (grouped and one-launch)    */
+    int64_t  graph_instantiations;  /* one-launch graphs built (the rest were cached graphs updated)   */
 } gb_server_stats;
 
 typedef struct gb_server gb_server;

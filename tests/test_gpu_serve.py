@@ -7,6 +7,8 @@
   in the mix as alone -- bit-identical for transpose and Jacobi and for GEMMs
   that take the same kernel, within the normwise GEMM tolerance otherwise --
   with grouping + CUDA graphs on and with one launch per request.
+* Server graphs for one-launch requests: the replays of a bucket's cached
+  (and in-place updated) graph give the bits of plain launches.
 """
 import numpy as np
 import pytest
@@ -140,7 +142,7 @@ def _result(it, d):
     return host(d["B"] if it["iters"] % 2 else d["A"])
 
 
-@pytest.mark.parametrize("grouped,graphs,streams", [(1, 1, 4), (0, 0, 1)])
+@pytest.mark.parametrize("grouped,graphs,streams", [(1, 1, 4), (0, 1, 3), (0, 0, 1)])
 def test_server_results_same_alone_and_in_mix(torch, grouped, graphs, streams):
     import gbblas
     rng = np.random.default_rng(11)
@@ -178,6 +180,51 @@ def test_server_results_same_alone_and_in_mix(torch, grouped, graphs, streams):
         assert e_mix <= 2 * K * u and e_alone <= 2 * K * u, (j, it["shape"], e_mix, e_alone)
         if not grouped:   # same kernel either way: identical bits
             assert mix.tobytes() == alone[j].tobytes(), j
+
+
+def _one_launch_items():
+    """Requests that run one launch each (no grouping): every GEMM route with
+    a workspace (3xBF16, FP16X3, BF16X6, Ozaki, skinny FP32 split-K, thin
+    FP64), plain SIMT / DMMA, transpose and Jacobi."""
+    import gbblas
+    reqs = [("gemm", 32, (1024, 1024, 1024), "NN"), ("gemm", 32, (640, 768, 1000), "TN"),
+            ("gemm", 32, (512, 512, 700), "NT"), ("gemm", 32, (300, 260, 500), "TT"),
+            ("gemm", 64, (700, 600, 800), "TN"), ("gemm", 64, (200, 220, 300), "NN"),
+            ("gemm", 32, (3000, 16, 20000), "NN"), ("gemm", 32, (8, 5000, 1500), "TT"),
+            ("gemm", 64, (2500, 8, 900), "NT"), ("transpose", 32, (700, 333), None),
+            ("transpose", 64, (257, 1030), None), ("stencil", 32, (300, 200), 17), ("stencil", 64, (129, 250), 4)]
+    algos = [gbblas.ALGO_AUTO, gbblas.ALGO_FP16X3, gbblas.ALGO_BF16X6, gbblas.ALGO_SIMT, gbblas.ALGO_AUTO,
+             gbblas.ALGO_DMMA, gbblas.ALGO_AUTO, gbblas.ALGO_AUTO, gbblas.ALGO_AUTO] + [gbblas.ALGO_AUTO] * 4
+    return _materialize(reqs), algos
+
+
+def test_server_one_launch_requests_replay_graphs_bit_identical(torch):
+    """Three requests of one bucket in a row, each on fresh buffers: the first
+    runs as plain launches, the second is captured and instantiated, the third
+    updates the cached graph in place.  All three give the bits one plain
+    launch gives, and the second and third are graph replays."""
+    import gbblas
+    items, algos = _one_launch_items()
+    for j, (it, algo) in enumerate(zip(items, algos)):
+        d = _device_set([it])[0]
+        with gbblas.Server(streams=1, use_grouped=0, use_graphs=0) as s:
+            r = _as_request(it, d, 0)
+            r.algo = algo
+            s.submit(r)
+            s.drain(60.0)
+            assert s.stats()["failed"] == 0
+        want = _result(it, d)
+        with gbblas.Server(streams=1, use_grouped=0, use_graphs=1) as s:
+            for rep in range(3):
+                d = _device_set([it])[0]
+                r = _as_request(it, d, rep)
+                r.algo = algo
+                s.submit(r)
+                s.drain(60.0)
+                assert _result(it, d).tobytes() == want.tobytes(), (j, it["kind"], it.get("shape"), rep)
+            st = s.stats()
+        assert st["failed"] == 0 and st["completed"] == 3
+        assert st["graph_launches"] == 2 and st["graph_instantiations"] == 1, (j, it["kind"], it.get("shape"), st)
 
 
 def test_autotune_picks_a_working_algorithm(torch):
