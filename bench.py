@@ -576,6 +576,19 @@ def run_sgemm(ctx):
 
     e2e, h2d, d2h = e2e_measure(ctx, step_host, max(1, min(args.steps, 5)), len(MODES) * flops, 1e12)
 
+    # the library's own per-call error report (gb_gemm_opts.err_out) of the headline form, after
+    # the timed region: 16 x 16 sample, Dot2 on the device
+    report = {}
+    rep = torch.zeros(1, dtype=torch.float64, device=ctx.dev)
+    for mode in MODES:
+        Cw = C0.clone()
+        A, B = ops(mode)
+        gb.sgemm(mode[0], mode[1], M, N, K, ALPHA, A, LD, B, LD, BETA, Cw, LD, algo=algo, stream=ctx.stream,
+                 err_out=rep)
+        torch.cuda.synchronize()
+        report[mode] = float(rep.item())
+    report["note"] = "gb_gemm_opts.err_out: 16 rows x 16 columns spread evenly, Dot2 on the device"
+
     kernel_tflops = flops / (kms * 1e-3) / 1e12
     if algo_name in products:
         npr = products[algo_name]
@@ -601,7 +614,8 @@ def run_sgemm(ctx):
     line = base_line(ctx, METRIC, value, "TFLOP/s", ms, args.steps, "f32", config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
                                            "d2h_bytes_per_step": d2h},
-                 "gpu_launches": launches, "clocks": clocks, "errors_normwise": errors, "compare": compare})
+                 "gpu_launches": launches, "clocks": clocks, "errors_normwise": errors, "err_report": report,
+                 "compare": compare})
     if ctx.rank == 0 and not args.no_cpu_baseline:
         v, nt, desc = cpu_sgemm_sample()
         line["cpu_baseline"] = {"value": v, "unit": "TFLOP/s", "cores": nt, "kind": "port", "sample": desc}

@@ -56,6 +56,8 @@ void *workspace(size_t bytes, void *stream);
 // between two halves of the buffer place them by *size, so that calls of
 // different sizes never overlap each other's half.
 void *workspace(size_t bytes, void *stream, unsigned *seq, size_t *size);
+// small per-stream scratch (>= 64 KB), separate from the workspace
+void *aux_buffer(size_t bytes, void *stream);
 
 // Per-device one-time setup (kernel attributes such as the dynamic shared
 // memory limit hold per device): `done` has one bit per device.  Running the
@@ -195,7 +197,11 @@ gb_status launch_thin_oz(int64_t rows, int64_t K, const double *X, int64_t ldx, 
 
 gb_status launch_skinny_f32(const GemmArgs &g);
 gb_status launch_skinny_f64(const GemmArgs &g);
-size_t skinny_workspace_bytes(const GemmArgs &g, int bits);   // what launch_skinny_* takes; launches nothing
+size_t skinny_workspace_bytes(const GemmArgs &g, int bits);
+// gemm_report.cu: the normwise error report around one product (before: norms and sampled C0;
+// after: Dot2 of the sample against C, reduced into *out)
+gb_status report_before(const GemmArgs &g, int bits);
+gb_status report_after(const GemmArgs &g, int bits, double *out);   // what launch_skinny_* takes; launches nothing
 // C = beta*C (beta==0: C = 0) or C = C + beta (scalar) epilogue-only path (K == 0)
 gb_status launch_gemm_k0_f32(const GemmArgs &g);
 gb_status launch_gemm_k0_f64(const GemmArgs &g);

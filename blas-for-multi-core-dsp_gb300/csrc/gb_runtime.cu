@@ -106,45 +106,53 @@ void *workspace(size_t bytes, void *stream, unsigned *seq, size_t *size) {
     return p;
 }
 
-void *workspace(size_t bytes, void *stream) {
+// The (device, stream) entry of `pool`, grown to at least `bytes` (never below
+// `floor`).  Growing synchronises the stream (the old buffer may still be read
+// by work queued on it) and is refused while the stream is being captured.
+static void *pool_buffer(std::vector<WsEntry> &pool, size_t bytes, void *stream, size_t floor, const char *what) {
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(g_ws_mu);
     WsEntry *w = nullptr;
-    for (auto &e : g_ws)
+    for (auto &e : pool)
         if (e.dev == dev && e.stream == stream) w = &e;
     if (w && w->size >= bytes) return w->ptr;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(as_stream(stream), &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone) {
         // growing would synchronise and free under the capture: the caller reserves first
-        set_status(GB_ERR_INVALID_ARG, "workspace: %zu bytes not reserved before the stream capture began (%zu held)",
+        set_status(GB_ERR_INVALID_ARG, "%s: %zu bytes not reserved before the stream capture began (%zu held)", what,
                    bytes, w ? w->size : (size_t)0);
         return nullptr;
     }
     cudaGetLastError();
     if (w && w->ptr) {
-        // the old buffer may still be read by work queued on its stream
         cudaStreamSynchronize(as_stream(stream));
         cudaFree(w->ptr);
         w->ptr = nullptr;
         w->size = 0;
     }
-    size_t want = bytes < (size_t(64) << 20) ? (size_t(64) << 20) : bytes;
+    size_t want = bytes < floor ? floor : bytes;
     void *p = nullptr;
     cudaError_t e = cudaMalloc(&p, want);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        set_status(GB_ERR_OOM, "workspace: cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+        set_status(GB_ERR_OOM, "%s: cudaMalloc(%zu) failed: %s", what, want, cudaGetErrorString(e));
         return nullptr;
     }
     if (!w) {
-        g_ws.push_back(WsEntry{dev, stream, nullptr, 0, 0});
-        w = &g_ws.back();
+        pool.push_back(WsEntry{dev, stream, nullptr, 0, 0});
+        w = &pool.back();
     }
     w->ptr = p;
     w->size = want;
     return p;
 }
+
+void *workspace(size_t bytes, void *stream) { return pool_buffer(g_ws, bytes, stream, size_t(64) << 20, "workspace"); }
+
+// small per-stream scratch of the error report, apart from the GEMM workspace
+static std::vector<WsEntry> g_aux;
+void *aux_buffer(size_t bytes, void *stream) { return pool_buffer(g_aux, bytes, stream, size_t(64) << 10, "aux"); }
 
 // The error word lives in a file-scope device variable (zero when the module
 // loads), so finding it needs no allocation: its device address is looked up

@@ -70,6 +70,9 @@ int pick(int bits, bool ta, bool tb, int64_t M, int64_t N, int64_t K) {
 }
 
 template <typename T>
+gb_status run_algo(const GemmArgs &g, const gb_gemm_opts &o, const char *fn);
+
+template <typename T>
 gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alpha, const T *A, int64_t lda,
                const T *B, int64_t ldb, T beta, T *C, int64_t ldc, const gb_gemm_opts *opts) {
     gb_gemm_opts o;
@@ -86,7 +89,13 @@ gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alph
     GB_CHECK_ARG(o.semantics >= 0 && o.semantics <= 2, "%s: unknown semantics %d", fn, o.semantics);
     GB_CHECK_ARG(o.algo >= 0 && o.algo <= 8, "%s: unknown algo %d", fn, o.algo);
     GB_CHECK_ARG(o.k_block >= 0 && o.k_slab >= 0, "%s: negative k_block/k_slab", fn);
-    if (M == 0 || N == 0) return ok();
+    GB_CHECK_ARG(o.split_k >= 0 && o.split_k <= 64, "%s: split_k %d not in 0..64", fn, o.split_k);
+    if (M == 0 || N == 0) {
+        if (!o.err_out) return ok();
+        GemmArgs g0;
+        g0.M = M; g0.N = N; g0.stream = as_stream(o.stream);
+        return report_after(g0, sizeof(T) * 8, o.err_out);
+    }
     GB_CHECK_ARG(C != nullptr, "%s: C is null", fn);
     if (K > 0) GB_CHECK_ARG(A != nullptr && B != nullptr, "%s: A or B is null", fn);
     (void)arows; (void)brows;
@@ -97,10 +106,20 @@ gb_status gemm(char transA, char transB, int64_t M, int64_t N, int64_t K, T alph
     g.alpha = (double)alpha; g.beta = (double)beta;
     g.semantics = o.semantics;
     g.k_block = o.k_block; g.k_slab = o.k_slab; g.alpha_on_b = o.alpha_on_b;
-    GB_CHECK_ARG(o.split_k >= 0 && o.split_k <= 64, "%s: split_k %d not in 0..64", fn, o.split_k);
     g.accum_k = o.accum_k; g.split_k = o.split_k;
     g.stream = as_stream(o.stream);
+    if (!o.err_out) return run_algo<T>(g, o, fn);
+    gb_status st = report_before(g, sizeof(T) * 8);
+    if (st == GB_OK) st = run_algo<T>(g, o, fn);
+    if (st == GB_OK) st = report_after(g, sizeof(T) * 8, o.err_out);
+    return st;
+}
 
+// The product itself, with the algorithm the options ask for (AUTO picked by shape).
+template <typename T>
+gb_status run_algo(const GemmArgs &g, const gb_gemm_opts &o, const char *fn) {
+    const bool ta = g.ta, tb = g.tb;
+    const int64_t M = g.M, N = g.N, K = g.K;
     int algo = o.algo;
     if (algo == GB_ALGO_AUTO) algo = pick(sizeof(T) * 8, ta, tb, M, N, K);
     if (algo == GB_ALGO_ORDERED)

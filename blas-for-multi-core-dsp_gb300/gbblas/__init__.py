@@ -46,7 +46,7 @@ class GemmOpts(ctypes.Structure):
     _fields_ = [("stream", ctypes.c_void_p), ("algo", ctypes.c_int32), ("semantics", ctypes.c_int32),
                 ("k_block", ctypes.c_int32), ("k_slab", ctypes.c_int32), ("alpha_on_b", ctypes.c_int32),
                 ("ozaki_slices", ctypes.c_int32), ("target_err", ctypes.c_double),
-                ("accum_k", ctypes.c_int32), ("split_k", ctypes.c_int32), ("reserved", ctypes.c_int32 * 2)]
+                ("accum_k", ctypes.c_int32), ("split_k", ctypes.c_int32), ("err_out", ctypes.c_void_p)]
 
 
 class TuneChoice(ctypes.Structure):
@@ -231,7 +231,7 @@ def sync(stream=None):
 
 
 def opts(algo=ALGO_AUTO, semantics=SEM_BLAS, stream=None, k_block=0, k_slab=0, alpha_on_b=0,
-         ozaki_slices=0, target_err=0.0, accum_k=0, split_k=0):
+         ozaki_slices=0, target_err=0.0, accum_k=0, split_k=0, err_out=None):
     o = GemmOpts()
     lib().gb_gemm_opts_init(ctypes.byref(o))
     o.stream = _stream(stream)
@@ -244,6 +244,7 @@ def opts(algo=ALGO_AUTO, semantics=SEM_BLAS, stream=None, k_block=0, k_slab=0, a
     o.target_err = target_err
     o.accum_k = accum_k
     o.split_k = split_k
+    o.err_out = _ptr(err_out) if err_out is not None else None
     return o
 
 

@@ -145,7 +145,20 @@ typedef struct gb_gemm_opts {
                               BF16X6 256, BF16X3 never); < 0 -> never         */
     int32_t split_k;       /* SKINNY: number of K ranges computed apart and
                               summed (split-K); 0 -> the planner's choice     */
-    int32_t reserved[2];
+    double *err_out;       /* non-NULL: after the product, in stream order,
+                              store its normwise error estimate here (memory
+                              the device writes: device, managed or mapped
+                              pinned host memory):
+                              ||C - C*||_F / (|alpha| ||op(A)_I||_F
+                              ||op(B)_J||_F + |beta| ||C0_IJ||_F) over 16
+                              rows I and 16 columns J spread evenly over C
+                              (all when M or N < 16), C* by Dot2 rounded to
+                              FP64; scalar-beta semantics use |beta|
+                              sqrt(|I||J|) (+ ||C0_IJ||_F when accumulating)
+                              for the last term.  Two extra launches; the
+                              buffer they share is per stream (64 KB, made
+                              on first use: before a graph capture, make one
+                              call with err_out on the stream)              */
 } gb_gemm_opts;
 
 /* Fill *opts with defaults (AUTO, BLAS, NULL stream). */
