@@ -277,7 +277,9 @@ class Ctx:
 def base_line(ctx, metric, value, unit, ms, steps, dtype, config, hib=True):
     return {"metric": metric, "value": value, "unit": unit, "n_gpus": ctx.world, "steps": steps,
             "warmup": ctx.args.warmup, "ms_per_step": ms / steps, "higher_is_better": hib, "scaling": "weak",
-            "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config}
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config,
+            "fma_peak_tflops": {"ffma": ctx.fma_peak[32], "dfma": ctx.fma_peak[64],
+                                "note": "scalar FMA throughput measured on this GPU (gb_measure_fma_peak)"}}
 
 
 def memcpy(ctx, dst, src, nbytes, kind, stream=None):
