@@ -499,7 +499,6 @@ struct EpiParams {
     int tiles_m, tiles_n;
     int *err;
     int chunk_kb;    // k-blocks per accumulator chunk (folding form)
-    int c_prefetch;  // wide folding form: chunks before a tile's end at which its C is prefetched to L2
     // Half-tile tail: tiles [half_start, tiles) (a last wave at most half
     // full) run as two 128-column halves on different CTAs, so the wave takes
     // half a tile time.
@@ -587,21 +586,6 @@ __device__ __forceinline__ void store_recomputed(const EpiParams &p, int64_t row
 //    16 columns at a time.
 // The MMAs of chunk c+1 overlap the fold of chunk c.
 // F16: FP16 pieces of scaled lines (FP16X3), the epilogue applies the scales.
-// Rows m0 .. m0+127 of C, columns n0 .. n0+width-1, into L2 by bulk prefetches (one per row; a
-// row whose start is not 16-byte aligned is skipped, and the length is rounded down to 16 bytes,
-// so every prefetched byte lies inside C).
-__device__ __forceinline__ void prefetch_c_tile(const EpiParams &p, int64_t m0, int64_t n0, int width) {
-    if (n0 >= p.N) return;
-    const int64_t cols = p.N - n0 < width ? p.N - n0 : width;
-    const uint32_t bytes = (uint32_t)(cols * 4) & ~15u;
-    if (bytes == 0) return;
-    const int64_t rows = p.M - m0 < 128 ? p.M - m0 : 128;
-    for (int64_t r = 0; r < rows; r++) {
-        const float *rp = p.C + (m0 + r) * p.ldc + n0;
-        if (((uintptr_t)rp & 15) == 0) ptx::bulk_prefetch_l2(rp, bytes);
-    }
-}
-
 template <int NP, int BN, bool FOLD, bool F16, int EW>
 __global__ void __launch_bounds__(64 + 32 * EW, 1)
     bf16x3_gemm_kernel(const __grid_constant__ PieceMaps maps, EpiParams p) {
@@ -660,13 +644,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
                 const int m0 = tm * BM, n0 = tn * BN + (half > 0 ? BN / 2 : 0);
                 const uint32_t bytes = half < 0 ? STAGE_BYTES : NP * A_TILE + NP * (B_TILE / 2);
-                // the k-block at which this tile's C is prefetched into L2 (wide folding form): the
-                // epilogue's C loads at the tile's end then wait on L2, not on HBM
-                const int kb_pf = EW == 8 && reads_c(p) ? (p.num_kb > p.c_prefetch * p.chunk_kb
-                                                               ? p.num_kb - p.c_prefetch * p.chunk_kb : 0)
-                                                        : -1;
                 for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
-                    if (kb == kb_pf) prefetch_c_tile(p, m0, n0, half < 0 ? BN : BN / 2);
                     const int s = kbg % STAGES;
                     if (kbg >= STAGES && !ptx::mbar_wait(&empty[s], ((kbg / STAGES) & 1) ^ 1, p.err, 1)) {
                         go = false;
@@ -1390,11 +1368,6 @@ static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64
     p.tiles_n = tiles_n;
     p.chunk_kb = FOLD ? (p.chunk_kb > 0 ? p.chunk_kb : p.num_kb) : 1;
     p.half_start = half_start;
-    static const int c_prefetch = [] {
-        const char *v = getenv("GB_C_PREFETCH_CHUNKS");
-        return v ? atoi(v) : 4;
-    }();
-    p.c_prefetch = c_prefetch;
     bf16x3_gemm_kernel<NP, BN, FOLD, F16, EW><<<grid, CF::NT, CF::SMEM_BYTES, g.stream>>>(maps, p);
     GB_LAUNCH_CHECK("bf16x3_gemm_kernel");
     *grid_out = grid;
