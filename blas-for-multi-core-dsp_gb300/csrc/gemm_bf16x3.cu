@@ -857,6 +857,57 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
             const int64_t c0 = (int64_t)tn * BN + (wi / 4) * 128;
             const int *cs_w = col_scale + wi * 128;
             const int *rs_w = row_scale + wi * 32;
+            // Direct store: lane l writes its row's 128 columns as 16-byte vectors, the C loads
+            // one group of 8 columns ahead.  Taken when the 128 columns are inside C, the rows'
+            // starts 16-byte aligned and (FP16) every scale 2^-(row + column scale) a normal
+            // float; else the store through shared memory below.
+            bool fast = c0 + 128 <= p.N && (p.ldc & 3) == 0 && ((uintptr_t)p.C & 15) == 0;
+            int nsr = 0;
+            if (F16) {   // non-finite lines have scale -100000: out of range
+                nsr = -rs_w[lane];
+                int lo = cs_w[lane], hi = lo;
+#pragma unroll
+                for (int j = 1; j < 4; j++) {
+                    lo = min(lo, cs_w[lane + 32 * j]);
+                    hi = max(hi, cs_w[lane + 32 * j]);
+                }
+                lo = __reduce_min_sync(0xffffffffu, lo);
+                hi = __reduce_max_sync(0xffffffffu, hi);
+                fast = fast && nsr - hi >= -126 && nsr - lo <= 127;
+            }
+            if (__all_sync(0xffffffffu, fast)) {
+                const bool rc = reads_c(p), rowok = row0 + lane < p.M;
+                float *crow = p.C + (row0 + lane) * p.ldc + c0;
+                float4 cn0 = make_float4(0.f, 0.f, 0.f, 0.f), cn1 = cn0;
+                if (rc && rowok) {
+                    cn0 = *reinterpret_cast<const float4 *>(crow);
+                    cn1 = *reinterpret_cast<const float4 *>(crow + 4);
+                }
+#pragma unroll
+                for (int g = 0; g < 16; g++) {
+                    const float cc[8] = {cn0.x, cn0.y, cn0.z, cn0.w, cn1.x, cn1.y, cn1.z, cn1.w};
+                    if (g + 1 < 16 && rc && rowok) {
+                        cn0 = *reinterpret_cast<const float4 *>(crow + 8 * (g + 1));
+                        cn1 = *reinterpret_cast<const float4 *>(crow + 8 * (g + 1) + 4);
+                    }
+                    float *o = total + 8 * g;   // the outputs replace their totals
+                    if (F16) {
+                        const int4 s0 = *reinterpret_cast<const int4 *>(cs_w + 8 * g);
+                        const int4 s1 = *reinterpret_cast<const int4 *>(cs_w + 8 * g + 4);
+                        const int sc[8] = {s0.x, s0.y, s0.z, s0.w, s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+                        for (int j = 0; j < 8; j++) o[j] = epi_value(p, o[j] * pow2f(nsr - sc[j]), cc[j]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 8; j++) o[j] = epi_value(p, o[j], cc[j]);
+                    }
+                    if (rowok) {
+                        *reinterpret_cast<float4 *>(crow + 8 * g) = make_float4(o[0], o[1], o[2], o[3]);
+                        *reinterpret_cast<float4 *>(crow + 8 * g + 4) = make_float4(o[4], o[5], o[6], o[7]);
+                    }
+                }
+                continue;
+            }
             float *stg = epi + wi * 32 * 17;
             const bool rc = reads_c(p);
             const int cl = lane & 15, rh = lane >> 4;   // this lane's column and row parity when storing
