@@ -58,6 +58,8 @@ void *workspace(size_t bytes, void *stream);
 void *workspace(size_t bytes, void *stream, unsigned *seq, size_t *size);
 // small per-stream scratch (>= 64 KB), separate from the workspace
 void *aux_buffer(size_t bytes, void *stream);
+// per-stream buffer of the FP16 form's line maxima (cleared when made, *size = its bytes)
+void *linemax_buffer(size_t bytes, void *stream, size_t *size);
 
 // Per-device one-time setup (kernel attributes such as the dynamic shared
 // memory limit hold per device): `done` has one bit per device.  Running the

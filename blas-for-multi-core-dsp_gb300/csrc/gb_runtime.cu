@@ -107,16 +107,21 @@ void *workspace(size_t bytes, void *stream, unsigned *seq, size_t *size) {
 }
 
 // The (device, stream) entry of `pool`, grown to at least `bytes` (never below
-// `floor`).  Growing synchronises the stream (the old buffer may still be read
-// by work queued on it) and is refused while the stream is being captured.
-static void *pool_buffer(std::vector<WsEntry> &pool, size_t bytes, void *stream, size_t floor, const char *what) {
+// `floor`; a new buffer is cleared on the stream when `zero`).  Growing
+// synchronises the stream (the old buffer may still be read by work queued on
+// it) and is refused while the stream is being captured.
+static void *pool_buffer(std::vector<WsEntry> &pool, size_t bytes, void *stream, size_t floor, const char *what,
+                         bool zero = false, size_t *size = nullptr) {
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(g_ws_mu);
     WsEntry *w = nullptr;
     for (auto &e : pool)
         if (e.dev == dev && e.stream == stream) w = &e;
-    if (w && w->size >= bytes) return w->ptr;
+    if (w && w->size >= bytes) {
+        if (size) *size = w->size;
+        return w->ptr;
+    }
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(as_stream(stream), &cap) == cudaSuccess && cap != cudaStreamCaptureStatusNone) {
         // growing would synchronise and free under the capture: the caller reserves first
@@ -139,12 +144,18 @@ static void *pool_buffer(std::vector<WsEntry> &pool, size_t bytes, void *stream,
         set_status(GB_ERR_OOM, "%s: cudaMalloc(%zu) failed: %s", what, want, cudaGetErrorString(e));
         return nullptr;
     }
+    if (zero && (e = cudaMemsetAsync(p, 0, want, as_stream(stream))) != cudaSuccess) {
+        cudaFree(p);
+        set_status(GB_ERR_CUDA, "%s: cudaMemsetAsync failed: %s", what, cudaGetErrorString(e));
+        return nullptr;
+    }
     if (!w) {
         pool.push_back(WsEntry{dev, stream, nullptr, 0, 0});
         w = &pool.back();
     }
     w->ptr = p;
     w->size = want;
+    if (size) *size = want;
     return p;
 }
 
@@ -153,6 +164,12 @@ void *workspace(size_t bytes, void *stream) { return pool_buffer(g_ws, bytes, st
 // small per-stream scratch of the error report, apart from the GEMM workspace
 static std::vector<WsEntry> g_aux;
 void *aux_buffer(size_t bytes, void *stream) { return pool_buffer(g_aux, bytes, stream, size_t(64) << 10, "aux"); }
+
+// per-stream line maxima of the FP16 form (cleared when made; only scans write it)
+static std::vector<WsEntry> g_lm;
+void *linemax_buffer(size_t bytes, void *stream, size_t *size) {
+    return pool_buffer(g_lm, bytes, stream, size_t(64) << 10, "line maxima", true, size);
+}
 
 // The error word lives in a file-scope device variable (zero when the module
 // loads), so finding it needs no allocation: its device address is looked up
@@ -382,6 +399,9 @@ gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int kind, void *st
 gb_status gb_workspace_reserve(size_t bytes, void *stream) {
     if (bytes == 0) return ok();
     if (!workspace(bytes, stream)) return (gb_status)gb_get_last_status();
+    // the FP16 form's line maxima: 2 x 8 bytes per line, at most bytes / 512 lines
+    size_t got = 0;
+    if (!linemax_buffer(bytes / 32, stream, &got)) return (gb_status)gb_get_last_status();
     return ok();
 }
 

@@ -202,30 +202,43 @@ __device__ __forceinline__ void split_entry_guard(const unsigned long long *done
 
 // ------------------------------------------------------------------ scan
 // Largest |x| bit pattern of every row of op(X) (rows x K) -- non-negative
-// floats order as their bit patterns -- by atomicMax from 64 x 64 tiles
-// (out cleared first).  Both operands in one launch; `vec`: 16-byte loads.
+// floats order as their bit patterns -- by atomicMax from 64 x 64 tiles.
+// Each line's entry is (gen << 32) | bits with the call's generation `gen`
+// (larger than any earlier call's on the stream), so no clearing is needed
+// between calls: every line receives its call's value, which is larger than
+// whatever an earlier call left.  Both operands in one launch; `vec`: 16-byte
+// loads.  The scan may be launched beside the previous call's GEMM, like a
+// split pass (split_entry_guard); each CTA then counts itself in `scan_done`
+// and triggers the split pass that follows, which waits for the count
+// instead of the scan's completion, so both can run beside that GEMM.
 struct ScanOp {
     const float *X;
     int64_t ldx, rows, tiles_k, tiles;
     int trans;                      // element (r, k) at X[k*ldx + r]
-    unsigned *out;
+    unsigned long long *out;
 };
 struct ScanArgs {
     ScanOp op[2];
     int64_t K;
     int vec;
+    unsigned gen;
+    const unsigned long long *done;   // split_entry_guard
+    unsigned long long expect;
+    unsigned long long *scan_done;    // finished scan CTAs of the stream (null: not counted)
 };
 
 __device__ __forceinline__ unsigned absbits(float x) { return __float_as_uint(x) & 0x7fffffffu; }
 
 __global__ void __launch_bounds__(256) maxbits_kernel(const __grid_constant__ ScanArgs a) {
     __shared__ unsigned red[16][65];
+    split_entry_guard(a.done, a.expect);
     int64_t b = blockIdx.x;
     const int w = b < a.op[0].tiles ? 0 : 1;
     if (w) b -= a.op[0].tiles;
     const ScanOp &o = a.op[w];
     const int64_t r0 = (b / o.tiles_k) * 64, k0 = (b % o.tiles_k) * 64;
     const int t = threadIdx.x, c4 = 4 * (t % 16), rl = t / 16;
+    const unsigned long long tag = (unsigned long long)a.gen << 32;
     if (!o.trans) {   // 16 threads (a half warp) per row, 4 k each
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -244,35 +257,61 @@ __global__ void __launch_bounds__(256) maxbits_kernel(const __grid_constant__ Sc
             }
 #pragma unroll
             for (int s = 8; s >= 1; s >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, s));
-            if ((t & 15) == 0 && r < o.rows && m) atomicMax(&o.out[r], m);
+            if ((t & 15) == 0 && r < o.rows) atomicMax(&o.out[r], tag | m);
         }
-        return;
-    }
-    unsigned m[4] = {0u, 0u, 0u, 0u};   // 4 consecutive rows, 4 k each
+    } else {
+        unsigned m[4] = {0u, 0u, 0u, 0u};   // 4 consecutive rows, 4 k each
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int64_t k = k0 + rl + 16 * i, r = r0 + c4;
-        if (k >= a.K) continue;
-        const float *src = o.X + k * o.ldx + r;
-        if (a.vec && r + 3 < o.rows) {
-            const float4 x = __ldg(reinterpret_cast<const float4 *>(src));
-            m[0] = max(m[0], absbits(x.x)); m[1] = max(m[1], absbits(x.y));
-            m[2] = max(m[2], absbits(x.z)); m[3] = max(m[3], absbits(x.w));
-        } else {
+        for (int i = 0; i < 4; i++) {
+            const int64_t k = k0 + rl + 16 * i, r = r0 + c4;
+            if (k >= a.K) continue;
+            const float *src = o.X + k * o.ldx + r;
+            if (a.vec && r + 3 < o.rows) {
+                const float4 x = __ldg(reinterpret_cast<const float4 *>(src));
+                m[0] = max(m[0], absbits(x.x)); m[1] = max(m[1], absbits(x.y));
+                m[2] = max(m[2], absbits(x.z)); m[3] = max(m[3], absbits(x.w));
+            } else {
 #pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (r + q < o.rows) m[q] = max(m[q], absbits(src[q]));
+                for (int q = 0; q < 4; q++)
+                    if (r + q < o.rows) m[q] = max(m[q], absbits(src[q]));
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) red[rl][c4 + q] = m[q];
+        __syncthreads();
+        if (t < 64) {
+            unsigned mm = 0;
+#pragma unroll
+            for (int j = 0; j < 16; j++) mm = max(mm, red[j][t]);
+            if (r0 + t < o.rows) atomicMax(&o.out[r0 + t], tag | mm);
         }
     }
-#pragma unroll
-    for (int q = 0; q < 4; q++) red[rl][c4 + q] = m[q];
+    // this CTA's maxima are in: count it, then let the split pass launch
+    __threadfence();
     __syncthreads();
-    if (t < 64) {
-        unsigned mm = 0;
-#pragma unroll
-        for (int j = 0; j < 16; j++) mm = max(mm, red[j][t]);
-        if (r0 + t < o.rows && mm) atomicMax(&o.out[r0 + t], mm);
+    if (threadIdx.x == 0) {
+        if (a.scan_done) atomicAdd(a.scan_done, 1ull);
+        ptx::pdl_launch_dependents();
     }
+    // as split_kernel: the grid does not complete before the previous grid has
+    if (blockIdx.x == 0 && threadIdx.x == 0) ptx::pdl_wait();
+}
+
+// The split pass of the FP16 form waits for every CTA of its scan: `expect`
+// finished scan CTAs on the stream (bounded; on expiry the error word is set
+// and the pass goes on, so nothing hangs).
+__device__ __forceinline__ void scan_entry_wait(const unsigned long long *scan_done, unsigned long long expect,
+                                                int *err) {
+    if (threadIdx.x == 0 && ld_acquire_u64(scan_done) < expect) {
+        const uint64_t t0 = ptx::globaltimer();
+        while (ld_acquire_u64(scan_done) < expect) {
+            if (ptx::globaltimer() - t0 > ptx::kWaitLimitNs) {
+                atomicCAS(err, 0, 20);
+                break;
+            }
+        }
+    }
+    __syncthreads();
 }
 
 // ------------------------------------------------------------------ split
@@ -316,16 +355,19 @@ struct Pieces<true> {
 // trans ? X[k*ldx + r] : X[r*ldx + k].  32x32 tiles through shared memory
 // so both the read and the write are coalesced in either layout.  With
 // out_lo2 the value is cut in three BF16 pieces (hi, mid, lo: 24 bits).
-// mbits (FP16 form): the largest |x| bit pattern of each row.
+// mbits (FP16 form): the largest |x| bit pattern of each row (low 32 bits).
 template <bool F16>
 __global__ void __launch_bounds__(256) split_kernel(const float *__restrict__ X, int64_t ldx, int trans, int64_t rows,
                                                     int64_t K, int64_t kp, uint16_t *__restrict__ out_hi,
                                                     uint16_t *__restrict__ out_lo, uint16_t *__restrict__ out_lo2,
-                                                    const unsigned *__restrict__ mbits,
-                                                    const unsigned long long *done, unsigned long long expect) {
+                                                    const unsigned long long *__restrict__ mbits,
+                                                    const unsigned long long *done, unsigned long long expect,
+                                                    const unsigned long long *scan_done,
+                                                    unsigned long long scan_expect, int *err) {
     using P = Pieces<F16>;
     __shared__ float tile[32][33];
-    split_entry_guard(done, expect);
+    if (scan_done) scan_entry_wait(scan_done, scan_expect, err);
+    else split_entry_guard(done, expect);
     const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;   // 32 x 8
     const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
 #pragma unroll
@@ -347,7 +389,7 @@ __global__ void __launch_bounds__(256) split_kernel(const float *__restrict__ X,
         int64_t r = r0 + ty + i, k = k0 + tx;
         if (r < rows && k < kp) {
             typename P::T h, l, l2;
-            P::cut(tile[tx][ty + i], F16 ? f16_line_scale(mbits[r]) : 0, h, l, l2);
+            P::cut(tile[tx][ty + i], F16 ? f16_line_scale((unsigned)mbits[r]) : 0, h, l, l2);
             out_hi[r * kp + k] = P::bits(h);
             out_lo[r * kp + k] = P::bits(l);
             if (out_lo2) out_lo2[r * kp + k] = P::bits(l2);
@@ -362,14 +404,15 @@ __global__ void __launch_bounds__(256) split_kernel(const float *__restrict__ X,
 // with leading dimensions a multiple of 4).  A CTA converts a 64 x 64 block
 // of (row, k): a K-contiguous source is read and written 4 values at a time
 // straight from registers; a row-contiguous source is read 4 rows at a time
-// into shared memory and written 4 k at a time.  Same values as
+// into shared memory and written 4 k at a time, in two halves of 32 k (a
+// small tile, so that a split CTA fits on an SM beside a GEMM CTA).  Same values as
 // split_kernel, about two-thirds of its time at the 4096^2 operands.
 struct SplitOp {
     const float *X;
     int64_t ldx, rows, tiles_k, tiles;
     int trans;                      // source element (r, k) at X[k*ldx + r]
     uint16_t *out[3];
-    const unsigned *mbits;          // FP16 form: largest |x| bit pattern per row
+    const unsigned long long *mbits;   // FP16 form: largest |x| bit pattern per row (low 32 bits)
 };
 struct SplitArgs {
     SplitOp op[2];
@@ -377,13 +420,16 @@ struct SplitArgs {
     int np;
     const unsigned long long *done;
     unsigned long long expect;
+    const unsigned long long *scan_done;   // FP16 form: wait for the scan's CTAs (scan_entry_wait)
+    unsigned long long scan_expect;
+    int *err;
 };
 
 template <bool F16>
 __device__ __forceinline__ void split_store4(const SplitArgs &a, const SplitOp &o, int64_t r, int64_t k,
                                              const float (&v)[4]) {
     using P = Pieces<F16>;
-    const int s = F16 ? f16_line_scale(o.mbits[r]) : 0;
+    const int s = F16 ? f16_line_scale((unsigned)o.mbits[r]) : 0;
     uint32_t h[2], l[2], l2[2];
 #pragma unroll
     for (int q = 0; q < 4; q += 2) {
@@ -402,8 +448,9 @@ __device__ __forceinline__ void split_store4(const SplitArgs &a, const SplitOp &
 
 template <bool F16>
 __global__ void __launch_bounds__(256) split_vec_kernel(const __grid_constant__ SplitArgs a) {
-    __shared__ float tile[64][65];
-    split_entry_guard(a.done, a.expect);
+    __shared__ float tile[32][65];   // 8.3 KB: fits beside a GEMM CTA on its SM
+    if (a.scan_done) scan_entry_wait(a.scan_done, a.scan_expect, a.err);
+    else split_entry_guard(a.done, a.expect);
     int64_t b = blockIdx.x;
     const int w = b < a.op[0].tiles ? 0 : 1;
     if (w) b -= a.op[0].tiles;
@@ -430,31 +477,37 @@ __global__ void __launch_bounds__(256) split_vec_kernel(const __grid_constant__ 
         if (blockIdx.x == 0 && threadIdx.x == 0) ptx::pdl_wait();   // as split_kernel
         return;
     }
+    // row-contiguous source: the 64 x 64 block in two halves of 32 k through tile[k][r]
+    const int kw = 4 * (t % 8), rw = t / 8;   // writer: 4 consecutive k of row rw (+ 32)
 #pragma unroll
-    for (int i = 0; i < 4; i++) {   // tile[k][r], 4 consecutive r per load
-        const int kl = rl + 16 * i;
-        const int64_t k = k0 + kl, r = r0 + c4;
-        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (k < a.K) {
-            const float *src = o.X + k * o.ldx + r;
-            if (r + 3 < o.rows) {
-                x = __ldg(reinterpret_cast<const float4 *>(src));
-            } else {
-                if (r < o.rows) x.x = src[0];
-                if (r + 1 < o.rows) x.y = src[1];
-                if (r + 2 < o.rows) x.z = src[2];
+    for (int h = 0; h < 2; h++) {
+        if (h) __syncthreads();   // the first half's reads of the tile are done
+#pragma unroll
+        for (int i = 0; i < 2; i++) {   // tile[k][r], 4 consecutive r per load
+            const int kl = rl + 16 * i;
+            const int64_t k = k0 + 32 * h + kl, r = r0 + c4;
+            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < a.K) {
+                const float *src = o.X + k * o.ldx + r;
+                if (r + 3 < o.rows) {
+                    x = __ldg(reinterpret_cast<const float4 *>(src));
+                } else {
+                    if (r < o.rows) x.x = src[0];
+                    if (r + 1 < o.rows) x.y = src[1];
+                    if (r + 2 < o.rows) x.z = src[2];
+                }
             }
+            tile[kl][c4] = x.x; tile[kl][c4 + 1] = x.y; tile[kl][c4 + 2] = x.z; tile[kl][c4 + 3] = x.w;
         }
-        tile[kl][c4] = x.x; tile[kl][c4 + 1] = x.y; tile[kl][c4 + 2] = x.z; tile[kl][c4 + 3] = x.w;
-    }
-    __syncthreads();
+        __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int rr = rl + 16 * i;
-        const int64_t r = r0 + rr;
-        if (r >= o.rows) continue;
-        const float v[4] = {tile[c4][rr], tile[c4 + 1][rr], tile[c4 + 2][rr], tile[c4 + 3][rr]};
-        split_store4<F16>(a, o, r, k0 + c4, v);
+        for (int i = 0; i < 2; i++) {
+            const int rr = rw + 32 * i;
+            const int64_t r = r0 + rr;
+            if (r >= o.rows) continue;
+            const float v[4] = {tile[kw][rr], tile[kw + 1][rr], tile[kw + 2][rr], tile[kw + 3][rr]};
+            split_store4<F16>(a, o, r, k0 + 32 * h + kw, v);
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) ptx::pdl_wait();   // as split_kernel
 }
@@ -509,7 +562,7 @@ struct EpiParams {
     // FP16 form: largest |x| bit patterns of op(A)'s rows and op(B)'s columns
     // (the scale of each line), and the operands, for the outputs recomputed
     // as plain dot products
-    const unsigned *rowbits, *colbits;
+    const unsigned long long *rowbits, *colbits;   // low 32 bits (scan entries)
     const float *A, *B;
     int64_t lda, ldb, K;
     int ta, tb;
@@ -831,9 +884,9 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int64_t col = c0 + lane + 32 * j;
-                    cb[j] = col < p.N ? p.colbits[col] : 0u;
+                    cb[j] = col < p.N ? (unsigned)p.colbits[col] : 0u;
                 }
-                const unsigned rb = row0 + lane < p.M ? p.rowbits[row0 + lane] : 0u;
+                const unsigned rb = row0 + lane < p.M ? (unsigned)p.rowbits[row0 + lane] : 0u;
                 int *cs_w = col_scale + (warp - 2) * 128;
                 __syncwarp();   // the previous tile's reads of the scales are done
 #pragma unroll
@@ -1361,15 +1414,18 @@ gb_status launch_sgemm_fp16x3(const GemmArgs &g) {
 // work the caller queued in between.
 constexpr int kDoneSlots = 1024;
 static __device__ unsigned long long g_gemm_done[kDoneSlots];
+static __device__ unsigned long long g_scan_done[kDoneSlots];   // finished FP16 scan CTAs
 
 struct StreamState {
     int dev;
     void *stream;
-    int slot;                    // index into g_gemm_done, -1: none left
+    int slot;                    // index into g_gemm_done / g_scan_done, -1: none left
     unsigned long long launched; // CTAs of this stream's GEMMs launched so far
     bool valid;                  // the stream's last two-pass GEMM is known
     uintptr_t c_lo, c_hi;        // its C
     unsigned parity;             // its workspace half
+    unsigned long long scanned;  // CTAs of this stream's FP16 scans launched so far
+    unsigned gen;                // generation of its last FP16 scan (captured scans use 1)
 };
 static std::mutex g_tp_mu;
 static std::vector<StreamState> g_tp;
@@ -1381,8 +1437,23 @@ static StreamState &stream_state(int dev, void *stream) {
         if (s.dev == dev && s.stream == stream) return s;
         if (s.dev == dev) used++;
     }
-    g_tp.push_back(StreamState{dev, stream, used < kDoneSlots ? used : -1, 0ull, false, 0, 0, 0u});
+    g_tp.push_back(StreamState{dev, stream, used < kDoneSlots ? used : -1, 0ull, false, 0, 0, 0u, 0ull, 1u});
     return g_tp.back();
+}
+
+static unsigned long long *g_scan_base[64] = {nullptr};
+
+static unsigned long long *scan_counter(int dev, int slot) {
+    if (slot < 0 || dev < 0 || dev >= 64) return nullptr;
+    if (!g_scan_base[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_scan_done) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        g_scan_base[dev] = (unsigned long long *)p;
+    }
+    return g_scan_base[dev] + slot;
 }
 
 static unsigned long long *done_counter(int dev, int slot) {
@@ -1464,13 +1535,12 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
     const int64_t kp = ceil_div(g.K, 64) * 64;   // multiple of BK, zero-padded
     const size_t a_bytes = (size_t)g.M * kp * 2, b_bytes = (size_t)g.N * kp * 2;
     const size_t piece_bytes = (np * (a_bytes + b_bytes) + 255) / 256 * 256;
-    const size_t bits_bytes = f16 ? ((size_t)(g.M + g.N) * 4 + 255) / 256 * 256 : 0;
-    const size_t pieces = piece_bytes + bits_bytes;
+    const size_t pieces = piece_bytes;
     // The buffer is [half 0 | half 1], the same for every call of any form (the halves move only
     // when the buffer grows, which first drains its stream).  Calls alternate between the halves,
     // so a split may run beside the previous GEMM; one half when two do not fit in 16 GiB.
     const char *pe = getenv("GB_BF16X3_PDL");
-    const bool pdl_env = !(pe && pe[0] == '0') && !f16;
+    const bool pdl_env = !(pe && pe[0] == '0');
     const size_t want = pieces <= (size_t(8) << 30) ? 2 * pieces : pieces;
     unsigned seq_unused = 0;
     size_t ws_size = 0;
@@ -1478,6 +1548,15 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
     if (!ws) return (gb_status)gb_get_last_status();
     const size_t half = ws_size / 2 / 256 * 256;
     const bool two_halves = half >= pieces;
+    // FP16 form: the line maxima, [half 0 | half 1] of lm_cap entries, in a buffer of their own
+    unsigned long long *lm_base = nullptr;
+    size_t lm_cap = 0;
+    if (f16) {
+        size_t lm_size = 0;
+        lm_base = (unsigned long long *)linemax_buffer((size_t)16 * (g.M + g.N), g.stream, &lm_size);
+        if (!lm_base) return (gb_status)gb_get_last_status();
+        lm_cap = lm_size / 16;
+    }
     int *err = error_word();
     if (!err) return set_status(GB_ERR_OOM, "bf16x3: no device error word");
     int dev = 0;
@@ -1486,6 +1565,9 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
     if (device_setup_needed(carve)) {   // the GEMM's shared-memory configuration, so a split fits beside it
         GB_CUDA_TRY(cudaFuncSetAttribute(split_vec_kernel<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         GB_CUDA_TRY(cudaFuncSetAttribute(split_kernel<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        GB_CUDA_TRY(cudaFuncSetAttribute(split_vec_kernel<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        GB_CUDA_TRY(cudaFuncSetAttribute(split_kernel<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+        GB_CUDA_TRY(cudaFuncSetAttribute(maxbits_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
         device_setup_done(carve);
     }
 
@@ -1512,9 +1594,19 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
         ap[i] = (uint16_t *)(pw + i * a_bytes);
         bp[i] = (uint16_t *)(pw + np * a_bytes + i * b_bytes);
     }
-    unsigned *bits = f16 ? (unsigned *)(pw + piece_bytes) : nullptr;   // op(A) rows, then op(B) columns
+    unsigned long long *bits = f16 ? lm_base + (size_t)parity * lm_cap : nullptr;   // op(A) rows, op(B) columns
     const unsigned long long *gdone = pdl ? done : nullptr;
     const unsigned long long expect = st.launched;
+    unsigned long long *scan_done = f16 && done ? scan_counter(dev, st.slot) : nullptr;
+    unsigned long long scan_expect = 0;
+    unsigned gen = 1;
+    if (f16 && !capturing) {
+        if (st.gen >= 0xfffffff0u) {   // generations run out: clear the maxima and start again
+            GB_CUDA_TRY(cudaMemsetAsync(lm_base, 0, 2 * lm_cap * sizeof(unsigned long long), g.stream));
+            st.gen = 1;
+        }
+        gen = ++st.gen;   // > 1: above what a captured scan (generation 1) leaves
+    }
 
     cudaLaunchAttribute pdl_attr[1];
     pdl_attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1522,18 +1614,33 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
     const bool vec = g.lda % 4 == 0 && g.ldb % 4 == 0 && (uintptr_t)g.A % 16 == 0 && (uintptr_t)g.B % 16 == 0;
 
     if (f16) {   // largest |x| of every row of op(A) and column of op(B)
-        GB_CUDA_TRY(cudaMemsetAsync(bits, 0, (size_t)(g.M + g.N) * 4, g.stream));
+        // a captured scan replays with its generation fixed: it clears its entries first
+        if (capturing) GB_CUDA_TRY(cudaMemsetAsync(bits, 0, (size_t)(g.M + g.N) * 8, g.stream));
         ScanArgs sc;
         memset(&sc, 0, sizeof(sc));
         sc.K = g.K;
         sc.vec = vec ? 1 : 0;
+        sc.gen = gen;
+        sc.done = gdone;
+        sc.expect = expect;
+        sc.scan_done = scan_done;
         const int64_t tk = ceil_div(g.K, 64);
         sc.op[0] = ScanOp{(const float *)g.A, g.lda, g.M, tk, ceil_div(g.M, 64) * tk, g.ta ? 1 : 0, bits};
         sc.op[1] = ScanOp{(const float *)g.B, g.ldb, g.N, tk, ceil_div(g.N, 64) * tk, g.tb ? 0 : 1, bits + g.M};
         const int64_t blocks = sc.op[0].tiles + sc.op[1].tiles;
         if (blocks > 0x7fffffff) return set_status(GB_ERR_UNSUPPORTED, "fp16x3: operands too large");
-        maxbits_kernel<<<(unsigned)blocks, 256, 0, g.stream>>>(sc);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)blocks);
+        cfg.blockDim = dim3(256);
+        cfg.stream = g.stream;
+        cfg.attrs = pdl_attr;
+        cfg.numAttrs = pdl ? 1 : 0;
+        GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, maxbits_kernel, sc));
         GB_LAUNCH_CHECK("fp16x3 scan");
+        if (scan_done) {
+            st.scanned += (unsigned long long)blocks;
+            scan_expect = st.scanned;
+        }
     }
 
     // split: op(A)(m, k) = ta ? A[k*lda + m] : A[m*lda + k]
@@ -1542,6 +1649,7 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
         SplitArgs sa;
         memset(&sa, 0, sizeof(sa));
         sa.K = g.K; sa.kp = kp; sa.np = np; sa.done = gdone; sa.expect = expect;
+        sa.scan_done = scan_done; sa.scan_expect = scan_expect; sa.err = err;
         sa.op[0] = SplitOp{(const float *)g.A, g.lda, g.M, kp / 64, ceil_div(g.M, 64) * (kp / 64), g.ta ? 1 : 0,
                            {ap[0], ap[1], np == 3 ? ap[2] : nullptr}, bits};
         sa.op[1] = SplitOp{(const float *)g.B, g.ldb, g.N, kp / 64, ceil_div(g.N, 64) * (kp / 64), g.tb ? 0 : 1,
@@ -1567,23 +1675,25 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
         cfg.stream = g.stream;
         cfg.attrs = pdl_attr;
         cfg.numAttrs = pdl ? 1 : 0;
-        const unsigned *mb = bits;
+        const unsigned long long *mb = bits;
+        const unsigned long long *no_scan = nullptr;
         if (f16)
             GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_kernel<true>, (const float *)g.A, g.lda, g.ta ? 1 : 0, g.M, g.K,
-                                           kp, ap[0], ap[1], (uint16_t *)nullptr, mb, gdone, expect));
+                                           kp, ap[0], ap[1], (uint16_t *)nullptr, mb, gdone, expect,
+                                           (const unsigned long long *)scan_done, scan_expect, err));
         else
             GB_CUDA_TRY(cudaLaunchKernelEx(&cfg, split_kernel<false>, (const float *)g.A, g.lda, g.ta ? 1 : 0, g.M,
                                            g.K, kp, ap[0], ap[1], np == 3 ? ap[2] : (uint16_t *)nullptr, mb, gdone,
-                                           expect));
+                                           expect, no_scan, 0ull, err));
         GB_LAUNCH_CHECK("bf16x3 split A");
-        const unsigned *mbB = f16 ? bits + g.M : nullptr;
+        const unsigned long long *mbB = f16 ? bits + g.M : nullptr;
         if (f16)
             split_kernel<true><<<sgB, 256, 0, g.stream>>>((const float *)g.B, g.ldb, g.tb ? 0 : 1, g.N, g.K, kp, bp[0],
-                                                          bp[1], nullptr, mbB, nullptr, 0ull);
+                                                          bp[1], nullptr, mbB, nullptr, 0ull, nullptr, 0ull, err);
         else
             split_kernel<false><<<sgB, 256, 0, g.stream>>>((const float *)g.B, g.ldb, g.tb ? 0 : 1, g.N, g.K, kp,
                                                            bp[0], bp[1], np == 3 ? bp[2] : nullptr, nullptr, nullptr,
-                                                           0ull);
+                                                           0ull, nullptr, 0ull, err);
         GB_LAUNCH_CHECK("bf16x3 split B");
     }
 

@@ -323,12 +323,14 @@ def _pdl_both(fn):
     return outs
 
 
-def test_back_to_back_chain_reads_previous_result(torch):
+@pytest.mark.parametrize("algo_name", ["bf16x3", "fp16x3"])
+def test_back_to_back_chain_reads_previous_result(torch, algo_name):
     """C1 = A B, then C2 = C1 D, then C3 = E C2 with no host synchronisation:
-    each call's operands are the previous call's result, so no split may read
-    them before the GEMM that writes them has finished.  Same bits as the
-    calls in plain order."""
+    each call's operands are the previous call's result, so no scan or split
+    may read them before the GEMM that writes them has finished.  Same bits
+    as the calls in plain order."""
     import gbblas
+    algo = gbblas.ALGO_BF16X3 if algo_name == "bf16x3" else gbblas.ALGO_FP16X3
     M = N = K = 1536
     A = dev(oracle.fill(M, K, 901, dtype=np.float32))
     D = dev(oracle.fill(K, N, 902, dtype=np.float32))
@@ -338,9 +340,9 @@ def test_back_to_back_chain_reads_previous_result(torch):
         C1 = dev(np.zeros((M, N), np.float32))
         C2 = dev(np.zeros((M, N), np.float32))
         C3 = dev(np.zeros((M, N), np.float32))
-        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, D, N, 0.0, C1, N, algo=gbblas.ALGO_BF16X3)
-        gbblas.sgemm("N", "N", M, N, K, 0.5, C1, N, D, N, 0.0, C2, N, algo=gbblas.ALGO_BF16X3)
-        gbblas.sgemm("N", "T", M, N, K, 0.25, E, K, C2, N, 0.0, C3, N, algo=gbblas.ALGO_BF16X3)
+        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, D, N, 0.0, C1, N, algo=algo)
+        gbblas.sgemm("N", "N", M, N, K, 0.5, C1, N, D, N, 0.0, C2, N, algo=algo)
+        gbblas.sgemm("N", "T", M, N, K, 0.25, E, K, C2, N, 0.0, C3, N, algo=algo)
         return host(C3).tobytes()
 
     a, b = _pdl_both(run)
@@ -370,11 +372,13 @@ def test_back_to_back_alternating_forms(torch):
     assert a == b
 
 
-def test_back_to_back_with_caller_work_in_between(torch):
+@pytest.mark.parametrize("algo_name", ["bf16x3", "fp16x3"])
+def test_back_to_back_with_caller_work_in_between(torch, algo_name):
     """A torch kernel on the same stream rewrites the next call's B between
-    two calls: the next call's split starts only after that kernel and reads
-    the new B.  Same bits as the calls in plain order."""
+    two calls: the next call's scan and split start only after that kernel
+    and read the new B.  Same bits as the calls in plain order."""
     import gbblas
+    algo = gbblas.ALGO_BF16X3 if algo_name == "bf16x3" else gbblas.ALGO_FP16X3
     tc = torch
     M = N = K = 1024
     A = dev(oracle.fill(M, K, 950, dtype=np.float32))
@@ -386,13 +390,53 @@ def test_back_to_back_with_caller_work_in_between(torch):
         C0 = dev(np.zeros((M, N), np.float32))
         C1 = dev(np.zeros((M, N), np.float32))
         tc.cuda.synchronize()
-        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B0, N, 0.0, C0, N, algo=gbblas.ALGO_BF16X3)
+        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B0, N, 0.0, C0, N, algo=algo)
         B1.copy_(B1src)          # torch's current stream is the legacy default stream gbblas uses
-        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B1, N, 0.0, C1, N, algo=gbblas.ALGO_BF16X3)
+        gbblas.sgemm("N", "N", M, N, K, 1.0, A, K, B1, N, 0.0, C1, N, algo=algo)
         return host(C0).tobytes() + host(C1).tobytes()
 
     a, b = _pdl_both(run)
     assert a == b
+
+
+def test_fp16x3_back_to_back_overlapped_scans(torch):
+    """FP16X3 calls in a row with disjoint operands (scan and split of each
+    call beside the previous call's GEMM), every layout and a ragged shape,
+    the line maxima kept between calls (generation tags, no clearing): same
+    bits as the calls in plain order, and as each call alone."""
+    import gbblas
+    shapes = [(1536, 1280, 1024, "NN"), (640, 768, 512, "TN"), (1000, 1100, 700, "NT"), (2048, 1024, 768, "TT")]
+    ops = []
+    for i, (M, N, K, mode) in enumerate(shapes):
+        ar, ac = op_shape(mode[0], M, K)
+        br, bc = op_shape(mode[1], K, N)
+        ops.append((dev(oracle.fill(ar, ac, 960 + i, dtype=np.float32)), ac,
+                    dev(oracle.fill(br, bc, 970 + i, dtype=np.float32)), bc))
+
+    def run():
+        Cs = [dev(oracle.fill(M, N, 980 + i, dtype=np.float32)) for i, (M, N, K, mode) in enumerate(shapes)]
+        for rep in range(3):
+            for i, (M, N, K, mode) in enumerate(shapes):
+                A, lda, B, ldb = ops[i]
+                gbblas.sgemm(mode[0], mode[1], M, N, K, 0.75, A, lda, B, ldb, 0.5, Cs[i], N, algo=gbblas.ALGO_FP16X3)
+        return [host(c).tobytes() for c in Cs]
+
+    a, b = _pdl_both(run)
+    assert a == b
+    # one call alone (synchronised before and after) equals the first round of the chain
+    i = 2
+    M, N, K, mode = shapes[i]
+    A, lda, B, ldb = ops[i]
+    C = dev(oracle.fill(M, N, 980 + i, dtype=np.float32))
+    torch.cuda.synchronize()
+    gbblas.sgemm(mode[0], mode[1], M, N, K, 0.75, A, lda, B, ldb, 0.5, C, N, algo=gbblas.ALGO_FP16X3)
+    torch.cuda.synchronize()
+    C1 = dev(oracle.fill(M, N, 980 + i, dtype=np.float32))
+    for _ in range(2):   # other calls in between leave other generations in the maxima
+        gbblas.sgemm("N", "N", 640, 768, 512, 1.0, ops[1][0], 512, ops[1][2], 768, 0.0,
+                     dev(np.zeros((640, 768), np.float32)), 768, algo=gbblas.ALGO_FP16X3)
+    gbblas.sgemm(mode[0], mode[1], M, N, K, 0.75, A, lda, B, ldb, 0.5, C1, N, algo=gbblas.ALGO_FP16X3)
+    assert host(C).tobytes() == host(C1).tobytes()
 
 
 # ---------------------------------------------------------------- FP16X3
