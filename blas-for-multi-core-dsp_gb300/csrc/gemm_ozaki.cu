@@ -458,6 +458,240 @@ __global__ void __launch_bounds__(NT, 1)
     }
 }
 
+// ------------------------------------------------------------ wide form
+// 128 x 256 C tiles (BN_W = 256): every MMA is M128 N256 K16, twice the work
+// of the 128 x 128 form's per instruction and per byte of V staged, and the
+// W tile of a k-block serves 256 columns.  The two FP32 accumulators take all
+// 512 TMEM columns, so the FP64 running sum of each diagonal flush lives in
+// a per-CTA scratch array in global memory (256 KB per CTA, L2-resident,
+// interleaved so that a warp's access to one pair of a lane's values is 512
+// contiguous bytes).  Warps: 0 TMA, 1 MMA, 2-9 epilogue (two per TMEM lane
+// quarter, 128 columns each).  The arithmetic is that of ozaki_gemm_kernel
+// (same chunk sums, flush order, exact scalings and rounding), so the
+// results are the same bit for bit.
+namespace wide {
+constexpr int BN_W = 256, STAGES_W = 4, EW = 8, NT_W = 64 + 32 * EW;
+constexpr int W_TILE = BN_W * BK * 2;                       // 32 KB
+constexpr int STAGE_W = TILE_BYTES + W_TILE;                // 48 KB
+constexpr int SMEM_W = STAGES_W * STAGE_W + 1024 + 256;
+static_assert(SMEM_W <= 232448, "shared memory");
+constexpr size_t SCRATCH_DOUBLES = (size_t)EW * 32 * 128;   // per CTA
+}  // namespace wide
+
+__global__ void __launch_bounds__(wide::NT_W, 1)
+    ozaki_wide_kernel(const __grid_constant__ CUtensorMap tmV, const __grid_constant__ CUtensorMap tmW, OzParams p,
+                      double *scratch) {
+    using namespace wide;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES_W * STAGE_W);
+    uint64_t *empty = full + STAGES_W;
+    uint64_t *acc_full = empty + STAGES_W;
+    uint64_t *acc_empty = acc_full + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int num_tiles = p.tiles_m * p.tiles_n;
+    const int nchunks = (p.num_kb + KCHUNK_BLOCKS - 1) / KCHUNK_BLOCKS;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES_W; s++) {
+            ptx::mbar_init(&full[s], 1);
+            ptx::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            ptx::mbar_init(&acc_full[b], 1);
+            ptx::mbar_init(&acc_empty[b], EW);
+        }
+        ptx::fence_mbar_init();
+        ptx::tma_prefetch_desc(&tmV);
+        ptx::tma_prefetch_desc(&tmW);
+    }
+    if (warp == 1) ptx::tmem_alloc(tmem_slot, TMEM_COLS);
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {   // TMA producer: per tile, per pair, every K block
+            int kbg = 0;
+            bool go = true;
+            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+                int tm, tn;
+                tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+                for (int q = 0; q < p.npairs && go; q++) {
+                    const int vrow = (int)((p.pt[q] - 1) * p.mp + (int64_t)tm * BM);
+                    const int wrow = (int)((p.pu[q] - 1) * p.np + (int64_t)tn * BN_W);
+                    for (int kb = 0; kb < p.num_kb; kb++, kbg++) {
+                        const int s = kbg % STAGES_W;
+                        if (kbg >= STAGES_W && !ptx::mbar_wait(&empty[s], ((kbg / STAGES_W) & 1) ^ 1, p.err, 11)) {
+                            go = false;
+                            break;
+                        }
+                        uint8_t *st = smem + s * STAGE_W;
+                        ptx::mbar_arrive_expect_tx(&full[s], STAGE_W);
+                        ptx::tma_load_2d(st, &tmV, &full[s], kb * BK, vrow);
+                        ptx::tma_load_2d(st + TILE_BYTES, &tmW, &full[s], kb * BK, wrow);
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {   // MMA issuer: one accumulator per K chunk of a pair
+            constexpr uint32_t idesc = ptx::idesc_bf16_f32(BM, BN_W);
+            int kbg = 0, gi = 0;
+            bool go = true;
+            for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+                for (int q = 0; q < p.npairs && go; q++) {
+                    for (int c = 0; c < nchunks && go; c++, gi++) {
+                        const int b = gi & 1;
+                        if (gi >= 2 && !ptx::mbar_wait(&acc_empty[b], ((gi >> 1) & 1) ^ 1, p.err, 12)) {
+                            go = false;
+                            break;
+                        }
+                        ptx::tc_fence_after();
+                        const uint32_t acc = tmem + (uint32_t)(b * BN_W);
+                        const int kb_end = min(p.num_kb, (c + 1) * KCHUNK_BLOCKS);
+                        for (int kb = c * KCHUNK_BLOCKS; kb < kb_end; kb++, kbg++) {
+                            const int s = kbg % STAGES_W;
+                            if (!ptx::mbar_wait(&full[s], (kbg / STAGES_W) & 1, p.err, 13)) {
+                                go = false;
+                                break;
+                            }
+                            ptx::tc_fence_after();
+                            const uint32_t st = ptx::smem_u32(smem + s * STAGE_W);
+                            const uint64_t vd = ptx::sdesc_kmajor_sw128(st);
+                            const uint64_t wd = ptx::sdesc_kmajor_sw128(st + TILE_BYTES);
+#pragma unroll
+                            for (int k = 0; k < BK / 16; k++) {
+                                const uint64_t dk = (uint64_t)((k * 32) >> 4);
+                                ptx::umma_f16(acc, vd + dk, wd + dk, idesc, (kb != c * KCHUNK_BLOCKS) || (k != 0));
+                            }
+                            ptx::umma_commit(&empty[s]);
+                        }
+                        if (go) ptx::umma_commit(&acc_full[b]);
+                    }
+                }
+            }
+        }
+    } else {   // epilogue warps 2..9: TMEM lane quarter warp % 4, columns 128 * ((warp - 2) / 4) + 0..127
+        const int w = warp - 2, q = warp % 4;
+        // this lane's value pair jp at scr[jp * 32] (formed where used: registers are tight here)
+#define OZ_SCR (reinterpret_cast<double2 *>(scratch + (size_t)blockIdx.x * SCRATCH_DOUBLES) + \
+                (size_t)(threadIdx.x / 32 - 2) * 64 * 32 + threadIdx.x % 32)
+        int gi = 0;
+        bool go = true;
+        for (int t = blockIdx.x; t < num_tiles && go; t += gridDim.x) {
+            bool first_flush = true;
+            int iacc[128];
+#pragma unroll
+            for (int j = 0; j < 128; j++) iacc[j] = 0;
+            int nacc = 0;
+            for (int qq = 0; qq < p.npairs && go; qq++) {
+                const int lev = p.pt[qq] + p.pu[qq];
+                const bool lev_ends = qq == p.npairs - 1 || p.pt[qq + 1] + p.pu[qq + 1] != lev;
+                for (int c = 0; c < nchunks; c++, gi++) {
+                    const int b = gi & 1;
+                    if (!ptx::mbar_wait(&acc_full[b], (gi >> 1) & 1, p.err, 14)) { go = false; break; }
+                    ptx::tc_fence_after();
+#pragma unroll
+                    for (int cb = 0; cb < 8; cb++) {   // 16 columns per load
+                        uint32_t r[16];
+                        ptx::tmem_ld_32x32b_x16(tmem + (uint32_t)(b * BN_W) + ((uint32_t)(q * 32) << 16) +
+                                                    (uint32_t)((w / 4) * 128 + cb * 16), r);
+                        ptx::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 16; j++) iacc[cb * 16 + j] += __float2int_rn(__uint_as_float(r[j]));
+                    }
+                    ptx::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
+                    const bool flush = (c == nchunks - 1 && lev_ends) || ++nacc == MAX_CHUNKS_INT32;
+                    if (flush) {   // FP64 sum += 2^(2-8(t+u)) * iacc (exact scaling, one rounding)
+                        nacc = 0;
+                        const double scale = __longlong_as_double((long long)(1023 + 2 - 8 * lev) << 52);
+                        double2 *scr = OZ_SCR;
+                        if (first_flush) {
+#pragma unroll
+                            for (int jp = 0; jp < 64; jp++)
+                                scr[jp * 32] = make_double2(fma((double)iacc[2 * jp], scale, 0.0),
+                                                            fma((double)iacc[2 * jp + 1], scale, 0.0));
+                        } else {
+#pragma unroll
+                            for (int g8 = 0; g8 < 64; g8 += 4) {   // four pairs' loads in flight
+                                double2 v[4];
+#pragma unroll
+                                for (int i = 0; i < 4; i++) v[i] = __ldcg(scr + (g8 + i) * 32);
+#pragma unroll
+                                for (int i = 0; i < 4; i++) {
+                                    v[i].x = fma((double)iacc[2 * (g8 + i)], scale, v[i].x);
+                                    v[i].y = fma((double)iacc[2 * (g8 + i) + 1], scale, v[i].y);
+                                    __stcg(scr + (g8 + i) * 32, v[i]);
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int j = 0; j < 128; j++) iacc[j] = 0;
+                        first_flush = false;
+                    }
+                }
+            }
+            if (!go) break;
+            // C = alpha * 2^(e_i + f_j) * sum (+ beta ...): this lane's row, 128 columns
+            int tm, tn;
+            tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
+            const int64_t row = (int64_t)tm * BM + q * 32 + lane;
+            const int64_t c0 = (int64_t)tn * BN_W + (w / 4) * 128;
+            const bool rowok = row < p.M;
+            const int erow = rowok ? p.erow[row] : 0;
+            const bool needc = p.semantics == GB_SEM_ACCUM_SCALAR_BETA || (p.semantics == GB_SEM_BLAS && p.beta != 0.0);
+            double *crow = p.C + row * p.ldc;
+            const double2 *scr = OZ_SCR;
+#pragma unroll 1
+            for (int g8 = 0; g8 < 64; g8 += 4) {   // eight columns at a time, their C loads in flight together
+                double2 sm[4];
+                double cv[8];
+#pragma unroll
+                for (int i = 0; i < 4; i++) sm[i] = __ldcg(scr + (g8 + i) * 32);
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int64_t col = c0 + 2 * g8 + j;
+                    cv[j] = (rowok && needc && col < p.N) ? crow[col] : 0.0;
+                }
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int64_t col = c0 + 2 * g8 + j;
+                    if (!rowok || col >= p.N) continue;
+                    const int fc = __ldg(p.fcol + col);
+                    const double sum = (j & 1) ? sm[j / 2].y : sm[j / 2].x;
+                    double v;
+                    if (fc == kNonFiniteLineExp || erow == kNonFiniteLineExp)
+                        v = p.alpha * native_dot_cold(p.A, p.lda, p.ta, row, p.B, p.ldb, p.tb, col, p.K);
+                    else
+                        v = p.alpha * mul_pow2(mul_pow2(sum, erow), fc);
+                    if (p.semantics == GB_SEM_BLAS) {
+                        if (p.beta != 0.0) v = fma(p.beta, cv[j], v);
+                    } else if (p.semantics == GB_SEM_SCALAR_BETA) {
+                        v = v + p.beta;
+                    } else {
+                        v = cv[j] + (v + p.beta);
+                    }
+                    crow[col] = v;
+                }
+            }
+        }
+    }
+
+#undef OZ_SCR
+    ptx::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
 }  // namespace
 
 static gb_status ozaki_one(const GemmArgs &g, int s);
@@ -505,18 +739,29 @@ gb_status launch_dgemm_ozaki(const GemmArgs &g, int slices) {
 }
 
 static gb_status ozaki_one(const GemmArgs &g, int s) {
+    // the wide form (128 x 256 tiles) once op(B) has 256 columns; GB_OZAKI_WIDE=0 keeps 128 x 128
+    static const bool wide_env = [] {
+        const char *v = getenv("GB_OZAKI_WIDE");
+        return !(v && v[0] == '0');
+    }();
+    const bool wide = wide_env && g.N >= wide::BN_W;
+    const int bn = wide ? wide::BN_W : BN;
     const int64_t kp = ceil_div(g.K, BK) * BK;
-    const int64_t mp = ceil_div(g.M, BM) * BM, np = ceil_div(g.N, BN) * BN;
+    const int64_t mp = ceil_div(g.M, BM) * BM, np = ceil_div(g.N, bn) * bn;
     if (s * mp > 0x7fffffff || s * np > 0x7fffffff || kp > 0x7fffffff)
         return set_status(GB_ERR_UNSUPPORTED, "ozaki: problem too large for 32-bit TMA coordinates");
-    const size_t ebytes = (size_t)(mp + np) * sizeof(int);
+    const size_t ebytes = ((size_t)(mp + np) * sizeof(int) + 255) / 256 * 256;
     const size_t vbytes = (size_t)s * mp * kp * 2, wbytes = (size_t)s * np * kp * 2;
-    uint8_t *ws = (uint8_t *)workspace(vbytes + wbytes + ebytes + 4096, g.stream);
+    const int64_t tiles_total = (mp / BM) * (np / bn);
+    const int grid = (int)(tiles_total < sm_count() ? tiles_total : sm_count());
+    const size_t sbytes = wide ? (size_t)grid * wide::SCRATCH_DOUBLES * sizeof(double) : 0;
+    uint8_t *ws = (uint8_t *)workspace(vbytes + wbytes + ebytes + sbytes + 4096, g.stream);
     if (!ws) return (gb_status)gb_get_last_status();
     unsigned short *V = (unsigned short *)ws;
     unsigned short *W = (unsigned short *)(ws + vbytes);
     int *erow = (int *)(ws + vbytes + wbytes);
     int *fcol = erow + mp;
+    double *scratch = wide ? (double *)(ws + vbytes + wbytes + ebytes) : nullptr;   // 256-byte aligned
     int *err = error_word();
     if (!err) return set_status(GB_ERR_OOM, "ozaki: no device error word");
 
@@ -546,14 +791,14 @@ static gb_status ozaki_one(const GemmArgs &g, int s) {
 
     CUtensorMap tV, tW;
     if (!make_tmap_bf16(&tV, V, kp, (uint64_t)s * mp, kp * 2, BK, BM, 128) ||
-        !make_tmap_bf16(&tW, W, kp, (uint64_t)s * np, kp * 2, BK, BN, 128))
+        !make_tmap_bf16(&tW, W, kp, (uint64_t)s * np, kp * 2, BK, bn, 128))
         return set_status(GB_ERR_CUDA, "ozaki: cuTensorMapEncodeTiled failed");
 
     OzParams p{};
     p.C = (double *)g.C; p.M = g.M; p.N = g.N; p.ldc = g.ldc;
     p.alpha = g.alpha; p.beta = g.beta; p.semantics = g.semantics;
     p.num_kb = (int)(kp / BK);
-    p.tiles_m = (int)(mp / BM); p.tiles_n = (int)(np / BN);
+    p.tiles_m = (int)(mp / BM); p.tiles_n = (int)(np / bn);
     p.mp = mp; p.np = np;
     p.erow = erow; p.fcol = fcol; p.err = err;
     p.A = A; p.B = B; p.lda = g.lda; p.ldb = g.ldb; p.K = g.K; p.ta = g.ta ? 1 : 0; p.tb = g.tb ? 1 : 0;
@@ -581,12 +826,16 @@ static gb_status ozaki_one(const GemmArgs &g, int s) {
     static std::atomic<uint64_t> attr{0};
     if (device_setup_needed(attr)) {
         GB_CUDA_TRY(cudaFuncSetAttribute(ozaki_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        GB_CUDA_TRY(cudaFuncSetAttribute(ozaki_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, wide::SMEM_W));
         device_setup_done(attr);
     }
-    const int tiles = p.tiles_m * p.tiles_n;
-    const int grid = tiles < sm_count() ? tiles : sm_count();
-    ozaki_gemm_kernel<<<grid, NT, SMEM_BYTES, g.stream>>>(tV, tW, p);
-    GB_LAUNCH_CHECK("ozaki_gemm_kernel");
+    if (wide) {
+        ozaki_wide_kernel<<<grid, wide::NT_W, wide::SMEM_W, g.stream>>>(tV, tW, p, scratch);
+        GB_LAUNCH_CHECK("ozaki_wide_kernel");
+    } else {
+        ozaki_gemm_kernel<<<grid, NT, SMEM_BYTES, g.stream>>>(tV, tW, p);
+        GB_LAUNCH_CHECK("ozaki_gemm_kernel");
+    }
     return ok();
 }
 
