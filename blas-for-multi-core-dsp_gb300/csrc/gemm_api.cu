@@ -181,11 +181,12 @@ size_t gemm_workspace_bound(int bits, int algo, bool ta, bool tb, int64_t M, int
         }
         case GB_ALGO_OZAKI: {   // slices of both operands (K cut into chunks past 4 GiB) + exponents
             const int s = slices > 0 ? slices : ozaki_pick_slices(0.0, K);
-            const int64_t kp = ceil_div(K, 64) * 64, mp = ceil_div(M, 128) * 128, np = ceil_div(N, 128) * 128;
+            const int64_t kp = ceil_div(K, 64) * 64, mp = ceil_div(M, 128) * 128, np = ceil_div(N, 256) * 256;
             double v = (double)s * (double)(mp + np) * (double)kp * 2.0;
             const double cap = 4.0 * (1ull << 30) + (double)s * (mp + np) * 1024 * 2.0;
             if (v > cap) v = cap;
-            return (size_t)v + (size_t)(mp + np) * 4 + 8192;
+            // + the wide form's FP64 scratch: 256 KB per CTA
+            return (size_t)v + (size_t)(mp + np) * 4 + (size_t)sm_count() * (256 << 10) + 8192;
         }
         default:
             return 0;

@@ -740,11 +740,8 @@ gb_status launch_dgemm_ozaki(const GemmArgs &g, int slices) {
 
 static gb_status ozaki_one(const GemmArgs &g, int s) {
     // the wide form (128 x 256 tiles) once op(B) has 256 columns; GB_OZAKI_WIDE=0 keeps 128 x 128
-    static const bool wide_env = [] {
-        const char *v = getenv("GB_OZAKI_WIDE");
-        return !(v && v[0] == '0');
-    }();
-    const bool wide = wide_env && g.N >= wide::BN_W;
+    const char *wv = getenv("GB_OZAKI_WIDE");
+    const bool wide = !(wv && wv[0] == '0') && g.N >= wide::BN_W;
     const int bn = wide ? wide::BN_W : BN;
     const int64_t kp = ceil_div(g.K, BK) * BK;
     const int64_t mp = ceil_div(g.M, BM) * BM, np = ceil_div(g.N, bn) * bn;

@@ -167,3 +167,29 @@ def test_ozaki_nonfinite_propagate(torch, mode):
     assert np.array_equal(np.sign(got[inf]), np.sign(want[inf]))
     fin = np.isfinite(want)
     assert np.abs(got[fin] - want[fin]).max() <= 1e-12 * np.abs(want[fin]).max()
+
+
+@pytest.mark.parametrize("mode", ["NN", "TN", "NT", "TT"])
+@pytest.mark.parametrize("M,N,K", [(640, 768, 1100), (300, 513, 2100)])
+def test_ozaki_wide_form_bit_identical_to_narrow(torch, mode, M, N, K):
+    """The 128 x 256 form (N >= 256) does the 128 x 128 form's arithmetic in
+    the same order: identical bits, ragged shapes and every layout, beta != 0
+    and a K past one exact chunk (1024)."""
+    import os
+    import gbblas
+    ta, tb = mode
+    ar, ac = op_shape(ta, M, K)
+    br, bc = op_shape(tb, K, N)
+    A = dev(oracle.fill(ar, ac, 71, kind=2))
+    B = dev(oracle.fill(br, bc, 72, kind=2))
+    C0 = oracle.fill(M, N, 73)
+    outs = []
+    for wide in ("1", "0"):
+        os.environ["GB_OZAKI_WIDE"] = wide
+        try:
+            C = dev(C0)
+            gbblas.dgemm(ta, tb, M, N, K, 1.25, A, ac, B, bc, -0.5, C, N, algo=gbblas.ALGO_OZAKI)
+            outs.append(host(C).tobytes())
+        finally:
+            os.environ.pop("GB_OZAKI_WIDE", None)
+    assert outs[0] == outs[1]
