@@ -879,7 +879,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 int tm, tn;
                 tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
                 const int64_t row0 = (int64_t)tm * BM + (warp % 4) * 32;
-                const int64_t c0 = (int64_t)tn * BN + ((warp - 2) / 4) * 128;
+                const int64_t c0 = (int64_t)tn * BN + (half < 0 ? ((warp - 2) / 4) * 128 : half * 128);
                 unsigned cb[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
@@ -916,11 +916,16 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 if (lane == 0) ptx::mbar_arrive(&acc_empty[b]);
             }
             if (!go) break;
+            // a half tile of the tail (128 columns in accumulator columns 0..127) is stored by the
+            // warps of column half 0; the other four folded columns the MMA did not write
+            const int tl = blockIdx.x + (it - 1) * gridDim.x;
+            const int hf = tl < p.half_start ? -1 : ((tl - p.half_start) & 1);
+            if (hf >= 0 && warp >= 6) continue;
             int tm, tn;
             tile_coords(t, p.tiles_m, p.tiles_n, tm, tn);
             const int wi = warp - 2;
             const int64_t row0 = (int64_t)tm * BM + (warp % 4) * 32;
-            const int64_t c0 = (int64_t)tn * BN + (wi / 4) * 128;
+            const int64_t c0 = (int64_t)tn * BN + (hf < 0 ? (wi / 4) * 128 : hf * 128);
             const int *cs_w = col_scale + wi * 128;
             const int *rs_w = row_scale + wi * 32;
             // Direct store (FP16 pieces): lane l writes its row's 128 columns as 16-byte vectors,
@@ -1497,7 +1502,8 @@ static gb_status two_pass_launch(const GemmArgs &g, const PieceMaps &maps, int64
     {
         const char *e = getenv("GB_BF16X3_HALF");
         const int rem = tiles % grid;
-        if (!FOLD && BN == 256 && !(e && e[0] == '0') && rem > 0 && 2 * rem <= grid) half_start = tiles - rem;
+        if (BN == 256 && (!FOLD || EW == 8) && !(e && e[0] == '0') && rem > 0 && 2 * rem <= grid)
+            half_start = tiles - rem;
     }
     EpiParams p = base;
     p.num_kb = (int)(kp / BK);

@@ -439,6 +439,32 @@ def test_fp16x3_back_to_back_overlapped_scans(torch):
     assert host(C).tobytes() == host(C1).tobytes()
 
 
+@pytest.mark.parametrize("algo_name,accum", [("bf16x3", 0), ("fp16x3", 0), ("bf16x3", 128), ("fp16x3", 256)])
+def test_half_tile_tail_bit_identical(torch, algo_name, accum):
+    """A last wave at most half full runs as half tiles (128 columns) on twice
+    as many CTAs, for the one-accumulator form and the folding form alike:
+    the same bits as whole tiles (GB_BF16X3_HALF=0).  Shapes with 8 / 12
+    tail tiles for 152 / 148 SMs, and a ragged one."""
+    import os
+    import gbblas
+    algo = gbblas.ALGO_BF16X3 if algo_name == "bf16x3" else gbblas.ALGO_FP16X3
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for M, N, K in ((128 * 10, 256 * 16, 512), (128 * ((sms + 6) // 16) + 50, 256 * 16 + 100, 300)):
+        A = dev(oracle.fill(M, K, 991, dtype=np.float32))
+        B = dev(oracle.fill(K, N, 992, dtype=np.float32))
+        C0 = oracle.fill(M, N, 993, dtype=np.float32)
+        outs = []
+        for half in ("1", "0"):
+            os.environ["GB_BF16X3_HALF"] = half
+            try:
+                C = dev(C0)
+                gbblas.sgemm("N", "N", M, N, K, 1.5, A, K, B, N, -0.5, C, N, algo=algo, accum_k=accum)
+                outs.append(host(C).tobytes())
+            finally:
+                os.environ.pop("GB_BF16X3_HALF", None)
+        assert outs[0] == outs[1], (M, N, K)
+
+
 # ---------------------------------------------------------------- FP16X3
 # Two FP16 pieces (11 + 11 significand bits) of every value after its row of
 # op(A) / column of op(B) is scaled by a power of two that puts the line's
