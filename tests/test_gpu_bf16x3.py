@@ -442,9 +442,9 @@ def test_fp16x3_back_to_back_overlapped_scans(torch):
 @pytest.mark.parametrize("algo_name,accum", [("bf16x3", 0), ("fp16x3", 0), ("bf16x3", 128), ("fp16x3", 256)])
 def test_half_tile_tail_bit_identical(torch, algo_name, accum):
     """A last wave at most half full runs as half tiles (128 columns) on twice
-    as many CTAs, for the one-accumulator form and the folding form alike:
-    the same bits as whole tiles (GB_BF16X3_HALF=0).  Shapes with 8 / 12
-    tail tiles for 152 / 148 SMs, and a ragged one."""
+    as many CTAs (by default for the one-accumulator form; the folding form
+    when GB_BF16X3_HALF=1): the same bits as whole tiles (GB_BF16X3_HALF=0).
+    Shapes with 8 / 12 tail tiles for 152 / 148 SMs, and a ragged one."""
     import os
     import gbblas
     algo = gbblas.ALGO_BF16X3 if algo_name == "bf16x3" else gbblas.ALGO_FP16X3
