@@ -202,7 +202,7 @@ __device__ __forceinline__ void split_entry_guard(const unsigned long long *done
 
 // ------------------------------------------------------------------ scan
 // Largest |x| bit pattern of every row of op(X) (rows x K) -- non-negative
-// floats order as their bit patterns -- by atomicMax from 64 x 64 tiles.
+// floats order as their bit patterns -- by atomicMax from 64 x 256 tiles.
 // Each line's entry is (gen << 32) | bits with the call's generation `gen`
 // (larger than any earlier call's on the stream), so no clearing is needed
 // between calls: every line receives its call's value, which is larger than
@@ -236,44 +236,56 @@ __global__ void __launch_bounds__(256) maxbits_kernel(const __grid_constant__ Sc
     const int w = b < a.op[0].tiles ? 0 : 1;
     if (w) b -= a.op[0].tiles;
     const ScanOp &o = a.op[w];
-    const int64_t r0 = (b / o.tiles_k) * 64, k0 = (b % o.tiles_k) * 64;
+    // a CTA: 64 lines x 256 k (four 64-k blocks), one atomic per line
+    const int64_t r0 = (b / o.tiles_k) * 64, kb0 = (b % o.tiles_k) * 256;
     const int t = threadIdx.x, c4 = 4 * (t % 16), rl = t / 16;
     const unsigned long long tag = (unsigned long long)a.gen << 32;
     if (!o.trans) {   // 16 threads (a half warp) per row, 4 k each
+        unsigned m[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int64_t r = r0 + rl + 16 * i, k = k0 + c4;
-            unsigned m = 0;
-            if (r < o.rows) {
+        for (int sb = 0; sb < 4; sb++) {
+            const int64_t k = kb0 + 64 * sb + c4;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int64_t r = r0 + rl + 16 * i;
+                if (r >= o.rows || k >= a.K) continue;
                 const float *src = o.X + r * o.ldx + k;
                 if (a.vec && k + 3 < a.K) {
                     const float4 x = __ldg(reinterpret_cast<const float4 *>(src));
-                    m = max(max(absbits(x.x), absbits(x.y)), max(absbits(x.z), absbits(x.w)));
+                    m[i] = max(m[i], max(max(absbits(x.x), absbits(x.y)), max(absbits(x.z), absbits(x.w))));
                 } else {
 #pragma unroll
                     for (int q = 0; q < 4; q++)
-                        if (k + q < a.K) m = max(m, absbits(src[q]));
+                        if (k + q < a.K) m[i] = max(m[i], absbits(src[q]));
                 }
             }
-#pragma unroll
-            for (int s = 8; s >= 1; s >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, s));
-            if ((t & 15) == 0 && r < o.rows) atomicMax(&o.out[r], tag | m);
         }
-    } else {
-        unsigned m[4] = {0u, 0u, 0u, 0u};   // 4 consecutive rows, 4 k each
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int64_t k = k0 + rl + 16 * i, r = r0 + c4;
-            if (k >= a.K) continue;
-            const float *src = o.X + k * o.ldx + r;
-            if (a.vec && r + 3 < o.rows) {
-                const float4 x = __ldg(reinterpret_cast<const float4 *>(src));
-                m[0] = max(m[0], absbits(x.x)); m[1] = max(m[1], absbits(x.y));
-                m[2] = max(m[2], absbits(x.z)); m[3] = max(m[3], absbits(x.w));
-            } else {
+            const int64_t r = r0 + rl + 16 * i;
+            unsigned mi = m[i];
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (r + q < o.rows) m[q] = max(m[q], absbits(src[q]));
+            for (int s = 8; s >= 1; s >>= 1) mi = max(mi, __shfl_xor_sync(0xffffffffu, mi, s));
+            if ((t & 15) == 0 && r < o.rows) atomicMax(&o.out[r], tag | mi);
+        }
+    } else {
+        unsigned m[4] = {0u, 0u, 0u, 0u};   // 4 consecutive rows, 4 k each per 64-k block
+#pragma unroll
+        for (int sb = 0; sb < 4; sb++) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int64_t k = kb0 + 64 * sb + rl + 16 * i, r = r0 + c4;
+                if (k >= a.K) continue;
+                const float *src = o.X + k * o.ldx + r;
+                if (a.vec && r + 3 < o.rows) {
+                    const float4 x = __ldg(reinterpret_cast<const float4 *>(src));
+                    m[0] = max(m[0], absbits(x.x)); m[1] = max(m[1], absbits(x.y));
+                    m[2] = max(m[2], absbits(x.z)); m[3] = max(m[3], absbits(x.w));
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (r + q < o.rows) m[q] = max(m[q], absbits(src[q]));
+                }
             }
         }
 #pragma unroll
@@ -1633,7 +1645,7 @@ static gb_status two_pass(const GemmArgs &g, int np, int fold_kb, bool f16) {
         sc.done = gdone;
         sc.expect = expect;
         sc.scan_done = scan_done;
-        const int64_t tk = ceil_div(g.K, 64);
+        const int64_t tk = ceil_div(g.K, 256);   // a scan CTA covers 64 lines x 256 k
         sc.op[0] = ScanOp{(const float *)g.A, g.lda, g.M, tk, ceil_div(g.M, 64) * tk, g.ta ? 1 : 0, bits};
         sc.op[1] = ScanOp{(const float *)g.B, g.ldb, g.N, tk, ceil_div(g.N, 64) * tk, g.tb ? 0 : 1, bits + g.M};
         const int64_t blocks = sc.op[0].tiles + sc.op[1].tiles;
