@@ -1131,8 +1131,11 @@ def run_serve(ctx):
     l0 = gb.launch_count()
     sampler = ClockSampler(ctx.local)
     sampler.start()
-    main = serve("streams=%d grouped=%d graphs=%d" % (args.serve_streams, args.serve_grouped, args.serve_graphs),
-                 streams=args.serve_streams, use_grouped=args.serve_grouped, use_graphs=args.serve_graphs)
+    main = serve("streams=%d grouped=%d graphs=%d short_us=%g short_streams=%d"
+                 % (args.serve_streams, args.serve_grouped, args.serve_graphs, args.serve_short_us,
+                    args.serve_short_streams),
+                 streams=args.serve_streams, use_grouped=args.serve_grouped, use_graphs=args.serve_graphs,
+                 short_us=args.serve_short_us, short_streams=args.serve_short_streams)
     clocks = sampler.stop()
     launches = gb.launch_count() - l0
     plain = serve("plain", streams=1, use_grouped=0, use_graphs=0) if not args.no_plain else None
@@ -1161,7 +1164,8 @@ def run_serve(ctx):
     config = {"workload": "serving stream: Poisson %g req/s for %g s (seed 4), mixed GEMM/thinB/shortA/transpose/"
                           "Jacobi, 70/30 FP32/FP64, 48 GB HBM budget" % (args.rate, args.duration),
               "requests": len(reqs), "budget_gb": args.budget_gb, "streams": args.serve_streams,
-              "grouped": args.serve_grouped, "graphs": args.serve_graphs, "ring_slots": slots,
+              "grouped": args.serve_grouped, "graphs": args.serve_graphs, "short_us": args.serve_short_us,
+              "short_streams": args.serve_short_streams, "ring_slots": slots,
               "max_dim": args.max_dim, "tuned": tuned}
     line = base_line(ctx, "serve p50/p99, req/s", main["req_per_s"], "req/s", main["submit_span_s"] * 1e3, 1,
                      "f32+f64", config)
@@ -1236,9 +1240,12 @@ def main():
     ap.add_argument("--drain-timeout", type=float, default=120.0)
     ap.add_argument("--iso-sample", type=int, default=200)
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--serve-streams", type=int, default=4, help="serve: stream pool of the measured server")
+    ap.add_argument("--serve-streams", type=int, default=6, help="serve: stream pool of the measured server")
     ap.add_argument("--serve-grouped", type=int, default=1, help="serve: group small GEMMs (1) or not (0)")
     ap.add_argument("--serve-graphs", type=int, default=1, help="serve: replay CUDA graphs (1) or not (0)")
+    ap.add_argument("--serve-short-us", type=float, default=200.0,
+                    help="serve: requests estimated below this go to the high-priority streams (0: off)")
+    ap.add_argument("--serve-short-streams", type=int, default=2, help="serve: high-priority streams")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

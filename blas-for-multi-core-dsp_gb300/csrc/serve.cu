@@ -112,7 +112,7 @@ struct Server {
     std::vector<std::map<GKey, cudaGraphExec_t>> execs;       // one-launch graphs per stream
     std::set<GKey> seen;                                      // buckets that ran once without a graph
     std::atomic<int64_t> graph_launches{0}, graph_instantiations{0};
-    size_t rr = 0;
+    size_t rr = 0, rr_short = 0;
     GroupRunner *grouped = nullptr;
     std::thread dispatcher;
     bool stop = false;
@@ -302,6 +302,31 @@ gb_status launch_request(Server *s, const gb_request &r, size_t si, bool *graphe
     return GB_OK;
 }
 
+// A request's duration at the rates the library reaches on GB300 (tensor-core GEMM forms ~300
+// TFLOP/s FP32 and ~35 FP64, HBM-bound streams ~5 TB/s), in microseconds: only to tell short
+// requests from long ones.
+double estimate_us(const gb_request &r) {
+    const double es = r.dtype_bits == 64 ? 8.0 : 4.0;
+    const double M = (double)r.M, N = (double)r.N, K = (double)r.K;
+    if (r.op == GB_OP_GEMM) {
+        const double flops = 2.0 * M * N * K;
+        const double bytes = es * (M * K + K * N + 2.0 * M * N);
+        return std::max(flops / (r.dtype_bits == 64 ? 35e6 : 300e6), bytes / 5e6) + 5.0;
+    }
+    if (r.op == GB_OP_TRANSPOSE) return 2.0 * es * M * N / 5e6 + 5.0;
+    return 2.0 * es * M * N * (double)std::max(r.iters, 1) / 8e6 + 5.0;   // Jacobi sweeps
+}
+
+// Short requests round-robin over the high-priority streams 0..h-1, the rest over h..n-1 (every
+// stream in turn when there is one stream or priorities are off).
+size_t pick_stream(Server *s, double est_us) {
+    const size_t n = s->streams.size();
+    if (n < 2 || s->cfg.short_us <= 0) return s->rr++ % n;
+    const size_t h = (size_t)s->cfg.short_streams;
+    if (est_us < s->cfg.short_us) return s->rr_short++ % h;
+    return h + (s->rr++ % (n - h));
+}
+
 void dispatcher_main(Server *s) {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
@@ -341,7 +366,7 @@ void dispatcher_main(Server *s) {
                 group_reqs.push_back(p);
                 continue;
             }
-            const size_t si = s->rr++ % s->streams.size();
+            const size_t si = pick_stream(s, estimate_us(p.r));
             cudaStream_t st = s->streams[si];
             Batch *b = new Batch{s, {{p.r.tag, p.t_submit}}, p.bytes};
             bool graphed = false;
@@ -357,7 +382,7 @@ void dispatcher_main(Server *s) {
             s->launches++;
         }
         if (!group.empty()) {
-            cudaStream_t st = s->streams[s->rr++ % s->streams.size()];
+            cudaStream_t st = s->streams[pick_stream(s, 0.0)];   // grouped launches are short
             Batch *b = new Batch{s, {}, 0};
             for (auto &p : group_reqs) {
                 b->reqs.push_back({p.r.tag, p.t_submit});
@@ -403,12 +428,14 @@ void gb_server_config_init(gb_server_config *c) {
     if (!c) return;
     memset(c, 0, sizeof(*c));
     c->hbm_budget_bytes = 48ull << 30;
-    c->streams = 4;
+    c->streams = 6;
     c->max_batch = 256;
     c->max_inflight = 1 << 20;
     c->use_graphs = 1;
     c->use_grouped = 1;
     c->group_max_work = 512.0 * 512.0 * 512.0;
+    c->short_us = 200.0;
+    c->short_streams = 2;
 }
 
 gb_status gb_server_create(const gb_server_config *cfg, gb_server **out) {
@@ -420,13 +447,20 @@ gb_status gb_server_create(const gb_server_config *cfg, gb_server **out) {
     GB_CHECK_ARG(c.streams >= 1 && c.streams <= 64, "gb_server_create: streams must be 1..64");
     GB_CHECK_ARG(c.max_batch >= 1 && c.max_batch <= 4096, "gb_server_create: max_batch must be 1..4096");
     GB_CHECK_ARG(c.max_inflight >= 1, "gb_server_create: max_inflight must be positive");
+    GB_CHECK_ARG(c.short_us <= 0 || c.streams < 2 || (c.short_streams >= 1 && c.short_streams < c.streams),
+                 "gb_server_create: short_streams must be 1..streams-1");
     Server *s = new Server();
     s->cfg = c;
     if (!c.dry_run) {
         cudaGetDevice(&s->device);
         for (int i = 0; i < c.streams; i++) {
+            // stream 0 carries the short requests at the device's highest priority (when there
+            // are at least two streams and short_us > 0)
+            int lo = 0, hi = 0;
+            cudaDeviceGetStreamPriorityRange(&lo, &hi);
+            const bool urgent = i < c.short_streams && c.streams >= 2 && c.short_us > 0;
             cudaStream_t st;
-            cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+            cudaError_t e = cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, urgent ? hi : lo);
             if (e != cudaSuccess) {
                 for (auto x : s->streams) cudaStreamDestroy(x);
                 delete s;

@@ -333,7 +333,7 @@ typedef struct gb_server_config {
     uint64_t workspace_bytes;   /* scratch reserved per stream at creation (0: grow)  */
     double   group_max_work;    /* GEMMs with M*N*K <= this, min(M,N) > 64 and algo
                                    AUTO go to grouped launches (default 512^3)        */
-    int32_t  streams;           /* device streams (default 4)                         */
+    int32_t  streams;           /* device streams (default 6)                         */
     int32_t  max_batch;         /* GEMMs per grouped launch (default 256)             */
     int32_t  max_inflight;      /* requests in flight at once (default 2^20)          */
     int32_t  use_graphs;        /* replay launches from CUDA graphs (1): grouped
@@ -343,6 +343,15 @@ typedef struct gb_server_config {
                                    bound before each capture                         */
     int32_t  use_grouped;       /* group small GEMMs (1); 0 = one launch per request  */
     int32_t  dry_run;           /* admission and bookkeeping only, no device work     */
+    double   short_us;          /* requests estimated below this many microseconds
+                                   (and grouped launches) go round-robin to the
+                                   first short_streams streams, created at the
+                                   device's highest priority, the rest round-robin
+                                   over the others, so that short work is not
+                                   queued behind long kernels (default 200; 0: one
+                                   pool, no priorities)                             */
+    int32_t  short_streams;     /* high-priority streams (default 2; < streams)     */
+    int32_t  reserved;
 } gb_server_config;
 
 typedef struct gb_server_stats {
