@@ -1092,6 +1092,7 @@ def run_serve(ctx):
 
     def serve(label, **cfg):
         srv = gb.Server(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), **cfg)
+        lats = {}
         free = list(range(slots))
         slot_of = {}
         t0 = time.perf_counter()
@@ -1103,12 +1104,14 @@ def run_serve(ctx):
             else:
                 lag = max(lag, -wait)
             while not free:   # every output slot is held by an unfinished request
-                for tag, _ in srv.poll():
+                for tag, lat in srv.poll():
                     free.append(slot_of.pop(tag))
+                    lats[tag] = lat
                 if not free:
                     time.sleep(50e-6)
-            for tag, _ in srv.poll():
+            for tag, lat in srv.poll():
                 free.append(slot_of.pop(tag))
+                lats[tag] = lat
             slot = free.pop()
             slot_of[i] = slot
             srv.submit(make_request(i, r, slot))
@@ -1118,15 +1121,24 @@ def run_serve(ctx):
             drained = True
         except gb.GBError:
             drained = False
+        for tag, lat in srv.poll(1 << 20):
+            lats[tag] = lat
         st = srv.stats()
         srv.close()
+        # latency by request class (the 1 % slowest of each)
+        per = {}
+        for tag, lat in lats.items():
+            r = reqs[tag]
+            per.setdefault("%s_f%d" % (("gemm", "thinB", "shortA", "transpose", "jacobi")[r[1]], r[2]), []).append(lat)
+        by_class = {k: {"n": len(v), "p50_ms": 1e3 * float(np.percentile(v, 50)),
+                        "p99_ms": 1e3 * float(np.percentile(v, 99))} for k, v in sorted(per.items())}
         return {"label": label, "p50_ms": st["p50_s"] * 1e3, "p99_ms": st["p99_s"] * 1e3,
                 "mean_ms": st["mean_s"] * 1e3, "req_per_s": st["req_per_s"], "completed": st["completed"],
                 "submitted": st["submitted"], "failed": st["failed"], "launches": st["launches"],
                 "grouped_launches": st["grouped_launches"], "grouped_requests": st["grouped_requests"],
                 "graph_launches": st["graph_launches"], "graph_instantiations": st["graph_instantiations"],
                 "graph_fraction": st["graph_launches"] / st["launches"] if st["launches"] else 0.0,
-                "drained": drained, "submit_lag_s": lag, "submit_span_s": submit_end}
+                "drained": drained, "submit_lag_s": lag, "submit_span_s": submit_end, "by_class": by_class}
 
     l0 = gb.launch_count()
     sampler = ClockSampler(ctx.local)
