@@ -1091,7 +1091,10 @@ def run_serve(ctx):
         return gb.request(gb.OP_STENCIL, bits, g, g, A=optr, C=optr + grid_bytes * es, iters=iters, tag=i)
 
     def serve(label, **cfg):
-        srv = gb.Server(hbm_budget_bytes=int(args.budget_gb * (1 << 30)), **cfg)
+        # each stream's workspace reserved up front (a workspace that grows mid-run frees its old
+        # buffer, and cudaFree waits for the whole device: every stream stalls)
+        srv = gb.Server(hbm_budget_bytes=int(args.budget_gb * (1 << 30)),
+                        workspace_bytes=int(args.workspace_gb * (1 << 30)), **cfg)
         lats = {}
         free = list(range(slots))
         slot_of = {}
@@ -1175,7 +1178,8 @@ def run_serve(ctx):
     offered = sum(share[k] / len(reqs) * args.rate * float(np.mean(v)) for k, v in by_class.items())
     config = {"workload": "serving stream: Poisson %g req/s for %g s (seed 4), mixed GEMM/thinB/shortA/transpose/"
                           "Jacobi, 70/30 FP32/FP64, 48 GB HBM budget" % (args.rate, args.duration),
-              "requests": len(reqs), "budget_gb": args.budget_gb, "streams": args.serve_streams,
+              "requests": len(reqs), "budget_gb": args.budget_gb, "workspace_gb_per_stream": args.workspace_gb,
+              "streams": args.serve_streams,
               "grouped": args.serve_grouped, "graphs": args.serve_graphs, "short_us": args.serve_short_us,
               "short_streams": args.serve_short_streams, "ring_slots": slots,
               "max_dim": args.max_dim, "tuned": tuned}
@@ -1247,6 +1251,7 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     ap.add_argument("--budget-gb", type=float, default=48.0, help="serve: HBM admission budget")
+    ap.add_argument("--workspace-gb", type=float, default=1.0, help="serve: workspace reserved per stream")
     ap.add_argument("--max-dim", type=int, default=65536, help="serve: cap on log-uniform sizes")
     ap.add_argument("--slots", type=int, default=64, help="serve: output ring slots (max in flight)")
     ap.add_argument("--drain-timeout", type=float, default=120.0)
