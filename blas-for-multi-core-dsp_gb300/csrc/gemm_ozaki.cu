@@ -9,7 +9,7 @@
 //
 // Each row i of op(A) is scaled by 2^-e_i (e_i: max_k |a_ik| < 2^e_i) and
 // written as s balanced base-256 digits, a_ik = 2^(e_i+1) * sum_t v_ikt 2^-8t
-// (+ a remainder below 2^(e_i+1-8s)), v in [-128, 127] (the leading digit
+// (+ a remainder of at most half of 2^(e_i+1-8s)), v in [-128, 127] (the leading digit
 // in [-128, 128]); columns of op(B) likewise with exponents f_j and digits w.
 // Then
 //     C_ij ~= 2^(e_i+f_j+2) sum_{t+u <= s+1} 2^-8(t+u) (V_t W_u^T)_ij .
@@ -148,8 +148,10 @@ static void launch_maxexp_strided(const double *X, int64_t ld, int64_t cols, int
 }
 
 // ---------------------------------------------------------------- digits
-// s balanced base-256 digits of x (|x| < 2^e): N = +-trunc(|x| 2^(8s-1-e)),
-// |N| < 2^(8s-1), cut from the least significant digit up (d = N mod 256 in
+// s balanced base-256 digits of x (|x| < 2^e): N = +-round(|x| 2^(8s-1-e))
+// (to nearest: the representation error is half a unit of the last digit
+// either way, where truncation erred up to a whole unit toward zero),
+// |N| <= 2^(8s-1), cut from the least significant digit up (d = N mod 256 in
 // [-128, 127], N = (N - d) / 256), so x ~= 2^(e+1) sum_t d_t 2^-8t; the
 // leading digit is in [-128, 128].  Written as BF16, most significant first.
 __device__ __forceinline__ void digits(double x, int e, int s, unsigned short *out, int64_t stride) {
@@ -163,9 +165,16 @@ __device__ __forceinline__ void digits(double x, int e, int s, unsigned short *o
         m |= 1ull << 52;
         ex = E - 1075;
     }
-    const int shift = ex + 8 * s - 1 - e;   // F = m * 2^shift < 2^(8s-1) <= 2^71
+    const int shift = ex + 8 * s - 1 - e;   // F = m * 2^shift <= 2^(8s-1) <= 2^71, rounded to nearest
     unsigned __int128 F = 0;
-    if (m != 0 && shift > -64) F = shift >= 0 ? ((unsigned __int128)m << shift) : (unsigned __int128)(m >> (-shift));
+    if (m != 0 && shift > -64) {
+        if (shift >= 0) {
+            F = (unsigned __int128)m << shift;
+        } else {   // half a unit of the last digit added first: the dropped part errs both ways
+            const int rs = -shift;
+            F = (unsigned __int128)((m + (1ull << (rs - 1))) >> rs);
+        }
+    }
     __int128 N = (b >> 63) ? -(__int128)F : (__int128)F;
     for (int t = s; t >= 1; t--) {
         const int d = (int)(((long long)N + 128) & 255) - 128;
