@@ -1146,11 +1146,12 @@ def run_serve(ctx):
     l0 = gb.launch_count()
     sampler = ClockSampler(ctx.local)
     sampler.start()
-    main = serve("streams=%d grouped=%d graphs=%d short_us=%g short_streams=%d"
+    main = serve("streams=%d grouped=%d graphs=%d short_us=%g short_streams=%d long_sm=%d%%"
                  % (args.serve_streams, args.serve_grouped, args.serve_graphs, args.serve_short_us,
-                    args.serve_short_streams),
+                    args.serve_short_streams, args.serve_long_sm),
                  streams=args.serve_streams, use_grouped=args.serve_grouped, use_graphs=args.serve_graphs,
-                 short_us=args.serve_short_us, short_streams=args.serve_short_streams)
+                 short_us=args.serve_short_us, short_streams=args.serve_short_streams,
+                 long_sm_percent=args.serve_long_sm)
     clocks = sampler.stop()
     launches = gb.launch_count() - l0
     plain = serve("plain", streams=1, use_grouped=0, use_graphs=0) if not args.no_plain else None
@@ -1181,7 +1182,8 @@ def run_serve(ctx):
               "requests": len(reqs), "budget_gb": args.budget_gb, "workspace_gb_per_stream": args.workspace_gb,
               "streams": args.serve_streams,
               "grouped": args.serve_grouped, "graphs": args.serve_graphs, "short_us": args.serve_short_us,
-              "short_streams": args.serve_short_streams, "ring_slots": slots,
+              "short_streams": args.serve_short_streams, "long_sm_percent": args.serve_long_sm,
+              "ring_slots": slots,
               "max_dim": args.max_dim, "tuned": tuned}
     line = base_line(ctx, "serve p50/p99, req/s", main["req_per_s"], "req/s", main["submit_span_s"] * 1e3, 1,
                      "f32+f64", config)
@@ -1263,6 +1265,7 @@ def main():
     ap.add_argument("--serve-short-us", type=float, default=200.0,
                     help="serve: requests estimated below this go to the high-priority streams (0: off)")
     ap.add_argument("--serve-short-streams", type=int, default=2, help="serve: high-priority streams")
+    ap.add_argument("--serve-long-sm", type=int, default=100, help="serve: percent of SMs a long request plans for")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

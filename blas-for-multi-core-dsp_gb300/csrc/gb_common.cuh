@@ -43,6 +43,7 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 
 // Number of SMs of the current device (cached per device).
 int sm_count();
+void set_sm_cap(int cap);   // this host thread's launches plan for at most cap SMs (0: all)
 // Opt-in shared memory per block (bytes) of the current device.
 int smem_optin();
 

@@ -41,6 +41,11 @@ gb_status cuda_status(cudaError_t e, const char *where) {
 
 static const int kMaxDev = 64;
 
+// A cap on the SMs this host thread's launches plan for (0: none): the persistent kernels size
+// their grids from sm_count(), so a capped call leaves the other SMs to other streams' work.
+static thread_local int t_sm_cap = 0;
+void set_sm_cap(int cap) { t_sm_cap = cap > 0 ? cap : 0; }
+
 int sm_count() {
     static int cache[kMaxDev] = {0};
     int dev = 0;
@@ -51,7 +56,7 @@ int sm_count() {
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         cache[dev] = n > 0 ? n : 148;
     }
-    return cache[dev];
+    return t_sm_cap > 0 && t_sm_cap < cache[dev] ? t_sm_cap : cache[dev];
 }
 
 static uint64_t device_bit() {

@@ -366,11 +366,20 @@ void dispatcher_main(Server *s) {
                 group_reqs.push_back(p);
                 continue;
             }
-            const size_t si = pick_stream(s, estimate_us(p.r));
+            const double est = estimate_us(p.r);
+            const size_t si = pick_stream(s, est);
+            // a long request on the normal streams plans for a share of the SMs only
+            const bool capped = s->cfg.long_sm_percent < 100 && s->cfg.short_us > 0 && est >= s->cfg.short_us &&
+                                s->streams.size() >= 2;
+            if (capped) {
+                set_sm_cap(0);
+                set_sm_cap((int)((int64_t)sm_count() * s->cfg.long_sm_percent / 100));
+            }
             cudaStream_t st = s->streams[si];
             Batch *b = new Batch{s, {{p.r.tag, p.t_submit}}, p.bytes};
             bool graphed = false;
             gb_status rc = s->cfg.dry_run ? GB_OK : launch_request(s, p.r, si, &graphed);
+            if (capped) set_sm_cap(0);
             if (rc != GB_OK) {
                 std::lock_guard<std::mutex> g(s->mu);
                 s->failed++;
@@ -436,6 +445,7 @@ void gb_server_config_init(gb_server_config *c) {
     c->group_max_work = 512.0 * 512.0 * 512.0;
     c->short_us = 200.0;
     c->short_streams = 2;
+    c->long_sm_percent = 100;
 }
 
 gb_status gb_server_create(const gb_server_config *cfg, gb_server **out) {
@@ -447,8 +457,9 @@ gb_status gb_server_create(const gb_server_config *cfg, gb_server **out) {
     GB_CHECK_ARG(c.streams >= 1 && c.streams <= 64, "gb_server_create: streams must be 1..64");
     GB_CHECK_ARG(c.max_batch >= 1 && c.max_batch <= 4096, "gb_server_create: max_batch must be 1..4096");
     GB_CHECK_ARG(c.max_inflight >= 1, "gb_server_create: max_inflight must be positive");
-    GB_CHECK_ARG(c.short_us <= 0 || c.streams < 2 || (c.short_streams >= 1 && c.short_streams < c.streams),
-                 "gb_server_create: short_streams must be 1..streams-1");
+    GB_CHECK_ARG(c.short_us <= 0 || c.short_streams >= 1, "gb_server_create: short_streams must be positive");
+    if (c.short_streams >= c.streams) c.short_streams = c.streams - 1;   // at least one stream for long work
+    GB_CHECK_ARG(c.long_sm_percent >= 1 && c.long_sm_percent <= 100, "gb_server_create: long_sm_percent must be 1..100");
     Server *s = new Server();
     s->cfg = c;
     if (!c.dry_run) {

@@ -80,7 +80,7 @@ class ServerConfig(ctypes.Structure):
                 ("group_max_work", ctypes.c_double), ("streams", ctypes.c_int32), ("max_batch", ctypes.c_int32),
                 ("max_inflight", ctypes.c_int32), ("use_graphs", ctypes.c_int32), ("use_grouped", ctypes.c_int32),
                 ("dry_run", ctypes.c_int32), ("short_us", ctypes.c_double), ("short_streams", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("long_sm_percent", ctypes.c_int32)]
 
 
 class ServerStats(ctypes.Structure):

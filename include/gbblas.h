@@ -350,8 +350,11 @@ typedef struct gb_server_config {
                                    over the others, so that short work is not
                                    queued behind long kernels (default 200; 0: one
                                    pool, no priorities)                             */
-    int32_t  short_streams;     /* high-priority streams (default 2; < streams)     */
-    int32_t  reserved;
+    int32_t  short_streams;     /* high-priority streams (default 2; at most
+                                   streams - 1 are used)                            */
+    int32_t  long_sm_percent;   /* long requests plan their persistent grids for
+                                   this share of the SMs, leaving the rest to short
+                                   work (1..100; default 100: all)                  */
 } gb_server_config;
 
 typedef struct gb_server_stats {

@@ -62,7 +62,7 @@ def test_malformed_requests_are_rejected(L, bad):
 
 def test_server_config_validation(L):
     for field, val in (("streams", 0), ("max_batch", 0), ("hbm_budget_bytes", 0), ("max_inflight", 0),
-                       ("short_streams", 0), ("short_streams", 6)):
+                       ("short_streams", 0), ("long_sm_percent", 0), ("long_sm_percent", 101)):
         c = gbblas.ServerConfig()
         L.gb_server_config_init(ctypes.byref(c))
         c.dry_run = 1
