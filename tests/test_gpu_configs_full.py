@@ -35,7 +35,8 @@ def torch():
 
 def _fill(torch, rows, cols, ld, seed, kind, bits):
     import gbblas
-    t = torch.empty((rows, ld), dtype=torch.float64 if bits == 64 else torch.float32, device="cuda:0")
+    # the padding columns keep a finite sentinel (never recycled memory, which may hold NaNs)
+    t = torch.full((rows, ld), 7.25, dtype=torch.float64 if bits == 64 else torch.float32, device="cuda:0")
     gbblas.fill(t, rows, cols, ld, seed, kind, bits)
     return t
 
@@ -103,7 +104,7 @@ def test_sgemm_4096_ld4112_alpha1p5_beta_m0p5_all_forms(torch, mode):
         torch.cuda.synchronize()
         errs[name] = _sub_error(C, rows, cols, ref, rn2, cn2, ALPHA, BETA, c0)
         # the padding columns of C are never written
-        assert torch.equal(C[:, N:], C0[:, N:])
+        assert torch.equal(C[:, N:], C0[:, N:]), name
     bound = 2 * K * 2.0 ** -24
     assert all(e <= bound for e in errs.values()), errs
     assert errs["BF16X6"] <= errs["SIMT"], errs
