@@ -13,6 +13,7 @@
 // registers while the current one is consumed.  alpha/beta are applied in
 // the epilogue (BLAS, scalar-beta or accumulate semantics).
 #include "gb_common.cuh"
+#include "sm100_ptx.cuh"
 
 namespace gb {
 namespace {
@@ -112,11 +113,13 @@ __global__ void __launch_bounds__(NT, 2) sgemm_simt_kernel(const float *__restri
     const int tx = tid % 16, ty = tid / 16;
     const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
 
-    float acc[8][8];
+    // acc[i][jj]: the outputs (i, 2jj) and (i, 2jj + 1) as one packed FP32x2 register; each output
+    // still sees its own FMAs in k order, so results equal one FFMA per product
+    uint64_t acc[8][4];
 #pragma unroll
     for (int i = 0; i < 8; i++)
 #pragma unroll
-        for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
+        for (int jj = 0; jj < 4; jj++) acc[i][jj] = 0ull;
 
     float ra[4], rb[4];
     ldg_a<TA, VEC>(A, p, m0, 0, ra);
@@ -135,19 +138,21 @@ __global__ void __launch_bounds__(NT, 2) sgemm_simt_kernel(const float *__restri
         }
 #pragma unroll
         for (int kk = 0; kk < BK; kk++) {
-            float a[8], b[8];
+            float a[8];
             float4 a0 = *reinterpret_cast<const float4 *>(&As[cur][kk][ty * 4]);
             float4 a1 = *reinterpret_cast<const float4 *>(&As[cur][kk][64 + ty * 4]);
             float4 b0 = *reinterpret_cast<const float4 *>(&Bs[cur][kk][tx * 4]);
             float4 b1 = *reinterpret_cast<const float4 *>(&Bs[cur][kk][64 + tx * 4]);
             a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w;
             a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
-            b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w;
-            b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
+            const uint64_t b2[4] = {ptx::f2_pack(b0.x, b0.y), ptx::f2_pack(b0.z, b0.w), ptx::f2_pack(b1.x, b1.y),
+                                    ptx::f2_pack(b1.z, b1.w)};
 #pragma unroll
-            for (int i = 0; i < 8; i++)
+            for (int i = 0; i < 8; i++) {
+                const uint64_t ai = ptx::f2_pack(a[i], a[i]);
 #pragma unroll
-                for (int j = 0; j < 8; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+                for (int jj = 0; jj < 4; jj++) acc[i][jj] = ptx::f2_fma_rn(ai, b2[jj], acc[i][jj]);
+            }
         }
         if (more) {
             sts_a<TA>(As[cur ^ 1], ra);
@@ -161,12 +166,15 @@ __global__ void __launch_bounds__(NT, 2) sgemm_simt_kernel(const float *__restri
     for (int i = 0; i < 8; i++) {
         int64_t m = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + (i - 4));
         if (m >= p.M) continue;
+        float accf[8];
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) ptx::f2_unpack(acc[i][jj], accf[2 * jj], accf[2 * jj + 1]);
 #pragma unroll
         for (int j = 0; j < 8; j++) {
             int64_t n = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
             if (n >= p.N) continue;
             float *cp = C + m * p.ldc + n;
-            float v = p.alpha * acc[i][j];
+            float v = p.alpha * accf[j];
             if (p.semantics == GB_SEM_BLAS) {
                 if (p.beta != 0.f) v = fmaf(p.beta, *cp, v);
             } else if (p.semantics == GB_SEM_SCALAR_BETA) {

@@ -176,33 +176,10 @@ __device__ __forceinline__ uint64_t scaled_mantissa_fast(uint32_t hi, uint32_t l
     return shr64(((uint64_t)((hi & 0xFFFFFu) | 0x100000u) << 32) | lo, rs);
 }
 
-// Two FP32 values in one 64-bit register (value 0 in the low half) for the
-// packed f32x2 instructions, which apply the same IEEE operation and rounding
-// to both halves: one instruction per step of the digit cut serves two values.
-__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
-    uint64_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
-    uint64_t r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ uint64_t f2_fma_rz(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t r;
-    asm("fma.rz.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-__device__ __forceinline__ uint64_t f2_fma_rn(uint64_t a, uint64_t b, uint64_t c) {
-    uint64_t r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
 // the two halves as a bf16x2 word (exact: the digits are small integers)
 __device__ __forceinline__ uint32_t f2_bf16x2(uint64_t v) {
     float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+    ptx::f2_unpack(v, lo, hi);
     return bf16x2_bits(__floats2bfloat162_rn(lo, hi));
 }
 
@@ -215,29 +192,29 @@ __device__ __forceinline__ uint32_t f2_bf16x2(uint64_t v) {
 // hi = trunc(f / 2^s) by a round-toward-zero fma onto +-2^23 and f - 2^s hi.
 __device__ __forceinline__ void digit_words(uint64_t F0, uint32_t hi0, uint64_t F1, uint32_t hi1, uint32_t (&w)[S]) {
     const uint32_t C0 = (hi0 & 0x80000000u) | 0x4B000000u, C1 = (hi1 & 0x80000000u) | 0x4B000000u;
-    const uint64_t M = f2_pack(__uint_as_float(C0), __uint_as_float(C1));
+    const uint64_t M = ptx::f2_pack(__uint_as_float(C0), __uint_as_float(C1));
     const uint32_t fh0 = (uint32_t)(F0 >> 32), fl0 = (uint32_t)F0, fh1 = (uint32_t)(F1 >> 32), fl1 = (uint32_t)F1;
-    const uint64_t f0 = f2_sub(f2_pack(__uint_as_float(__funnelshift_r(fl0, fh0, 30) | C0),   // bits 30..47
+    const uint64_t f0 = ptx::f2_sub(ptx::f2_pack(__uint_as_float(__funnelshift_r(fl0, fh0, 30) | C0),   // bits 30..47
                                        __uint_as_float(__funnelshift_r(fl1, fh1, 30) | C1)), M);
-    const uint64_t f1 = f2_sub(f2_pack(__uint_as_float(((fl0 >> 12) & 0x3FFFFu) | C0),        // bits 12..29
+    const uint64_t f1 = ptx::f2_sub(ptx::f2_pack(__uint_as_float(((fl0 >> 12) & 0x3FFFFu) | C0),        // bits 12..29
                                        __uint_as_float(((fl1 >> 12) & 0x3FFFFu) | C1)), M);
-    const uint64_t f2 = f2_sub(f2_pack(__uint_as_float((fl0 & 0xFFFu) | C0),                  // bits 0..11
+    const uint64_t f2 = ptx::f2_sub(ptx::f2_pack(__uint_as_float((fl0 & 0xFFFu) | C0),                  // bits 0..11
                                        __uint_as_float((fl1 & 0xFFFu) | C1)), M);
-    const uint64_t s12 = f2_pack(1.0f / 4096.0f, 1.0f / 4096.0f), m12 = f2_pack(-4096.0f, -4096.0f);
-    const uint64_t s6 = f2_pack(0.015625f, 0.015625f), m6 = f2_pack(-64.0f, -64.0f);
+    const uint64_t s12 = ptx::f2_pack(1.0f / 4096.0f, 1.0f / 4096.0f), m12 = ptx::f2_pack(-4096.0f, -4096.0f);
+    const uint64_t s6 = ptx::f2_pack(0.015625f, 0.015625f), m6 = ptx::f2_pack(-64.0f, -64.0f);
 #pragma unroll
     for (int i = 0; i < 2; i++) {
         const uint64_t f = i ? f1 : f0;
-        const uint64_t h = f2_sub(f2_fma_rz(f, s12, M), M);
-        const uint64_t r = f2_fma_rn(m12, h, f);
-        const uint64_t h2 = f2_sub(f2_fma_rz(r, s6, M), M);
+        const uint64_t h = ptx::f2_sub(ptx::f2_fma_rz(f, s12, M), M);
+        const uint64_t r = ptx::f2_fma_rn(m12, h, f);
+        const uint64_t h2 = ptx::f2_sub(ptx::f2_fma_rz(r, s6, M), M);
         w[3 * i] = f2_bf16x2(h);
         w[3 * i + 1] = f2_bf16x2(h2);
-        w[3 * i + 2] = f2_bf16x2(f2_fma_rn(m6, h2, r));
+        w[3 * i + 2] = f2_bf16x2(ptx::f2_fma_rn(m6, h2, r));
     }
-    const uint64_t h = f2_sub(f2_fma_rz(f2, s6, M), M);
+    const uint64_t h = ptx::f2_sub(ptx::f2_fma_rz(f2, s6, M), M);
     w[6] = f2_bf16x2(h);
-    w[7] = f2_bf16x2(f2_fma_rn(m6, h, f2));
+    w[7] = f2_bf16x2(ptx::f2_fma_rn(m6, h, f2));
 }
 
 // The 16 values of one box row -> 8 digit slices of 8 bf16x2 words.
