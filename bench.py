@@ -65,6 +65,63 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+def _gpu_local_cpus(torch, dev):
+    """The host cores attached to GPU `dev` (the sysfs local_cpulist of its PCI function) that
+    this process may run on; empty when that is unknown."""
+    try:
+        p = torch.cuda.get_device_properties(dev)
+        path = "/sys/bus/pci/devices/%04x:%02x:%02x.0/local_cpulist" % (p.pci_domain_id, p.pci_bus_id,
+                                                                          p.pci_device_id)
+        with open(path) as f:
+            return parse_cpulist(f.read()) & os.sched_getaffinity(0)
+    except (AttributeError, OSError, ValueError):
+        return set()
+
+
+def parse_cpulist(spec):
+    """A sysfs CPU list ("0-3,8,10-11") as a set of core numbers."""
+    cpus = set()
+    for part in spec.strip().split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        elif part:
+            cpus.add(int(part))
+    return cpus
+
+
+class near_gpu:
+    """Context: the enclosed host allocations run on the GPU's local cores, so that pinned
+    buffers are first touched, and placed, on the memory node next to the GPU (a far node puts
+    every host<->device copy across the socket link).  The process's own core set comes back
+    on exit; where the local cores are unknown or not ours, nothing changes."""
+
+    def __init__(self, torch, dev):
+        self.torch, self.dev, self.saved, self.note = torch, dev, None, "pinned"
+
+    def __enter__(self):
+        local = _gpu_local_cpus(self.torch, self.dev)
+        allowed = os.sched_getaffinity(0)
+        if not local:
+            self.note = "pinned (the GPU's local cores unknown or outside this process's set)"
+        elif local == allowed:
+            self.note = "pinned, allocated on the GPU-local cores (all %d of this process's)" % len(local)
+        else:
+            try:
+                os.sched_setaffinity(0, local)
+                self.saved = allowed
+                self.note = "pinned, allocated on the %d GPU-local cores of this process's %d" % (len(local),
+                                                                                                  len(allowed))
+            except OSError:
+                self.note = "pinned (could not bind to the GPU's local cores)"
+        return self
+
+    def __exit__(self, *exc):
+        if self.saved is not None:
+            os.sched_setaffinity(0, self.saved)
+        return False
+
+
 def profile_traffic(name):
     """DRAM bytes per launch from profiles/<name>.txt ('traffic_bytes_per_launch: N'), else None."""
     try:
@@ -538,8 +595,9 @@ def run_sgemm(ctx):
     by_mode = ctx.per_mode_ms(MODES)
     compare["speedup_vs_simt"] = value / ctx.world / compare["simt_tflops"]
 
-    pin = {k: v.cpu().pin_memory() for k, v in bufs.items()}
-    hostC = [torch.empty((M, LD), dtype=torch.float32).pin_memory() for _ in range(2)]
+    with near_gpu(torch, torch.cuda.current_device()) as placed:
+        pin = {k: v.cpu().pin_memory() for k, v in bufs.items()}
+        hostC = [torch.empty((M, LD), dtype=torch.float32).pin_memory() for _ in range(2)]
     nbytes = M * LD * 4
     # End to end, pipelined over the four modes as a caller would: mode i+1's operands go up on
     # one stream while mode i computes and mode i-1's C comes down on another (the host link
@@ -621,7 +679,7 @@ def run_sgemm(ctx):
               "l2": "inputs larger than L2 (8 operand buffers of 67 MB + C per step)"}
     line = base_line(ctx, METRIC, value, "TFLOP/s", ms, args.steps, "f32", config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
                  "gpu_launches": launches, "clocks": clocks, "errors_normwise": errors, "err_report": report,
                  "compare": compare})
     if ctx.rank == 0 and not args.no_cpu_baseline:
@@ -754,8 +812,9 @@ def run_dgemm(ctx):
     roof["traffic"] = profile_traffic("dgemm_ozaki_8192")
     roof["kernel_ms"] = kms
     nbytes = n * n * 8
-    pin = {k: v.cpu().pin_memory() for k, v in bufs.items()}
-    hostC = torch.empty((n, n), dtype=torch.float64).pin_memory()
+    with near_gpu(torch, torch.cuda.current_device()) as placed:
+        pin = {k: v.cpu().pin_memory() for k, v in bufs.items()}
+        hostC = torch.empty((n, n), dtype=torch.float64).pin_memory()
 
     def step_host():
         h2d = d2h = 0
@@ -775,7 +834,7 @@ def run_dgemm(ctx):
               "parallelism": "replicas x%d" % ctx.world, "l2": "inputs larger than L2 (5 x 512 MB)"}
     line = base_line(ctx, METRIC, value, "TFLOP/s", ms, args.steps, "f64", config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
                  "gpu_launches": launches, "clocks": clocks, "precision_study": study})
     if ctx.rank == 0 and not args.no_cpu_baseline:
         v, nt, desc = cpu_dgemm_sample()
@@ -846,8 +905,9 @@ def run_skinny(ctx):
                     "compute_frac": tflops / cpeak, "kernel_ms": kms, "kernel_ms_by_mode": ctx.per_mode_ms(MODES),
                     "peak_note_compute": "%s peak measured on this GPU (gb_measure_fma_peak)"
                                          % ("DFMA" if bits == 64 else "FFMA")})
-    hostbufs = {m: (ops[m][0].cpu().pin_memory(), ops[m][2].cpu().pin_memory()) for m in MODES}
-    hostC = C.cpu().pin_memory()
+    with near_gpu(torch, torch.cuda.current_device()) as placed:
+        hostbufs = {m: (ops[m][0].cpu().pin_memory(), ops[m][2].cpu().pin_memory()) for m in MODES}
+        hostC = C.cpu().pin_memory()
 
     def step_host():
         h2d = d2h = 0
@@ -869,7 +929,7 @@ def run_skinny(ctx):
               "l2": "inputs larger than L2 (large operand %d MB)" % (s * big * K // 10 ** 6)}
     line = base_line(ctx, "HBM GB/s (%s)" % args.workload, value, "GB/s", ms, args.steps, "f%d" % bits, config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
                  "gpu_launches": launches, "clocks": clocks})
     if ctx.rank == 0 and not args.no_cpu_baseline:
         v, nt, desc = cpu_bw_sample("skinny", bits)
@@ -905,8 +965,9 @@ def run_transpose(ctx):
     ms, kms, clocks, launches = ctx.timed(step, args.steps)
     value = aggregate(ctx.world, args.steps, nbytes, ms) / 1e9
     roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "transpose_f%d_%s" % (bits, args.shape), {"kernel_ms": kms})
-    hA = A.cpu().pin_memory()
-    hB = torch.empty_like(B, device="cpu").pin_memory()
+    with near_gpu(torch, torch.cuda.current_device()) as placed:
+        hA = A.cpu().pin_memory()
+        hB = torch.empty_like(B, device="cpu").pin_memory()
 
     def step_host():
         memcpy(ctx, A, hA, A.numel() * s, 0)
@@ -919,7 +980,7 @@ def run_transpose(ctx):
               "parallelism": "replicas x%d" % ctx.world, "l2": "inputs larger than L2"}
     line = base_line(ctx, "HBM GB/s (transpose)", value, "GB/s", ms, args.steps, "f%d" % bits, config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
                  "gpu_launches": launches, "clocks": clocks})
     if ctx.rank == 0 and not args.no_cpu_baseline:
         v, nt, desc = cpu_bw_sample("transpose", bits)
@@ -973,8 +1034,9 @@ def run_jacobi(ctx):
                       "compute_frac": gflops / ctx.fma_peak[64], "compute_peak_note": "DFMA peak measured on this GPU"})
     roof = bw_roof(ctx, nbytes / (kms * 1e-3) / 1e9, None, "%s_f%d_8192" % ("stencil9" if nine else "jacobi", bits),
                    extra)
-    hA = A0.cpu().pin_memory()
-    hR = torch.empty_like(A, device="cpu").pin_memory()
+    with near_gpu(torch, torch.cuda.current_device()) as placed:
+        hA = A0.cpu().pin_memory()
+        hR = torch.empty_like(A, device="cpu").pin_memory()
 
     def step_host():
         memcpy(ctx, A, hA, A.numel() * s, 0)
@@ -992,7 +1054,7 @@ def run_jacobi(ctx):
     line = base_line(ctx, "HBM GB/s (%s)" % ("stencil9" if nine else "jacobi"), value, "GB/s", ms, args.steps,
                      "f%d" % bits, config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
                  "gpu_launches": launches, "clocks": clocks})
     if ctx.rank == 0 and not args.no_cpu_baseline and not nine:
         v, nt, desc = cpu_bw_sample("jacobi", bits)

@@ -71,3 +71,28 @@ def test_reference_arm_other_ranks_exit_quietly():
                         "--warmup", "3"], env=env, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_parse_cpulist():
+    sys.path.insert(0, REPO)
+    import bench
+    assert bench.parse_cpulist("0-3,8,10-11\n") == {0, 1, 2, 3, 8, 10, 11}
+    assert bench.parse_cpulist("5") == {5}
+    assert bench.parse_cpulist("") == set()
+
+
+def test_near_gpu_leaves_affinity_alone_when_local_cores_unknown():
+    sys.path.insert(0, REPO)
+    import bench
+
+    class NoProps:   # a torch whose device properties carry no PCI ids
+        class cuda:
+            @staticmethod
+            def get_device_properties(dev):
+                raise AttributeError("no PCI ids")
+
+    before = os.sched_getaffinity(0)
+    with bench.near_gpu(NoProps, 0) as placed:
+        assert os.sched_getaffinity(0) == before
+    assert os.sched_getaffinity(0) == before
+    assert "unknown" in placed.note
