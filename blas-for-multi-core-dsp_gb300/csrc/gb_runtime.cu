@@ -327,6 +327,7 @@ const char *gb_status_string(int status) {
 
 int gb_get_last_status(void) { return t_status; }
 const char *gb_last_error(void) { return t_msg; }
+const char *gb_last_error_string(void) { return t_msg; }
 void gb_clear_last_status(void) {
     t_status = GB_OK;
     t_msg[0] = 0;

@@ -208,6 +208,26 @@ int gb_gemm_pick_algo(int dtype_bits, char transA, char transB, int64_t M, int64
     return gb::pick(dtype_bits, gb::is_trans(transA), gb::is_trans(transB), M, N, K);
 }
 
+gb_status gb_workspace_query(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
+                             const void *A, int64_t lda, const void *B, int64_t ldb, const gb_gemm_opts *opts,
+                             size_t *bytes) {
+    GB_CHECK_ARG(bytes != nullptr, "gb_workspace_query: bytes is NULL");
+    *bytes = 0;
+    GB_CHECK_ARG(dtype_bits == 32 || dtype_bits == 64, "gb_workspace_query: dtype_bits %d", dtype_bits);
+    GB_CHECK_ARG(gb::is_mode(transA) && gb::is_mode(transB), "gb_workspace_query: transA/transB must be 'N' or 'T'");
+    GB_CHECK_ARG(M >= 0 && N >= 0 && K >= 0, "gb_workspace_query: negative dimension");
+    gb_gemm_opts o;
+    if (opts) o = *opts;
+    else gb_gemm_opts_init(&o);
+    GB_CHECK_ARG(o.ozaki_slices == 0 || (o.ozaki_slices >= 2 && o.ozaki_slices <= 9),
+                 "gb_workspace_query: ozaki_slices %d not in 2..9", o.ozaki_slices);
+    GB_CHECK_ARG(o.target_err >= 0.0, "gb_workspace_query: negative target_err");
+    const bool ta = gb::is_trans(transA), tb = gb::is_trans(transB);
+    const int slices = o.ozaki_slices > 0 ? o.ozaki_slices : gb::ozaki_pick_slices(o.target_err, K);
+    *bytes = gb::gemm_workspace_bound(dtype_bits, o.algo, ta, tb, M, N, K, A, lda, B, ldb, slices, o.split_k);
+    return gb::ok();
+}
+
 gb_status gb_sgemm(char transA, char transB, int64_t M, int64_t N, int64_t K, float alpha, const float *A,
                    int64_t lda, const float *B, int64_t ldb, float beta, float *C, int64_t ldc,
                    const gb_gemm_opts *opts) {

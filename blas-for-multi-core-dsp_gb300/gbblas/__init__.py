@@ -101,6 +101,7 @@ _SIGS = {
     "gb_status_string": ([_int], ctypes.c_char_p),
     "gb_get_last_status": ([], _int),
     "gb_last_error": ([], ctypes.c_char_p),
+    "gb_last_error_string": ([], ctypes.c_char_p),
     "gb_clear_last_status": ([], None),
     "gb_version": ([], _int),
     "gb_launch_count": ([], ctypes.c_uint64),
@@ -130,6 +131,8 @@ _SIGS = {
     "gb_exec": ([ctypes.c_char_p, _int, _int, ctypes.POINTER(_ul)], _int),
     "gb_ref_set_stream": ([_vp], None),
     "gb_workspace_reserve": ([ctypes.c_size_t, _vp], _int),
+    "gb_workspace_query": ([_int, ctypes.c_char, ctypes.c_char, _i64, _i64, _i64, _vp, _i64, _vp, _i64,
+                            ctypes.POINTER(GemmOpts), ctypes.POINTER(ctypes.c_size_t)], _int),
     "gb_selftest_bounded_wait": ([ctypes.c_uint64, _vp], _int),
     "gb_measure_fma_peak": ([_int, ctypes.POINTER(ctypes.c_double), _vp], _int),
     "gb_gemm_batch": ([ctypes.POINTER(GemmDesc), _int, _vp], _int),
@@ -268,6 +271,19 @@ def gemm(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, dtype_bits, **kw)
 
 def pick_algo(bits, ta, tb, M, N, K):
     return lib().gb_gemm_pick_algo(bits, ta.encode(), tb.encode(), M, N, K)
+
+
+def workspace_query(bits, ta, tb, M, N, K, lda, ldb, A=None, B=None, **kw):
+    """Workspace bytes the gb_sgemm / gb_dgemm call with these arguments and options may use."""
+    o = opts(**kw)
+    n = ctypes.c_size_t(0)
+    _check(lib().gb_workspace_query(bits, ta.encode(), tb.encode(), M, N, K, _ptr(A), lda, _ptr(B), ldb,
+                                    ctypes.byref(o), ctypes.byref(n)), "gb_workspace_query")
+    return n.value
+
+
+def workspace_reserve(nbytes, stream=None):
+    _check(lib().gb_workspace_reserve(nbytes, _stream(stream)), "gb_workspace_reserve")
 
 
 def transpose(M, N, A, lda, B, ldb, bits, stream=None):

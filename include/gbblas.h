@@ -42,6 +42,7 @@ const char *gb_status_string(int status);
 /* Status and message of the last failing call on this host thread. */
 int         gb_get_last_status(void);
 const char *gb_last_error(void);
+const char *gb_last_error_string(void);   /* the same message (alias) */
 void        gb_clear_last_status(void);
 
 /* Library version and the device it runs on (major*10+minor, e.g. 103). */
@@ -212,6 +213,19 @@ gb_status gb_sgemm_skinny_noalloc(char transA, char transB, int64_t M, int64_t N
 
 /* Algorithm that GB_ALGO_AUTO picks for a shape (for logging/tests). */
 int gb_gemm_pick_algo(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K);
+
+/* Workspace bytes (the library-owned scratch of the call's stream) that the
+ * gb_sgemm (dtype_bits 32) / gb_dgemm (64) call with these arguments and
+ * options may use: the 16-bit operand pieces of BF16X3 / BF16X6 / FP16X3, the
+ * skinny products' split-K parts, the Ozaki slices; 0 for the forms that need
+ * none.  opts as the call's (NULL: the defaults; algo AUTO resolves as the
+ * call would; ozaki_slices 0 takes the count target_err picks); A and B are
+ * read only for their alignment, and NULL stands for 16-byte aligned.
+ * Reserving the figure with gb_workspace_reserve before capturing such a call
+ * into a CUDA graph keeps the capture from needing to grow the buffer. */
+gb_status gb_workspace_query(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
+                             const void *A, int64_t lda, const void *B, int64_t ldb,
+                             const gb_gemm_opts *opts, size_t *bytes);
 
 /* ------------------------------------------------------ grouped GEMM */
 /* One GEMM of a batch (same meaning as the gb_sgemm / gb_dgemm arguments). */

@@ -133,3 +133,30 @@ def test_headers_compile_and_link(lang, tmp_path):
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
     assert subprocess.run([out], capture_output=True).returncode == 0
+
+
+def test_workspace_query_two_pass_forms_and_validation(L):
+    """The workspace bound of the split-operand forms is the two halves of
+    up to three 16-bit pieces per operand value (K padded to 64); forms that
+    keep no scratch report 0; bad arguments are refused like a call's."""
+    M, N, K = 1000, 700, 900
+    kp = (K + 63) // 64 * 64
+    want = 2 * (3 * (M + N) * kp * 2 + (M + N) * 4 + 1024) + 4096
+    for algo in (gbblas.ALGO_BF16X3, gbblas.ALGO_BF16X6, gbblas.ALGO_FP16X3):
+        assert gbblas.workspace_query(32, "N", "T", M, N, K, K, K, algo=algo) == want
+    assert gbblas.workspace_query(32, "N", "N", M, N, K, K, N, algo=gbblas.ALGO_SIMT) == 0
+    assert gbblas.workspace_query(64, "T", "N", M, N, K, M, N, algo=gbblas.ALGO_ORDERED) == 0
+    assert gbblas.workspace_query(32, "N", "N", 0, N, K, K, N, algo=gbblas.ALGO_BF16X3) == 0
+    n = ctypes.c_size_t(7)
+    o = gbblas.opts()
+    assert L.gb_workspace_query(16, b"N", b"N", 4, 4, 4, None, 4, None, 4, ctypes.byref(o),
+                                ctypes.byref(n)) == gbblas.ERR_INVALID_ARG
+    assert b"dtype_bits" in L.gb_last_error() and n.value == 0
+    assert L.gb_workspace_query(32, b"X", b"N", 4, 4, 4, None, 4, None, 4, ctypes.byref(o),
+                                ctypes.byref(n)) == gbblas.ERR_INVALID_ARG
+    assert L.gb_last_error_string() == L.gb_last_error()
+    o = gbblas.opts(algo=gbblas.ALGO_OZAKI, ozaki_slices=1)
+    assert L.gb_workspace_query(64, b"N", b"N", 4, 4, 4, None, 4, None, 4, ctypes.byref(o),
+                                ctypes.byref(n)) == gbblas.ERR_INVALID_ARG
+    assert L.gb_workspace_query(32, b"N", b"N", 4, 4, 4, None, 4, None, 4, ctypes.byref(o),
+                                None) == gbblas.ERR_INVALID_ARG
