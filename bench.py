@@ -1203,6 +1203,7 @@ def run_serve(ctx):
                 "grouped_launches": st["grouped_launches"], "grouped_requests": st["grouped_requests"],
                 "graph_launches": st["graph_launches"], "graph_instantiations": st["graph_instantiations"],
                 "graph_fraction": st["graph_launches"] / st["launches"] if st["launches"] else 0.0,
+                "urgent_launches": st["urgent_launches"],
                 "drained": drained, "submit_lag_s": lag, "submit_span_s": submit_end, "by_class": by_class}
 
     l0 = gb.launch_count()

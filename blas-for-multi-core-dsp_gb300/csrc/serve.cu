@@ -112,6 +112,7 @@ struct Server {
     std::vector<std::map<GKey, cudaGraphExec_t>> execs;       // one-launch graphs per stream
     std::set<GKey> seen;                                      // buckets that ran once without a graph
     std::atomic<int64_t> graph_launches{0}, graph_instantiations{0};
+    int64_t urgent_launches = 0;   // launches on the high-priority streams (under mu)
     size_t rr = 0, rr_short = 0;
     GroupRunner *grouped = nullptr;
     std::thread dispatcher;
@@ -317,6 +318,11 @@ double estimate_us(const gb_request &r) {
     return 2.0 * es * M * N * (double)std::max(r.iters, 1) / 8e6 + 5.0;   // Jacobi sweeps
 }
 
+// Streams 0..short_streams-1 carry the short requests when priorities are on.
+bool urgent_stream(const Server *s, size_t si) {
+    return s->streams.size() >= 2 && s->cfg.short_us > 0 && si < (size_t)s->cfg.short_streams;
+}
+
 // Short requests round-robin over the high-priority streams 0..h-1, the rest over h..n-1 (every
 // stream in turn when there is one stream or priorities are off).
 size_t pick_stream(Server *s, double est_us) {
@@ -370,7 +376,7 @@ void dispatcher_main(Server *s) {
             const size_t si = pick_stream(s, est);
             // a long request on the normal streams plans for a share of the SMs only
             const bool capped = s->cfg.long_sm_percent < 100 && s->cfg.short_us > 0 && est >= s->cfg.short_us &&
-                                s->streams.size() >= 2;
+                                s->streams.size() >= 2 && !s->cfg.dry_run;
             if (capped) {
                 set_sm_cap(0);
                 set_sm_cap((int)((int64_t)sm_count() * s->cfg.long_sm_percent / 100));
@@ -389,9 +395,11 @@ void dispatcher_main(Server *s) {
             else cudaLaunchHostFunc(st, on_done, b);
             std::lock_guard<std::mutex> g(s->mu);
             s->launches++;
+            if (urgent_stream(s, si)) s->urgent_launches++;
         }
         if (!group.empty()) {
-            cudaStream_t st = s->streams[pick_stream(s, 0.0)];   // grouped launches are short
+            const size_t gsi = pick_stream(s, 0.0);   // grouped launches are short
+            cudaStream_t st = s->streams[gsi];
             Batch *b = new Batch{s, {}, 0};
             for (auto &p : group_reqs) {
                 b->reqs.push_back({p.r.tag, p.t_submit});
@@ -409,6 +417,7 @@ void dispatcher_main(Server *s) {
             else cudaLaunchHostFunc(st, on_done, b);
             std::lock_guard<std::mutex> g(s->mu);
             s->launches++;
+            if (urgent_stream(s, gsi)) s->urgent_launches++;
             if (rc == GB_OK && s->cfg.use_graphs && !s->cfg.dry_run) s->graph_launches++;
             s->grouped_launches++;
             s->grouped_requests += (int64_t)group.size();
@@ -490,10 +499,12 @@ gb_status gb_server_create(const gb_server_config *cfg, gb_server **out) {
             }
         }
         s->grouped = gb::group_runner_create(2 * c.streams, c.max_batch);
-    } else {
-        s->streams.push_back(nullptr);
-        s->ws_reserved.push_back(0);
-        s->execs.emplace_back();
+    } else {   // no device work: the streams are placeholders, so that routing runs as it would
+        for (int i = 0; i < c.streams; i++) {
+            s->streams.push_back(nullptr);
+            s->ws_reserved.push_back(0);
+            s->execs.emplace_back();
+        }
     }
     s->dispatcher = std::thread(gb::dispatcher_main, s);
     *out = reinterpret_cast<gb_server *>(s);
@@ -576,6 +587,7 @@ gb_status gb_server_get_stats(gb_server *sv, gb_server_stats *out) {
     out->grouped_requests = s->grouped_requests;
     out->graph_launches = s->graph_launches.load();
     out->graph_instantiations = s->graph_instantiations.load();
+    out->urgent_launches = s->urgent_launches;
     out->p50_s = gb::percentile(s->latencies, 0.50);
     out->p99_s = gb::percentile(s->latencies, 0.99);
     out->mean_s = 0;

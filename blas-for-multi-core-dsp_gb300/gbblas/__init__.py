@@ -90,7 +90,7 @@ class ServerStats(ctypes.Structure):
                 ("grouped_launches", ctypes.c_int64), ("grouped_requests", ctypes.c_int64),
                 ("p50_s", ctypes.c_double), ("p99_s", ctypes.c_double), ("mean_s", ctypes.c_double),
                 ("req_per_s", ctypes.c_double), ("graph_launches", ctypes.c_int64),
-                ("graph_instantiations", ctypes.c_int64)]
+                ("graph_instantiations", ctypes.c_int64), ("urgent_launches", ctypes.c_int64)]
 
 
 OP_GEMM, OP_TRANSPOSE, OP_STENCIL = range(3)

@@ -378,6 +378,7 @@ typedef struct gb_server_stats {
     double   p50_s, p99_s, mean_s, req_per_s;
     int64_t  graph_launches;        /* launches that replayed a CUDA graph (grouped and one-launch)    */
     int64_t  graph_instantiations;  /* one-launch graphs built (the rest were cached graphs updated)   */
+    int64_t  urgent_launches;       /* launches on the high-priority streams (short requests, groups) */
 } gb_server_stats;
 
 typedef struct gb_server gb_server;

@@ -128,3 +128,21 @@ def test_gemm_batch_rejects_bad_descriptors(L):
     arr = (gbblas.GemmDesc * 1)(d)
     assert L.gb_gemm_batch(arr, 1, None) == gbblas.ERR_INVALID_ARG
     assert L.gb_gemm_batch(None, 0, None) == gbblas.OK
+
+
+@pytest.mark.parametrize("streams,short_streams,short_us,urgent", [(6, 2, 200.0, 10), (6, 2, 0.0, 0), (1, 2, 200.0, 0)])
+def test_short_requests_go_to_the_urgent_streams(L, streams, short_streams, short_us, urgent):
+    """Requests estimated below short_us (small transposes) are routed to the high-priority
+    streams and long ones (a 2048^3 FP64 product) to the others; with priorities off (short_us 0)
+    or a single stream nothing is urgent."""
+    with gbblas.Server(dry_run=1, streams=streams, short_streams=short_streams, short_us=short_us,
+                       use_grouped=0) as s:
+        for i in range(10):
+            s.submit(gbblas.request(gbblas.OP_TRANSPOSE, 32, 256, 256, A=16, lda=256, B=32, ldb=256, tag=i))
+        for i in range(7):
+            s.submit(gbblas.request(gbblas.OP_GEMM, 64, 2048, 2048, 2048, A=16, lda=2048, B=32, ldb=2048, C=48,
+                                    ldc=2048, algo=gbblas.ALGO_OZAKI, tag=100 + i))
+        s.drain(10.0)
+        st = s.stats()
+        assert st["completed"] == 17 and st["launches"] == 17
+        assert st["urgent_launches"] == urgent
