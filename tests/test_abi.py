@@ -160,3 +160,30 @@ def test_workspace_query_two_pass_forms_and_validation(L):
                                 ctypes.byref(n)) == gbblas.ERR_INVALID_ARG
     assert L.gb_workspace_query(32, b"N", b"N", 4, 4, 4, None, 4, None, 4, ctypes.byref(o),
                                 None) == gbblas.ERR_INVALID_ARG
+
+
+@pytest.mark.parametrize("lang", ["c99", "c++17"])
+def test_serving_loop_from_c_dry_run(lang, tmp_path):
+    """The serving calls and the workspace query from a C (and C++) program,
+    on a dry-run server: struct layouts, defaults, routing to the urgent
+    streams and the statistics as the header declares them."""
+    import shutil
+    import subprocess
+    import gbblas
+    if not os.path.exists(gbblas.LIB_PATH):
+        pytest.skip("libgbblas.so not built")
+    cc = "gcc" if lang == "c99" else "g++"
+    if not shutil.which(cc):
+        pytest.skip(cc + " not found")
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = os.path.join(repo, "tests", "c", "server_dryrun.c")
+    flags = ["-std=c99", "-x", "c"] if lang == "c99" else ["-std=c++17", "-x", "c++"]
+    out = str(tmp_path / "server_dryrun")
+    libdir = os.path.dirname(gbblas.LIB_PATH)
+    r = subprocess.run([cc] + flags + ["-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(repo, "include"),
+                        src, "-x", "none", "-L" + libdir, "-lgbblas", "-Wl,-rpath," + libdir, "-o", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    run = subprocess.run([out], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, (run.returncode, run.stdout, run.stderr)
+    assert "server dry run ok" in run.stdout
