@@ -220,7 +220,9 @@ int gb_gemm_pick_algo(int dtype_bits, char transA, char transB, int64_t M, int64
  * skinny products' split-K parts, the Ozaki slices; 0 for the forms that need
  * none.  opts as the call's (NULL: the defaults; algo AUTO resolves as the
  * call would; ozaki_slices 0 takes the count target_err picks); A and B are
- * read only for their alignment, and NULL stands for 16-byte aligned.
+ * read only for their alignment, and NULL stands for 16-byte aligned.  The
+ * Ozaki figure includes scratch per SM of the current device: query with the
+ * device that will run the call current.
  * Reserving the figure with gb_workspace_reserve before capturing such a call
  * into a CUDA graph keeps the capture from needing to grow the buffer. */
 gb_status gb_workspace_query(int dtype_bits, char transA, char transB, int64_t M, int64_t N, int64_t K,
