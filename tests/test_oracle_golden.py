@@ -119,3 +119,46 @@ def test_stencil9_reduces_to_weighted_sum():
             ref += w[di * 3 + dj] * A[di:di + M, dj:dj + N]
     assert np.allclose(b[1:M + 1, 1:N + 1], ref, rtol=0, atol=1e-14)
     assert np.array_equal(b[0], B[0]) and np.array_equal(b[:, 0], B[:, 0])
+
+
+@pytest.mark.parametrize("spread,seed", [(0, 1), (20, 2), (60, 3)])
+def test_dot2_within_its_published_bound_against_exact_rationals(spread, seed):
+    """The accuracy oracle itself: Dot2 (Ogita, Rump & Oishi 2005, Prop. 5.5) satisfies
+    |dot2 - x.y| <= u |x.y| + gamma_{n-1}^2 sum |x_i y_i| (u = 2^-53, gamma_k = k u / (1 - k u));
+    checked against the exact dot product in rational arithmetic, on entries u * 2^e with e
+    spread over [-spread, spread] as in the DGEMM precision study."""
+    from fractions import Fraction
+    rng = np.random.default_rng(seed)
+    K, rows, cols = 400, 3, 4
+    A = rng.uniform(-1, 1, size=(rows, K)) * np.exp2(rng.integers(-spread, spread + 1, size=(rows, K)))
+    B = rng.uniform(-1, 1, size=(K, cols)) * np.exp2(rng.integers(-spread, spread + 1, size=(K, cols)))
+    ref = oracle.gemm_dot2("N", "N", rows, cols, K, 1.0, A, K, B, cols, 0.0, None, cols, np.arange(rows),
+                           np.arange(cols))
+    u = Fraction(1, 2 ** 53)
+    g = (K - 1) * u / (1 - (K - 1) * u)
+    for i in range(rows):
+        for j in range(cols):
+            exact = sum(Fraction(float(A[i, k])) * Fraction(float(B[k, j])) for k in range(K))
+            absum = sum(abs(Fraction(float(A[i, k])) * Fraction(float(B[k, j]))) for k in range(K))
+            err = abs(Fraction(float(ref[i, j])) - exact)
+            assert err <= u * abs(exact) + g * g * absum, (i, j, float(err), float(exact))
+
+
+def test_normwise_metric_matches_its_definition():
+    """normwise_error = ||C - C*||_F / (|alpha| ||op(A)||_F ||op(B)||_F + |beta| ||C0||_F) on the
+    sampled rows / columns, recomputed here from numpy norms."""
+    rng = np.random.default_rng(5)
+    M, N, K = 20, 15, 30
+    A = rng.uniform(-1, 1, size=(M, K))
+    B = rng.uniform(-1, 1, size=(K, N))
+    C0 = rng.uniform(-1, 1, size=(M, N))
+    alpha, beta = 1.5, -0.5
+    rows, cols = np.array([0, 3, 7, 19]), np.array([1, 2, 14])
+    ref = oracle.gemm_dot2("N", "N", M, N, K, alpha, A, K, B, N, beta, C0, N, rows, cols)
+    got = ref + 1e-6 * rng.standard_normal(ref.shape)
+    C_hat = np.zeros((M, N))
+    C_hat[np.ix_(rows, cols)] = got
+    e, _ = oracle.normwise_error(C_hat, "N", "N", M, N, K, alpha, A, K, B, N, beta, C0, N, rows, cols)
+    den = abs(alpha) * np.linalg.norm(A[rows]) * np.linalg.norm(B[:, cols]) + abs(beta) * np.linalg.norm(
+        C0[np.ix_(rows, cols)])
+    assert e == pytest.approx(np.linalg.norm(got - ref) / den, rel=1e-12)
