@@ -79,3 +79,37 @@ def test_wrapper_signature_matches_header(name):
     for i, (p, a) in enumerate(zip(params, args)):
         assert _c_kind(p) == _py_kind(a), (name, i, p, a)
     assert _c_kind(ret) == _py_kind(res), (name, ret, res)
+
+
+STRUCTS = {"gb_gemm_opts": "GemmOpts", "gb_tune_choice": "TuneChoice", "gb_gemm_desc": "GemmDesc",
+           "gb_request": "Request", "gb_server_config": "ServerConfig", "gb_server_stats": "ServerStats"}
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """sizeof and every member's offset of the structs the wrapper mirrors, as the C compiler
+    lays them out from the header, against the ctypes layouts."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not found")
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gbblas.h"', 'int main(void) {']
+    for cname, pyname in STRUCTS.items():
+        lines.append('    printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in getattr(gbblas, pyname)._fields_:
+            lines.append('    printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ['    return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(REPO, "include"), str(src), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = {}
+    for line in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines():
+        c, f, v = line.split()
+        got[(c, f)] = int(v)
+    for cname, pyname in STRUCTS.items():
+        cls = getattr(gbblas, pyname)
+        assert got[(cname, "sizeof")] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
