@@ -345,19 +345,28 @@ def memcpy(ctx, dst, src, nbytes, kind, stream=None):
     assert st == 0, ctx.gb.lib().gb_last_error()
 
 
-def e2e_measure(ctx, step_host, steps, flops_or_bytes, unit_div):
-    """Time step_host() (copies + compute through the C ABI) `steps` times."""
+E2E_RUNS = 3
+E2E_TIMING = "median of %d timed runs of the steps (slowest rank each), after one untimed step" % E2E_RUNS
+
+
+def e2e_measure(ctx, step_host, steps, flops_or_bytes, unit_div, runs=E2E_RUNS):
+    """Time step_host() (copies + compute through the C ABI) `steps` times, `runs` times over;
+    the median run's rate (one run of a few steps is short enough for a burst of other traffic
+    on the host side to decide it)."""
     step_host()
     ctx.torch.cuda.synchronize()
     ctx.barrier()
-    t0, t1 = ctx.event(), ctx.event()
-    t0.record(ctx.stream)
-    for _ in range(steps):
-        h2d, d2h = step_host()
-    t1.record(ctx.stream)
-    ctx.torch.cuda.synchronize()
-    ms = ctx.max_over_ranks(t0.elapsed_time(t1))
-    return aggregate(ctx.world, steps, flops_or_bytes, ms) / unit_div, h2d, d2h
+    rates = []
+    for _ in range(runs):
+        t0, t1 = ctx.event(), ctx.event()
+        t0.record(ctx.stream)
+        for _ in range(steps):
+            h2d, d2h = step_host()
+        t1.record(ctx.stream)
+        ctx.torch.cuda.synchronize()
+        ms = ctx.max_over_ranks(t0.elapsed_time(t1))
+        rates.append(aggregate(ctx.world, steps, flops_or_bytes, ms) / unit_div)
+    return statistics.median(rates), h2d, d2h
 
 
 # ================================================================== CPU legs
@@ -679,7 +688,8 @@ def run_sgemm(ctx):
               "l2": "inputs larger than L2 (8 operand buffers of 67 MB + C per step)"}
     line = base_line(ctx, METRIC, value, "TFLOP/s", ms, args.steps, "f32", config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note,
+                                           "timing": E2E_TIMING},
                  "gpu_launches": launches, "clocks": clocks, "errors_normwise": errors, "err_report": report,
                  "compare": compare})
     if ctx.rank == 0 and not args.no_cpu_baseline:
@@ -834,7 +844,8 @@ def run_dgemm(ctx):
               "parallelism": "replicas x%d" % ctx.world, "l2": "inputs larger than L2 (5 x 512 MB)"}
     line = base_line(ctx, METRIC, value, "TFLOP/s", ms, args.steps, "f64", config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note,
+                                           "timing": E2E_TIMING},
                  "gpu_launches": launches, "clocks": clocks, "precision_study": study})
     if ctx.rank == 0 and not args.no_cpu_baseline:
         v, nt, desc = cpu_dgemm_sample()
@@ -929,7 +940,8 @@ def run_skinny(ctx):
               "l2": "inputs larger than L2 (large operand %d MB)" % (s * big * K // 10 ** 6)}
     line = base_line(ctx, "HBM GB/s (%s)" % args.workload, value, "GB/s", ms, args.steps, "f%d" % bits, config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note,
+                                           "timing": E2E_TIMING},
                  "gpu_launches": launches, "clocks": clocks})
     if ctx.rank == 0 and not args.no_cpu_baseline:
         v, nt, desc = cpu_bw_sample("skinny", bits)
@@ -980,7 +992,8 @@ def run_transpose(ctx):
               "parallelism": "replicas x%d" % ctx.world, "l2": "inputs larger than L2"}
     line = base_line(ctx, "HBM GB/s (transpose)", value, "GB/s", ms, args.steps, "f%d" % bits, config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note,
+                                           "timing": E2E_TIMING},
                  "gpu_launches": launches, "clocks": clocks})
     if ctx.rank == 0 and not args.no_cpu_baseline:
         v, nt, desc = cpu_bw_sample("transpose", bits)
@@ -1054,7 +1067,8 @@ def run_jacobi(ctx):
     line = base_line(ctx, "HBM GB/s (%s)" % ("stencil9" if nine else "jacobi"), value, "GB/s", ms, args.steps,
                      "f%d" % bits, config)
     line.update({"roofline": roof, "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note},
+                                           "d2h_bytes_per_step": d2h, "host_buffers": placed.note,
+                                           "timing": E2E_TIMING},
                  "gpu_launches": launches, "clocks": clocks})
     if ctx.rank == 0 and not args.no_cpu_baseline and not nine:
         v, nt, desc = cpu_bw_sample("jacobi", bits)

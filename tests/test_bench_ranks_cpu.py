@@ -96,3 +96,49 @@ def test_near_gpu_leaves_affinity_alone_when_local_cores_unknown():
         assert os.sched_getaffinity(0) == before
     assert os.sched_getaffinity(0) == before
     assert "unknown" in placed.note
+
+
+def test_e2e_measure_reports_the_median_run():
+    """e2e_measure: one untimed step, then `runs` timed runs of `steps` steps each; the rate of
+    the median run (a fake context whose events read a simulated clock)."""
+    sys.path.insert(0, REPO)
+    import bench
+
+    clock = [0.0]
+
+    class Ev:
+        def record(self, stream):
+            self.t = clock[0]
+
+        def elapsed_time(self, other):
+            return other.t - self.t
+
+    class FakeTorch:
+        class cuda:
+            @staticmethod
+            def synchronize():
+                pass
+
+    class FakeCtx:
+        torch, stream, world = FakeTorch, None, 1
+
+        def event(self):
+            return Ev()
+
+        def barrier(self):
+            pass
+
+        def max_over_ranks(self, ms):
+            return ms
+
+    # ms per step: the untimed one, then three runs of two steps (20, 60 and 40 ms per run)
+    per_step = iter([1.0, 10.0, 10.0, 30.0, 30.0, 20.0, 20.0])
+
+    def step_host():
+        clock[0] += next(per_step)
+        return 100, 200
+
+    rate, h2d, d2h = bench.e2e_measure(FakeCtx(), step_host, 2, 1e9, 1e9)
+    assert rate == pytest.approx(2 * 1e9 / 40e-3 / 1e9)   # the 40 ms run
+    assert (h2d, d2h) == (100, 200)
+    assert bench.E2E_RUNS == 3 and "median" in bench.E2E_TIMING
