@@ -216,7 +216,9 @@ int gb_gemm_pick_algo(int dtype_bits, char transA, char transB, int64_t M, int64
 
 /* Workspace bytes (the library-owned scratch of the call's stream) that the
  * gb_sgemm (dtype_bits 32) / gb_dgemm (64) call with these arguments and
- * options may use: the 16-bit operand pieces of BF16X3 / BF16X6 / FP16X3, the
+ * options may use (no reference counterpart: the reference's kernels work in
+ * fixed on-chip buffers, e.g. the static GSM array of
+ * sgemm_release_V1.3.2/device_code/sgemm_kernel.c:17): the 16-bit operand pieces of BF16X3 / BF16X6 / FP16X3, the
  * skinny products' split-K parts, the Ozaki slices; 0 for the forms that need
  * none.  opts as the call's (NULL: the defaults; algo AUTO resolves as the
  * call would; ozaki_slices 0 takes the count target_err picks); A and B are
